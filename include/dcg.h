@@ -1,0 +1,243 @@
+/*
+ * dcg.h — C ABI of the GB300-native DCGrid simulation step.
+ *
+ * This header replaces the reference's C++ simulation interface
+ *   FluidSimulation (src/fluid_simulation.h:4-27),
+ *   FluidSimulationDCGrid(const int3&, const size_t&)  (src/dcgrid/fluid_simulation_dcgrid.h:7),
+ *   FluidSimulationUniform(const int3&)                 (src/uniformgrid/fluid_simulation_uniform.h:7),
+ *   copySimParamsToDevice(SimParams&)                   (src/utils/sim_utils.h:5-6)
+ * with plain functions over an opaque handle. Every call returns an int status
+ * (DCG_OK or a DCG_E_* code) instead of calling exit(1) as the reference does
+ * (src/dcgrid/fluid_simulation_dcgrid.cu:35-53, include/cuda/helper_cuda.h:761-790).
+ *
+ * Threading: one handle is not thread-safe; separate handles are independent.
+ * All device work of a handle is issued on that handle's CUDA stream.
+ */
+#ifndef DCG_H
+#define DCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  DCG_OK = 0,
+  DCG_E_INVALID = 1,   /* bad argument / unsupported configuration            */
+  DCG_E_BUDGET = 2,    /* block budget cannot hold the coarsest level or L0   */
+  DCG_E_HASH_FULL = 3, /* reserved: no hash exists in this implementation     */
+  DCG_E_CUDA = 4,      /* a CUDA runtime call failed                          */
+  DCG_E_TIMEOUT = 5,   /* a bounded device-side wait gave up                  */
+  DCG_E_NAN = 6,       /* a non-finite value was produced                     */
+  DCG_E_NOT_FOUND = 7, /* no such field / handle state                        */
+  DCG_E_DEVICE = 8     /* device-side error word was set (see error string)   */
+};
+
+/* ---- grid type (the reference's adaptive/uniform switch,
+ *      src/simulation.cpp:32-35,52-64) -------------------------------------- */
+enum { DCG_MODE_ADAPTIVE = 0, DCG_MODE_UNIFORM = 1 };
+
+/* ---- solids / scene SDF (src/sdf.cuh:8-20, src/utils/sim_utils.cu:11-22) - */
+enum {
+  DCG_SOLIDS_NONE = 0,    /* enable_additional_solids = false                */
+  DCG_SOLIDS_SPHERE = 1,  /* the reference's sphere obstacle                 */
+  DCG_SOLIDS_TERRAIN = 2, /* extension: heightfield terrain, y - h(x,z)      */
+  DCG_SOLIDS_BOTH = 3
+};
+
+/* ---- refinement criterion --------------------------------------------- */
+enum {
+  DCG_REFINE_GEOMETRIC = 0, /* src/dcgrid/dcgrid_adaptation.cu:26-34          */
+  DCG_REFINE_FIELDS = 1     /* extension: |curl v| and |grad rho| thresholds */
+};
+
+/* ---- storage precision of the advected scalars ------------------------ */
+enum { DCG_PRECISION_FP32 = 0, DCG_PRECISION_MIXED = 1 };
+
+/*
+ * Simulation parameters. Units follow the reference's SimParams
+ * (src/data/sim_params.h:14-47): positions in finest-level cells, velocities in
+ * world units per time unit, dx = world size of one finest cell (rdx = 1/dx).
+ * Unlike the reference's single __constant__ SimParams, every handle owns its
+ * own copy, so simulations in one process may differ.
+ */
+typedef struct dcg_params {
+  int32_t gx, gy, gz;    /* domain size in finest cells                      */
+  int32_t levels;        /* 0 = derive as the reference does (cu:12-22)      */
+  int64_t max_blocks;    /* block budget (the reference's maxNumBlocks)      */
+  float dt;              /* time step                                        */
+  float dx;              /* world size of a finest cell                      */
+
+  /* reference inlet BC (src/utils/sim_utils.cu:24-55) */
+  int32_t inlet_enabled;
+  float velocity_emission_rate;
+  float density_emission_rate;
+  float emission_radius; /* world units                                      */
+
+  /* solids / fluidity */
+  int32_t solids;            /* DCG_SOLIDS_*                                 */
+  float sphere_radius_world; /* reference: 2000 world units (sdf.cuh:12)     */
+
+  /* solver */
+  int32_t jacobi_iters;      /* sweeps per level; reference: 10 (5 pairs)    */
+  int32_t init_adapt_passes; /* reference: 5 (fluid_simulation_dcgrid.cu:207) */
+
+  /* adaptation */
+  int32_t refine_criterion;  /* DCG_REFINE_*                                 */
+  float refine_threshold;    /* reference: 1e-4 (cu:461)                     */
+  float vort_threshold;      /* extension: |curl v| scale                    */
+  float grad_threshold;      /* extension: |grad rho| scale                  */
+  int32_t ref_compat;        /* 1 = reproduce the reference's selection quirks */
+
+  /* extension: scalars, buoyancy, sources, wind */
+  int32_t n_scalars;         /* 1 = density (reference); 3 = density, temperature, vapor */
+  float buoy_alpha, buoy_beta, t_ambient;
+  int32_t src_enabled;       /* sphere source, values set every step          */
+  float src_center[3];       /* finest cells                                 */
+  float src_radius;          /* finest cells                                 */
+  float src_density, src_temperature, src_vapor;
+  int32_t wind_enabled;      /* inflow at x<0, zero-gradient outflow at x>=gx */
+  float wind[3];             /* world units per time unit                     */
+
+  /* extension: terrain SDF from seeded value noise */
+  float terrain_amplitude;   /* finest cells                                 */
+  float terrain_base_height; /* finest cells                                 */
+  float terrain_frequency;   /* lattice frequency of the first octave, 1/cells */
+  float terrain_persistence;
+  int32_t terrain_octaves;
+  uint32_t terrain_seed;
+
+  int32_t precision;         /* DCG_PRECISION_*                              */
+  int32_t reserved[8];
+} dcg_params;
+
+/* Fills *p with the reference's defaults (src/data/sim_params.cpp:4-34) for a
+ * gx*gy*gz domain and the reference's solver/adaptation constants. */
+void dcg_default_params(dcg_params *p, int32_t gx, int32_t gy, int32_t gz,
+                        int64_t max_blocks);
+
+/* ---- fields ------------------------------------------------------------ */
+enum {
+  DCG_FIELD_DENSITY = 0,
+  DCG_FIELD_VEL_X = 1,
+  DCG_FIELD_VEL_Y = 2,
+  DCG_FIELD_VEL_Z = 3,
+  DCG_FIELD_FLUIDITY = 4,
+  DCG_FIELD_PRESSURE = 5,
+  DCG_FIELD_PRESSURE_TMP = 6,
+  DCG_FIELD_DIVERGENCE = 7,
+  DCG_FIELD_TEMPERATURE = 8,
+  DCG_FIELD_VAPOR = 9,
+  DCG_FIELD_COUNT = 10
+};
+enum { DCG_HOST = 0, DCG_DEVICE = 1 };
+
+/* Static description of a handle. Arrays hold up to 16 levels. */
+typedef struct dcg_info {
+  int32_t mode;
+  int32_t levels;
+  int32_t sparse_levels;       /* levels [0, sparse_levels) are hashed in the reference */
+  int32_t n_scalars;
+  int64_t max_blocks;          /* block pool size                               */
+  int64_t num_cells;           /* 64 * max_blocks (adaptive) or gx*gy*gz (uniform) */
+  int64_t full_blocks[16];     /* blocks that cover the whole domain per level  */
+  int64_t budget[16];          /* maxNumBlocksLevel                             */
+  int64_t offset[16];          /* levelOffsets                                  */
+  int64_t device_bytes;        /* bytes of device memory held by the handle     */
+} dcg_info;
+
+/* Per-step counters (the reference's debugStats, cu:517-529, plus more). */
+typedef struct dcg_stats {
+  int64_t load[16];            /* allocated blocks per level                   */
+  int64_t leaf_cells[16];      /* cells whose subblock has no child, per level */
+  int64_t active_cells;        /* sum of leaf_cells                             */
+  int64_t moved_blocks;        /* by the last adaptation                        */
+  int64_t refined_subblocks;   /* by the last adaptation                        */
+  int64_t steps;
+  double residual;             /* sum scale*|div - lap p| over leaf cells      */
+  double mass;                 /* sum rho*fluidity*scale^3 over leaf cells     */
+  uint32_t device_error;       /* device error word (DCG_DEVERR_* bits)         */
+  uint32_t pad;
+} dcg_stats;
+
+enum {
+  DCG_DEVERR_BUDGET = 1u,      /* a refinement found its level full             */
+  DCG_DEVERR_LOOKUP = 2u,      /* a block lookup failed                         */
+  DCG_DEVERR_NAN = 4u,
+  DCG_DEVERR_TIMEOUT = 8u
+};
+
+typedef struct dcg_sim dcg_sim;
+
+/* ---- lifecycle (FluidSimulationDCGrid ctor/dtor/reset/init,
+ *      fluid_simulation_dcgrid.cu:9-261; FluidSimulationUniform ctor,
+ *      fluid_simulation_uniform.cu:6-54) ------------------------------------ */
+int dcg_create(const dcg_params *params, int32_t mode, dcg_sim **out);
+int dcg_destroy(dcg_sim *sim);
+int dcg_reset(dcg_sim *sim);               /* FluidSimulation::reset (+ init)    */
+int dcg_set_params(dcg_sim *sim, const dcg_params *params); /* copySimParamsToDevice;
+                                               geometry/budget must not change */
+int dcg_set_mode(dcg_sim **sim, int32_t mode); /* the N-key switch: recreate,
+                                               state not transferred (simulation.cpp:52-64) */
+int dcg_set_stream(dcg_sim *sim, void *cuda_stream);
+int dcg_get_info(const dcg_sim *sim, dcg_info *info);
+const char *dcg_last_error_string(const dcg_sim *sim);
+
+/* ---- the step and its stages (simulation.cpp:104-112; stage bodies in
+ *      fluid_simulation_dcgrid.cu:263-346 and fluid_simulation_uniform.cu:62-142) */
+int dcg_step(dcg_sim *sim, int32_t n);     /* n x {advect_velocity, adapt, project, advect_scalars} */
+int dcg_advect_velocity(dcg_sim *sim);     /* + buoyancy when enabled                */
+int dcg_adapt(dcg_sim *sim);               /* adaptTopology                          */
+int dcg_project(dcg_sim *sim);             /* cascadic Jacobi projection             */
+int dcg_project_local(dcg_sim *sim);       /* projectLocal                           */
+int dcg_advect_scalars(dcg_sim *sim);      /* advectDensity (+ temperature, vapor, sources) */
+int dcg_sync(dcg_sim *sim);                /* wait for the handle's stream; read device error word */
+
+/* Adds seeded uniform noise in [-amplitude, amplitude] to every velocity
+ * component of every allocated cell (deterministic counter-based hash). */
+int dcg_add_velocity_noise(dcg_sim *sim, uint64_t seed, float amplitude);
+
+/* ---- field and topology access (no counterpart in the reference: fields are
+ *      private there, fluid_simulation_dcgrid.h:59-60) ----------------------- */
+/* Canonical layout: adaptive = block-major, cell c of block b at b*64 + c with
+ * the reference's local order (subblock bits x,y,z then cell bits x,y,z,
+ * dcgrid_utils.cuh:69-81); uniform = x-fastest dense array. fp32 only. */
+int dcg_get_field(dcg_sim *sim, int32_t field, float *dst, int32_t where);
+int dcg_set_field(dcg_sim *sim, int32_t field, const float *src, int32_t where);
+/* Dense gx*gy*gz x-fastest resampling: each finest cell takes the value of the
+ * leaf cell that covers it. */
+int dcg_get_dense(dcg_sim *sim, int32_t field, float *dst, int32_t where);
+
+/* Block table, host buffers sized by dcg_info.max_blocks:
+ *   pos[4*b] = x, y, z (level-local cells), level (-1 = free)
+ *   parent[b] = 8*parentBlock + subblock or 0xFFFFFFFF
+ *   child[8*b + s] = child block or 0xFFFFFFFF
+ *   flags[b] (1 = moved, 2 = refined by the last adaptation)
+ *   load[L], move_limit[L] per level.
+ * Any pointer may be NULL. set_topology rebuilds neighbour tables. */
+int dcg_get_topology(dcg_sim *sim, int32_t *pos, uint32_t *parent,
+                     uint32_t *child, uint8_t *flags, int64_t *load,
+                     int64_t *move_limit);
+int dcg_set_topology(dcg_sim *sim, const int32_t *pos, const uint32_t *parent,
+                     const uint32_t *child, const int64_t *load,
+                     const int64_t *move_limit);
+/* The reference's 6x6x6 apron index table per block (dcgrid.h:22), derived
+ * from the neighbour tables: dst[216*b + 36*i + 6*j + k] = global cell index,
+ * -1 for free blocks. Host buffer of 216*max_blocks entries. */
+int dcg_get_apron(dcg_sim *sim, int64_t *dst);
+
+/* Decisions of the last dcg_adapt: moves (block, destination subblock) and
+ * refinements (subblock, new block) in application order. Counts are returned
+ * in *n_moves / *n_refines; buffers may be NULL to query counts only. */
+int dcg_get_last_adapt(dcg_sim *sim, int64_t *moves, int64_t *n_moves,
+                       int64_t *refines, int64_t *n_refines);
+
+int dcg_get_stats(dcg_sim *sim, dcg_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DCG_H */
