@@ -1,0 +1,13 @@
+"""GB300-native DCGrid adaptive-grid simulation step.
+
+The compute path is the CUDA library libdcgrid_gb300.so (C ABI in
+include/dcg.h); this package holds its sources (csrc/), the build script and
+a ctypes host API mirroring the reference's simulation interface.
+"""
+from . import capi
+from .capi import DcgInfo, DcgParams, DcgStats
+from .sim import (DcgError, FluidSimulationDCGrid, FluidSimulationUniform, Simulation,
+                  default_params, lib)
+
+__all__ = ["capi", "DcgParams", "DcgInfo", "DcgStats", "DcgError", "Simulation",
+           "FluidSimulationDCGrid", "FluidSimulationUniform", "default_params", "lib"]

@@ -94,7 +94,9 @@ class DcgParams(C.Structure):
         ("terrain_octaves", C.c_int32),
         ("terrain_seed", C.c_uint32),
         ("precision", C.c_int32),
-        ("reserved", C.c_int32 * 8),
+        ("emission_n", C.c_int32),
+        ("emission_band", C.c_float),
+        ("reserved", C.c_int32 * 6),
     ]
 
 

@@ -1,0 +1,322 @@
+// dcg_dev.cuh — device-side data layout and helpers of the GB300 DCGrid step.
+//
+// Layout in HBM (one simulation):
+//   block table (SoA over the block pool of max_blocks entries)
+//     pos[b]      int4  {x, y, z, level}   level-local cell coords, level -1 = free
+//     parent[b]   u32   8*parentBlock + subblock, or NONE
+//     child[8b+s] u32   child block of subblock s, or NONE
+//     nbr[27b+d]  u32   neighbour of direction d (26 used, d=13 is the block):
+//                       (leveldiff << 28) | block, or OUT (outside the domain)
+//     flags[b]    u8    1 = moved, 2 = refined by the current adaptation
+//   fields: float planes of 64*max_blocks cells, cell c of block b at 64*b + c,
+//   c = subblock(x,y,z bits) * 8 + cell(x,y,z bits) as in the reference
+//   (src/dcgrid/dcgrid_utils.cuh:67-81).
+// The 26-entry neighbour table replaces the reference's 216-entry apron index
+// table (src/dcgrid/dcgrid.h:22): an apron cell is resolved from its
+// direction's neighbour block; a coarser neighbour is sampled by injection,
+// the coarse cell that contains the apron cell (dcgrid_structure.cu:85-91).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dcg {
+
+constexpr int BW = 4, BV = 64, AW = 6;
+constexpr uint32_t NONE = 0xFFFFFFFFu;
+constexpr uint32_t OUT = 0xFFFFFFFFu;
+constexpr uint32_t NBR_MASK = 0x0FFFFFFFu;
+constexpr int MAXL = 16;
+constexpr uint8_t MOVED = 1, REFINED = 2;
+
+// device counters (adaptation bookkeeping), indices into Dev::ctr
+enum : int {
+  C_MOVES = 0,        // moves recorded so far in this adaptation
+  C_REFINES = 1,      // refinements recorded
+  C_TOUCHED = 2,      // moved + new blocks
+  C_MOVE_LIMIT = 3,   // scratch: limit l of the level being matched
+  C_MATCHES = 4,      // scratch: first failing pair of the level being matched
+  C_NCAND = 5,        // scratch: candidate count of a compaction
+  C_MOVE_BEGIN = 16,  // [16 + L]: first move of level L
+  C_MOVE_END = 32,    // [32 + L]
+  C_REF_BEGIN = 48,   // [48 + L]: first refinement creating blocks of level L
+  C_REF_END = 64,     // [64 + L]
+  C_LOAD0 = 80,       // [80 + L]: load of level L before this adaptation's refinements
+  C_COUNT = 128
+};
+
+struct Geom {
+  int gx, gy, gz, levels, sparse, nq, ref_compat, mixed;
+  long long B;
+  long long full[MAXL], budget[MAXL], off[MAXL];
+  int rx[MAXL], ry[MAXL], rz[MAXL];
+};
+
+struct Phys {
+  float dt, dx, rdx;
+  int inlet;
+  float v_emit, d_emit, emit_radius;
+  int solids;
+  float sphere_r;
+  int criterion;
+  float refine_threshold, vort_t, grad_t;
+  float buoy_a, buoy_b, t_amb;
+  int src;
+  float src_c[3], src_r, src_val[3];
+  int wind;
+  float wind_v[3];
+  float ter_amp, ter_base, ter_freq, ter_pers;
+  int ter_oct;
+  unsigned ter_seed;
+  int em_n;
+  float em_band;
+  const float *em;  // em_n^3 emission field (device), or null
+};
+
+struct Dev {
+  Geom g;
+  Phys ph;
+  int4 *pos;
+  uint32_t *parent, *child, *nbr;
+  uint8_t *flags;
+  long long *load, *move_limit;
+  float *q[3], *tq[3], *v[3], *tv[3];
+  float *w, *p, *pt, *div;
+  float *ss, *bs;          // subblock / block scores (8B+1, B)
+  uint32_t *moves;         // (block, dest) pairs
+  uint32_t *refines;       // (subblock, new block) pairs
+  uint32_t *touched;       // moved + new blocks
+  long long *ctr;          // C_COUNT counters
+  uint32_t *err;           // device error word
+  double *red;             // reductions (stats)
+};
+
+// ---------------------------------------------------------------- index math
+__host__ __device__ inline int spread2(int d, int off) { return ((d & 1) | ((d << 2) & 8)) << off; }
+__host__ __device__ inline int local_of(int x, int y, int z) {
+  return spread2(x, 2) + spread2(y, 1) + spread2(z, 0);
+}
+__host__ __device__ inline void local_xyz(int c, int &x, int &y, int &z) {
+  const int sub = c >> 3;
+  x = (((sub >> 2) & 1) << 1) | ((c >> 2) & 1);
+  y = (((sub >> 1) & 1) << 1) | ((c >> 1) & 1);
+  z = ((sub & 1) << 1) | (c & 1);
+}
+__host__ __device__ inline int clampi(int v, int a, int b) { return v < a ? a : (v > b ? b : v); }
+__device__ inline float clampf_(float v, float a, float b) { return v < a ? a : (v > b ? b : v); }
+
+__device__ inline uint32_t dense_index(const Geom &g, int x, int y, int z, int level) {
+  return (uint32_t)(g.off[level] + ((long long)(x >> 2) * g.ry[level] + (y >> 2)) * g.rz[level] + (z >> 2));
+}
+
+// Finest allocated block at a level >= L that contains level-L cell q: the
+// result of getBlockIndexDeep (dcgrid_utils.cuh:201-233), found here by
+// descending the child pointers from the finest dense level.
+__device__ inline uint32_t locate(const Dev &D, int qx, int qy, int qz, int L, int &lev) {
+  const int S = D.g.sparse;
+  if (L >= S) {
+    lev = L;
+    return dense_index(D.g, qx, qy, qz, L);
+  }
+  uint32_t b = dense_index(D.g, qx >> (S - L), qy >> (S - L), qz >> (S - L), S);
+  int l = S;
+  while (l > L) {
+    const int4 bp = D.pos[b];
+    const int sh = l - L;
+    const int lx = (qx >> sh) - bp.x, ly = (qy >> sh) - bp.y, lz = (qz >> sh) - bp.z;
+    const uint32_t ch = D.child[8u * b + ((((lx >> 1) & 1) << 2) | (((ly >> 1) & 1) << 1) | ((lz >> 1) & 1))];
+    if (ch == NONE) break;
+    b = ch;
+    l--;
+  }
+  lev = l;
+  return b;
+}
+
+// Descends from block b at level l to the finest block containing level-0 cell q.
+__device__ inline uint32_t descend(const Dev &D, uint32_t b, int &l, int qx, int qy, int qz) {
+  while (l > 0) {
+    const int4 bp = D.pos[b];
+    const int lx = (qx >> l) - bp.x, ly = (qy >> l) - bp.y, lz = (qz >> l) - bp.z;
+    const uint32_t ch = D.child[8u * b + ((((lx >> 1) & 1) << 2) | (((ly >> 1) & 1) << 1) | ((lz >> 1) & 1))];
+    if (ch == NONE) break;
+    b = ch;
+    l--;
+  }
+  return b;
+}
+
+__device__ inline int dir_of(int a) { return a == 0 ? 0 : (a == AW - 1 ? 2 : 1); }
+
+// Global cell index of apron cell (ax, ay, az) in [0,6)^3 of block b.
+// Out-of-domain apron cells map to one of the block's own cells: the clamped
+// cell, or - for blocks of hashed levels in compat mode - the cell the
+// reference's refresh writes, SPREAD(clamp(a,1,4)) = clamp(a,1,4) mod 4
+// (dcgrid_structure.cu:55-61).
+__device__ inline unsigned long long apron_cell(const Dev &D, uint32_t b, int4 bp, int ax, int ay,
+                                                int az) {
+  const int d = dir_of(ax) * 9 + dir_of(ay) * 3 + dir_of(az);
+  if (d == 13) return (unsigned long long)b * BV + local_of(ax - 1, ay - 1, az - 1);
+  const uint32_t e = D.nbr[27u * b + d];
+  if (e == OUT) {
+    if (D.g.ref_compat && bp.w < D.g.sparse)
+      return (unsigned long long)b * BV +
+             local_of(clampi(ax, 1, BW) & 3, clampi(ay, 1, BW) & 3, clampi(az, 1, BW) & 3);
+    return (unsigned long long)b * BV +
+           local_of(clampi(ax, 1, BW) - 1, clampi(ay, 1, BW) - 1, clampi(az, 1, BW) - 1);
+  }
+  const uint32_t nb = e & NBR_MASK;
+  const int k = (int)(e >> 28);
+  const int cx = bp.x + ax - 1, cy = bp.y + ay - 1, cz = bp.z + az - 1;
+  return (unsigned long long)nb * BV + local_of((cx >> k) & 3, (cy >> k) & 3, (cz >> k) & 3);
+}
+
+// ---------------------------------------------------------------- physics
+// All float expressions below keep the operation order of the reference
+// (src/utils/sim_utils.cu, src/sdf.cuh); the library is compiled with
+// -fmad=false so no multiply-add is fused.
+__device__ inline uint32_t hash32(uint32_t seed, int32_t i, int32_t k, int32_t o) {
+  uint32_t h = seed ^ 0x9E3779B9u;
+  h ^= (uint32_t)i * 0x85EBCA6Bu; h = (h ^ (h >> 15)) * 0x2C1B3C6Du;
+  h ^= (uint32_t)k * 0xC2B2AE35u; h = (h ^ (h >> 13)) * 0x297A2D39u;
+  h ^= (uint32_t)o * 0x27D4EB2Fu; h = (h ^ (h >> 16)) * 0x85EBCA77u;
+  return h ^ (h >> 15);
+}
+__device__ inline unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ inline float noise_unit(unsigned long long seed, int x, int y, int z, int level, int comp) {
+  unsigned long long h = mix64(seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(comp + 1));
+  h = mix64(h ^ ((unsigned long long)(uint32_t)x * 0xD6E8FEB86659FD93ull));
+  h = mix64(h ^ ((unsigned long long)(uint32_t)y * 0xA0761D6478BD642Full));
+  h = mix64(h ^ ((unsigned long long)(uint32_t)z * 0xE7037ED1A0B428DBull));
+  h = mix64(h ^ (unsigned long long)(uint32_t)level);
+  const float u = (float)(uint32_t)(h >> 40) * (1.0f / 16777216.0f);
+  return 2.0f * u - 1.0f;
+}
+
+__device__ inline float terrain_height(const Phys &P, float x, float z) {
+  float sum = 0.f, amp = 1.f, norm = 0.f, f = P.ter_freq;
+  for (int o = 0; o < P.ter_oct; o++) {
+    const float u = x * f, v = z * f;
+    const float iu = floorf(u), iv = floorf(v);
+    const float fu = u - iu, fv = v - iv;
+    const float su = fu * fu * (3.f - 2.f * fu);
+    const float sv = fv * fv * (3.f - 2.f * fv);
+    const int i0 = (int)iu, k0 = (int)iv;
+    const float unit = 1.0f / 16777216.0f;
+    const float a = (float)(hash32(P.ter_seed, i0, k0, o) >> 8) * unit;
+    const float b = (float)(hash32(P.ter_seed, i0 + 1, k0, o) >> 8) * unit;
+    const float c = (float)(hash32(P.ter_seed, i0, k0 + 1, o) >> 8) * unit;
+    const float d = (float)(hash32(P.ter_seed, i0 + 1, k0 + 1, o) >> 8) * unit;
+    const float ab = a + (b - a) * su;
+    const float cd = c + (d - c) * su;
+    sum = sum + amp * (ab + (cd - ab) * sv);
+    norm = norm + amp;
+    amp = amp * P.ter_pers;
+    f = f * 2.f;
+  }
+  return P.ter_base + P.ter_amp * (sum / norm);
+}
+
+// sceneSDF (src/sdf.cuh:8-20) + terrain extension
+__device__ inline float scene_sdf(const Geom &g, const Phys &P, float x, float y, float z) {
+  float d = 3.402823466e+38f;
+  if (P.solids & 1) {
+    const float cx = (float)g.gx * 0.5f, cy = (float)g.gy * 0.45f, cz = (float)g.gz * 0.5f;
+    const float r = P.sphere_r * P.rdx;
+    const float ddx = x - cx, ddy = y - cy, ddz = z - cz;
+    d = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz) - r;
+  }
+  if (P.solids & 2) {
+    const float t = y - terrain_height(P, x, z);
+    d = fminf(d, t);
+  }
+  return d;
+}
+
+// getCellFluidity (src/utils/sim_utils.cu:11-22)
+__device__ inline float fluidity(const Geom &g, const Phys &P, int x, int y, int z, int scale) {
+  if (P.solids == 0) return 1.f;
+  const float s = (float)scale;
+  const float d = scene_sdf(g, P, ((float)x + 0.5f) * s, ((float)y + 0.5f) * s, ((float)z + 0.5f) * s);
+  const float overlap = clampf_(0.5f - d / (s * 1.73205f), 0.f, 1.f);
+  return 1.f - overlap;
+}
+
+__device__ inline bool in_inlet(const Geom &g, const Phys &P, int x, int y, int z, int scale) {
+  if (!P.inlet || y >= 0) return false;
+  const float a = (float)(x * scale) - 0.5f * (float)g.gx;
+  const float b = (float)(z * scale) - 0.5f * (float)g.gz;
+  return sqrtf(a * a + b * b) < P.emit_radius * P.rdx;
+}
+__device__ inline bool outside(const Geom &g, int x, int y, int z, int scale) {
+  return x < 0 || y < 0 || z < 0 || x * scale >= g.gx || y * scale >= g.gy || z * scale >= g.gz;
+}
+__device__ inline bool yz_inside(const Geom &g, int y, int z, int scale) {
+  return y >= 0 && z >= 0 && y * scale < g.gy && z * scale < g.gz;
+}
+// velocityBndCond (sim_utils.cu:24-39) + wind extension
+__device__ inline void vel_bc(const Geom &g, const Phys &P, float &vx, float &vy, float &vz, int x,
+                              int y, int z, int scale) {
+  if (in_inlet(g, P, x, y, z, scale)) {
+    vx = 0.f; vy = P.v_emit; vz = 0.f;
+    return;
+  }
+  if (P.wind && yz_inside(g, y, z, scale)) {
+    if (x < 0) { vx = P.wind_v[0]; vy = P.wind_v[1]; vz = P.wind_v[2]; return; }
+    if (x * scale >= g.gx) return;
+  }
+  if (outside(g, x, y, z, scale)) vx = vy = vz = 0.f;
+}
+// densityBndCond (sim_utils.cu:41-55) + wind extension; scalar k
+__device__ inline float q_bc(const Geom &g, const Phys &P, float q, int k, int x, int y, int z,
+                             int scale) {
+  if (in_inlet(g, P, x, y, z, scale)) return k == 0 ? P.d_emit : 0.f;
+  if (P.wind && yz_inside(g, y, z, scale)) {
+    if (x < 0) return 0.f;
+    if (x * scale >= g.gx) return q;
+  }
+  if (outside(g, x, y, z, scale)) return 0.f;
+  return q;
+}
+__device__ inline bool in_source(const Phys &P, int x, int y, int z, int scale) {
+  if (!P.src) return false;
+  const float s = (float)scale;
+  const float cx = ((float)x + 0.5f) * s - P.src_c[0];
+  const float cy = ((float)y + 0.5f) * s - P.src_c[1];
+  const float cz = ((float)z + 0.5f) * s - P.src_c[2];
+  return cx * cx + cy * cy + cz * cz < P.src_r * P.src_r;
+}
+
+// Emission field (extension): trilinear sample of the em_n^3 field over
+// x in [0,gx), y in [0,em_band), z in [0,gz) at the centre of cell (x,y,z) of
+// a level with cell size `scale`; 0 outside the band.
+__device__ inline float em_lerp(float a, float b, float t) { return a + (b - a) * t; }
+__device__ inline float emission_at(const Geom &g, const Phys &P, int x, int y, int z, int scale) {
+  if (P.em_n <= 0 || !P.em) return 0.f;
+  const float s = (float)scale;
+  const float yw = ((float)y + 0.5f) * s;
+  if (!(yw < P.em_band)) return 0.f;
+  const float xw = ((float)x + 0.5f) * s, zw = ((float)z + 0.5f) * s;
+  const int n = P.em_n;
+  const float top = (float)(n - 1);
+  const float u = clampf_(xw * ((float)n / (float)g.gx) - 0.5f, 0.f, top);
+  const float v = clampf_(yw * ((float)n / P.em_band) - 0.5f, 0.f, top);
+  const float w = clampf_(zw * ((float)n / (float)g.gz) - 0.5f, 0.f, top);
+  const int i0 = (int)floorf(u), j0 = (int)floorf(v), k0 = (int)floorf(w);
+  const int i1 = i0 + 1 < n ? i0 + 1 : n - 1, j1 = j0 + 1 < n ? j0 + 1 : n - 1, k1 = k0 + 1 < n ? k0 + 1 : n - 1;
+  const float fu = u - (float)i0, fv = v - (float)j0, fw = w - (float)k0;
+  const float *E = P.em;
+  auto at = [&](int i, int j, int k) { return E[((size_t)k * n + j) * n + i]; };
+  const float e00 = em_lerp(at(i0, j0, k0), at(i1, j0, k0), fu);
+  const float e10 = em_lerp(at(i0, j1, k0), at(i1, j1, k0), fu);
+  const float e01 = em_lerp(at(i0, j0, k1), at(i1, j0, k1), fu);
+  const float e11 = em_lerp(at(i0, j1, k1), at(i1, j1, k1), fu);
+  return em_lerp(em_lerp(e00, e10, fv), em_lerp(e01, e11, fv), fw);
+}
+
+__device__ inline void set_err(const Dev &D, uint32_t bits) { atomicOr(D.err, bits); }
+
+}  // namespace dcg

@@ -1,0 +1,66 @@
+// dcg_kernels.h — host-side launchers of the device kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "dcg_dev.cuh"
+
+namespace dcg {
+
+struct FieldList {
+  float *f[6];
+  int n;
+};
+
+// stable LSD radix sort of (key, value) u32 pairs; scratch sized by sort_scratch_words
+struct SortScratch {
+  uint32_t *k1, *v1;   // ping-pong buffers (n)
+  uint32_t *hist;      // 256 * tiles
+  uint32_t *totals;    // 256
+  uint32_t *tile_sums; // tiles (compaction)
+  long long max_n;
+};
+long long sort_tiles(long long n);
+void launch_radix_sort(uint32_t *keys, uint32_t *vals, long long n, const SortScratch &s,
+                       const long long *active, cudaStream_t st);
+
+// k_fluid.cu
+void launch_advect_velocity(const Dev &D, cudaStream_t st);
+void launch_advect_scalars(const Dev &D, cudaStream_t st);
+void launch_sources(const Dev &D, cudaStream_t st);
+void launch_add_noise(const Dev &D, unsigned long long seed, float amp, cudaStream_t st);
+void launch_restrict(const Dev &D, const FieldList &fl, cudaStream_t st);
+void launch_divergence(const Dev &D, cudaStream_t st);
+void launch_jacobi(const Dev &D, int level, const float *src, float *dst, cudaStream_t st);
+void launch_prolongate(const Dev &D, int level, cudaStream_t st);
+void launch_apply_pressure(const Dev &D, cudaStream_t st);
+
+// k_topology.cu
+void launch_init_blocks(const Dev &D, cudaStream_t st);
+void launch_activate_level(const Dev &D, int level, cudaStream_t st);
+void launch_build_nbr(const Dev &D, bool only_if_touched, cudaStream_t st);
+void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *vals,
+                  uint32_t *keys2, uint32_t *vals2, int sms, cudaStream_t st);
+void launch_stats(const Dev &D, cudaStream_t st);
+void launch_fields_to_dense(const Dev &D, const float *src, float *dst, cudaStream_t st);
+void launch_apron_table(const Dev &D, long long *dst, cudaStream_t st);
+
+// k_uniform.cu — uniform (dense, mip-mapped) grid
+struct UDev {
+  int gx, gy, gz, levels, nq, ref_compat, pad0, pad1;
+  long long nc, nmip;
+  long long mip_off[MAXL];
+  Phys ph;
+  Geom g;  // gx/gy/gz for the shared boundary-condition helpers
+  float *q[3], *tq[3], *v[3], *tv[3];
+  float *w, *p, *pt, *div;
+  double *red;
+};
+void launch_u_fluidity(const UDev &U, cudaStream_t st);
+void launch_u_sources(const UDev &U, cudaStream_t st);
+void launch_u_advect_velocity(const UDev &U, cudaStream_t st);
+void launch_u_advect_scalars(const UDev &U, cudaStream_t st);
+void launch_u_project(const UDev &U, int top_pairs, int pairs, bool local, cudaStream_t st);
+void launch_u_add_noise(const UDev &U, unsigned long long seed, float amp, cudaStream_t st);
+void launch_u_stats(const UDev &U, cudaStream_t st);
+
+}  // namespace dcg

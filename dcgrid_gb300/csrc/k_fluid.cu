@@ -1,0 +1,381 @@
+// k_fluid.cu — field stages of the adaptive step: semi-Lagrangian advection
+// (+ buoyancy / sources), divergence, Jacobi, prolongation, pressure gradient,
+// fine-to-coarse restriction.
+//
+// Thread mapping: 256-thread CTAs, 4 blocks per CTA, one thread per cell; a
+// warp covers half a block (4 subblocks, 32 contiguous floats = 128 B), so
+// every field plane is read and written in full 128-byte lines.
+#include "dcg_dev.cuh"
+#include "dcg_kernels.h"
+
+namespace dcg {
+
+struct Smp {
+  unsigned long long idx[8];
+  float wt[8];
+  float wAcc;
+  int x0, y0, z0, x1, y1, z1, scale;
+};
+
+// INIT_SAMPLE (src/dcgrid/dcgrid_fluid.cu:7-72): locate the finest block that
+// holds the back-traced point, then trilinear weights x fluidity, renormalised.
+// The block is found from the advected cell's own block through its neighbour
+// table and child pointers (no hash probes); points more than one block away
+// fall back to a descent from the finest dense level.
+__device__ inline void sample_at(const Dev &D, uint32_t b0, int4 bp0, float pxw, float pyw, float pzw,
+                                 Smp &s) {
+  const int ix = clampi((int)floorf(pxw), 0, D.g.gx - 1);
+  const int iy = clampi((int)floorf(pyw), 0, D.g.gy - 1);
+  const int iz = clampi((int)floorf(pzw), 0, D.g.gz - 1);
+  const int L0 = bp0.w;
+  const int ddx = ((ix >> L0) >> 2) - (bp0.x >> 2);
+  const int ddy = ((iy >> L0) >> 2) - (bp0.y >> 2);
+  const int ddz = ((iz >> L0) >> 2) - (bp0.z >> 2);
+  uint32_t b = NONE;
+  int lev = L0;
+  if (ddx >= -1 && ddx <= 1 && ddy >= -1 && ddy <= 1 && ddz >= -1 && ddz <= 1) {
+    if ((ddx | ddy | ddz) == 0) {
+      b = b0;
+    } else {
+      const uint32_t e = D.nbr[27u * b0 + (ddx + 1) * 9 + (ddy + 1) * 3 + (ddz + 1)];
+      if (e != OUT) {
+        b = e & NBR_MASK;
+        lev = L0 + (int)(e >> 28);
+      }
+    }
+    if (b != NONE && lev == L0) b = descend(D, b, lev, ix, iy, iz);
+  }
+  if (b == NONE) b = locate(D, ix, iy, iz, 0, lev);
+  const int4 bp = (b == b0) ? bp0 : D.pos[b];
+  s.scale = 1 << lev;
+  const float scaleInv = 1.f / (float)s.scale;
+  const float x = pxw * scaleInv - 0.5f, y = pyw * scaleInv - 0.5f, z = pzw * scaleInv - 0.5f;
+  const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+  const float dx = x - xf, dy = y - yf, dz = z - zf;
+  s.x0 = (int)xf; s.y0 = (int)yf; s.z0 = (int)zf;
+  s.x1 = s.x0 + 1; s.y1 = s.y0 + 1; s.z1 = s.z0 + 1;
+  const int i = clampi(s.x1 - bp.x, 0, AW - 2);
+  const int j = clampi(s.y1 - bp.y, 0, AW - 2);
+  const int k = clampi(s.z1 - bp.z, 0, AW - 2);
+#pragma unroll
+  for (int c = 0; c < 8; c++)
+    s.idx[c] = apron_cell(D, b, bp, i + ((c >> 2) & 1), j + ((c >> 1) & 1), k + (c & 1));
+  const float Dx = 1.f - dx, Dy = 1.f - dy, Dz = 1.f - dz;
+  s.wt[0] = D.w[s.idx[0]] * Dx * Dy * Dz;
+  s.wt[1] = D.w[s.idx[1]] * Dx * Dy * dz;
+  s.wt[2] = D.w[s.idx[2]] * Dx * dy * Dz;
+  s.wt[3] = D.w[s.idx[3]] * Dx * dy * dz;
+  s.wt[4] = D.w[s.idx[4]] * dx * Dy * Dz;
+  s.wt[5] = D.w[s.idx[5]] * dx * Dy * dz;
+  s.wt[6] = D.w[s.idx[6]] * dx * dy * Dz;
+  s.wt[7] = D.w[s.idx[7]] * dx * dy * dz;
+  s.wAcc = s.wt[0] + s.wt[1] + s.wt[2] + s.wt[3] + s.wt[4] + s.wt[5] + s.wt[6] + s.wt[7];
+  const float wInv = 1.f / s.wAcc;
+#pragma unroll
+  for (int c = 0; c < 8; c++) s.wt[c] = s.wt[c] * wInv;
+}
+
+__device__ inline void corner_of(const Smp &s, int c, int &x, int &y, int &z) {
+  x = (c & 4) ? s.x1 : s.x0;
+  y = (c & 2) ? s.y1 : s.y0;
+  z = (c & 1) ? s.z1 : s.z0;
+}
+
+// Back-trace (dcgrid_fluid.cu:115-122): (pos + .5) * scale - v * dt * rdx.
+__device__ inline void back_trace(const Dev &D, int4 bp, int c, size_t cell, float &px, float &py,
+                                  float &pz) {
+  int lx, ly, lz;
+  local_xyz(c, lx, ly, lz);
+  const float scale = (float)(1 << bp.w);
+  const float alpha = D.ph.dt * D.ph.rdx;
+  px = ((float)(bp.x + lx) + 0.5f) * scale - D.v[0][cell] * alpha;
+  py = ((float)(bp.y + ly) + 0.5f) * scale - D.v[1][cell] * alpha;
+  pz = ((float)(bp.z + lz) + 0.5f) * scale - D.v[2][cell] * alpha;
+}
+
+// k_dcgrid_advect_velocity (dcgrid_fluid.cu:112-127) + buoyancy extension:
+// v.y += dt * (-alpha * rho + beta * (T - T_amb)) on leaf cells.
+__global__ void __launch_bounds__(256) k_advect_velocity(Dev D) {
+  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+  if (b >= D.g.B) return;
+  const int4 bp = D.pos[b];
+  if (bp.w < 0) return;
+  const int c = threadIdx.x & 63;
+  const size_t cell = (size_t)b * BV + c;
+  float o0 = 0.f, o1 = 0.f, o2 = 0.f;
+  if (D.child[cell >> 3] == NONE) {
+    float px, py, pz;
+    back_trace(D, bp, c, cell, px, py, pz);
+    Smp s;
+    sample_at(D, (uint32_t)b, bp, px, py, pz, s);
+    if (!(s.wAcc < 1e-6f)) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        int x, y, z;
+        corner_of(s, k, x, y, z);
+        float vx = D.v[0][s.idx[k]], vy = D.v[1][s.idx[k]], vz = D.v[2][s.idx[k]];
+        vel_bc(D.g, D.ph, vx, vy, vz, x, y, z, s.scale);
+        if (k == 0) {
+          o0 = vx * s.wt[0]; o1 = vy * s.wt[0]; o2 = vz * s.wt[0];
+        } else {
+          o0 = o0 + vx * s.wt[k]; o1 = o1 + vy * s.wt[k]; o2 = o2 + vz * s.wt[k];
+        }
+      }
+    }
+    if (D.ph.buoy_a != 0.f || D.ph.buoy_b != 0.f) {
+      float f = -D.ph.buoy_a * D.q[0][cell];
+      if (D.g.nq > 1) f = f + D.ph.buoy_b * (D.q[1][cell] - D.ph.t_amb);
+      o1 = o1 + D.ph.dt * f;
+    }
+  }
+  D.tv[0][cell] = o0;
+  D.tv[1][cell] = o1;
+  D.tv[2][cell] = o2;
+}
+
+// k_dcgrid_advect_density (dcgrid_fluid.cu:129-144) for every scalar; sphere
+// sources (extension) overwrite leaf cells inside the source.
+__global__ void __launch_bounds__(256) k_advect_scalars(Dev D) {
+  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+  if (b >= D.g.B) return;
+  const int4 bp = D.pos[b];
+  if (bp.w < 0) return;
+  const int c = threadIdx.x & 63;
+  const size_t cell = (size_t)b * BV + c;
+  const int nq = D.g.nq;
+  float o[3] = {0.f, 0.f, 0.f};
+  if (D.child[cell >> 3] == NONE) {
+    float px, py, pz;
+    back_trace(D, bp, c, cell, px, py, pz);
+    Smp s;
+    sample_at(D, (uint32_t)b, bp, px, py, pz, s);
+    if (!(s.wAcc < 1e-6f)) {
+      for (int kq = 0; kq < nq; kq++) {
+        float acc = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          int x, y, z;
+          corner_of(s, k, x, y, z);
+          const float qc = q_bc(D.g, D.ph, D.q[kq][s.idx[k]], kq, x, y, z, s.scale);
+          acc = (k == 0) ? qc * s.wt[0] : acc + qc * s.wt[k];
+        }
+        o[kq] = acc;
+      }
+    }
+    int lx, ly, lz;
+    local_xyz(c, lx, ly, lz);
+    if (D.ph.em_n > 0)
+      o[0] = o[0] + D.ph.dt * emission_at(D.g, D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w);
+    if (D.ph.src) {
+      if (in_source(D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w))
+        for (int kq = 0; kq < nq; kq++) o[kq] = D.ph.src_val[kq];
+    }
+  }
+  for (int kq = 0; kq < nq; kq++) D.tq[kq][cell] = o[kq];
+}
+
+// Source cells set on every leaf cell (used once at initialisation).
+__global__ void __launch_bounds__(256) k_sources(Dev D) {
+  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+  if (b >= D.g.B) return;
+  const int4 bp = D.pos[b];
+  if (bp.w < 0) return;
+  const int c = threadIdx.x & 63;
+  const size_t cell = (size_t)b * BV + c;
+  if (D.child[cell >> 3] != NONE) return;
+  int lx, ly, lz;
+  local_xyz(c, lx, ly, lz);
+  if (in_source(D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w))
+    for (int kq = 0; kq < D.g.nq; kq++) D.q[kq][cell] = D.ph.src_val[kq];
+}
+
+// Seeded velocity noise on every allocated cell.
+__global__ void __launch_bounds__(256) k_add_noise(Dev D, unsigned long long seed, float amp) {
+  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+  if (b >= D.g.B) return;
+  const int4 bp = D.pos[b];
+  if (bp.w < 0) return;
+  const int c = threadIdx.x & 63;
+  const size_t cell = (size_t)b * BV + c;
+  int lx, ly, lz;
+  local_xyz(c, lx, ly, lz);
+  for (int d = 0; d < 3; d++)
+    D.v[d][cell] = D.v[d][cell] + amp * noise_unit(seed, bp.x + lx, bp.y + ly, bp.z + lz, bp.w, d);
+}
+
+// accumulate<T> (dcgrid_structure.cu:188-205): parent cell = mean of the 8
+// cells of the child subblock; one thread per subblock of one level.
+__global__ void __launch_bounds__(256) k_restrict(Dev D, int level, FieldList fl) {
+  const long long sl = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (sl >= 8 * D.g.budget[level]) return;
+  const long long b = D.g.off[level] + (sl >> 3);
+  if (D.pos[b].w != level) return;
+  const uint32_t par = D.parent[b];
+  if (par == NONE) return;
+  const int s = (int)(sl & 7);
+  const size_t pc = (size_t)par * 8 + s;
+  const size_t base = (size_t)b * BV + 8 * s;
+  for (int f = 0; f < fl.n; f++) {
+    const float4 a = *reinterpret_cast<const float4 *>(fl.f[f] + base);
+    const float4 c = *reinterpret_cast<const float4 *>(fl.f[f] + base + 4);
+    float acc = 0.f;
+    acc = acc + a.x; acc = acc + a.y; acc = acc + a.z; acc = acc + a.w;
+    acc = acc + c.x; acc = acc + c.y; acc = acc + c.z; acc = acc + c.w;
+    fl.f[f][pc] = acc * 0.125f;
+  }
+}
+
+// k_dcgrid_calc_divergence (dcgrid_fluid.cu:174-230): zero p, p~, div on all
+// cells; div on leaf cells from fluidity-weighted central differences, apron
+// velocities through the boundary conditions.
+__global__ void __launch_bounds__(256) k_divergence(Dev D) {
+  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+  if (b >= D.g.B) return;
+  const int4 bp = D.pos[b];
+  if (bp.w < 0) return;
+  const int c = threadIdx.x & 63;
+  const size_t cell = (size_t)b * BV + c;
+  D.p[cell] = 0.f;
+  D.pt[cell] = 0.f;
+  float dv = 0.f;
+  if (D.child[cell >> 3] == NONE) {
+    int lx, ly, lz;
+    local_xyz(c, lx, ly, lz);
+    const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+    const int x = bp.x + lx, y = bp.y + ly, z = bp.z + lz;
+    const int scale = 1 << bp.w;
+    const float alpha = 0.5f * D.ph.rdx / (float)scale;
+    float nbv[6];
+    float nbw[6];
+    const int off[6][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+#pragma unroll
+    for (int n = 0; n < 6; n++) {
+      const int i = ax + off[n][0], j = ay + off[n][1], k = az + off[n][2];
+      const unsigned long long nc = apron_cell(D, (uint32_t)b, bp, i, j, k);
+      nbw[n] = D.w[nc];
+      const int comp = n >> 1;
+      float vx = D.v[0][nc], vy = D.v[1][nc], vz = D.v[2][nc];
+      if (i == 0 || i == AW - 1 || j == 0 || j == AW - 1 || k == 0 || k == AW - 1)
+        vel_bc(D.g, D.ph, vx, vy, vz, x + off[n][0], y + off[n][1], z + off[n][2], scale);
+      nbv[n] = comp == 0 ? vx : (comp == 1 ? vy : vz);
+    }
+    dv = alpha * (nbw[1] * nbv[1] - nbw[0] * nbv[0] + nbw[3] * nbv[3] - nbw[2] * nbv[2] +
+                  nbw[5] * nbv[5] - nbw[4] * nbv[4]);
+  }
+  D.div[cell] = dv;
+}
+
+// k_dcgrid_jacobi / _inv (dcgrid_multigrid_solver.cu:5-41) over every
+// allocated cell of one level (leaf or covered): dst = (sum6 src - a div) / 6.
+__global__ void __launch_bounds__(256) k_jacobi(Dev D, int level, const float *__restrict__ src,
+                                                float *__restrict__ dst) {
+  const long long bl = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+  if (bl >= D.g.budget[level]) return;
+  const long long b = D.g.off[level] + bl;
+  const int4 bp = D.pos[b];
+  if (bp.w != level) return;
+  const int c = threadIdx.x & 63;
+  int lx, ly, lz;
+  local_xyz(c, lx, ly, lz);
+  const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+  const int s = 1 << level;
+  const float alpha = (float)(s * s) * D.ph.dx * D.ph.dx;
+  const float pl = src[apron_cell(D, (uint32_t)b, bp, ax - 1, ay, az)];
+  const float pr = src[apron_cell(D, (uint32_t)b, bp, ax + 1, ay, az)];
+  const float pd = src[apron_cell(D, (uint32_t)b, bp, ax, ay - 1, az)];
+  const float pu = src[apron_cell(D, (uint32_t)b, bp, ax, ay + 1, az)];
+  const float pb = src[apron_cell(D, (uint32_t)b, bp, ax, ay, az - 1)];
+  const float pf = src[apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1)];
+  const size_t cell = (size_t)b * BV + c;
+  dst[cell] = (pl + pr + pd + pu + pb + pf - alpha * D.div[cell]) / 6.f;
+}
+
+// k_dcgrid_prolongate (dcgrid_multigrid_solver.cu:43-76): 27/9/3/1 trilinear
+// interpolation from the parent block's apron.
+__global__ void __launch_bounds__(256) k_prolongate(Dev D, int level) {
+  const long long bl = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+  if (bl >= D.g.budget[level]) return;
+  const long long b = D.g.off[level] + bl;
+  const int4 bp = D.pos[b];
+  if (bp.w != level) return;
+  const uint32_t par = D.parent[b];
+  if (par == NONE) return;
+  const uint32_t pb = par >> 3;
+  const int4 pbp = D.pos[pb];
+  const int c = threadIdx.x & 63;
+  int lx, ly, lz;
+  local_xyz(c, lx, ly, lz);
+  const int x = bp.x + lx, y = bp.y + ly, z = bp.z + lz;
+  const int ax = 1 + (x / 2) % BW, ay = 1 + (y / 2) % BW, az = 1 + (z / 2) % BW;
+  const int i = x % 2 ? 1 : -1, j = y % 2 ? 1 : -1, k = z % 2 ? 1 : -1;
+  const float *P = D.p;
+  const float p000 = P[apron_cell(D, pb, pbp, ax, ay, az)];
+  const float p001 = P[apron_cell(D, pb, pbp, ax, ay, az + k)];
+  const float p010 = P[apron_cell(D, pb, pbp, ax, ay + j, az)];
+  const float p100 = P[apron_cell(D, pb, pbp, ax + i, ay, az)];
+  const float p011 = P[apron_cell(D, pb, pbp, ax, ay + j, az + k)];
+  const float p101 = P[apron_cell(D, pb, pbp, ax + i, ay, az + k)];
+  const float p110 = P[apron_cell(D, pb, pbp, ax + i, ay + j, az)];
+  const float p111 = P[apron_cell(D, pb, pbp, ax + i, ay + j, az + k)];
+  D.p[(size_t)b * BV + c] =
+      (27.f * p000 + 9.f * (p001 + p010 + p100) + 3.f * (p011 + p101 + p110) + p111) / 64.f;
+}
+
+// k_dcgrid_apply_pressure (dcgrid_fluid.cu:232-259) on leaf cells.
+__global__ void __launch_bounds__(256) k_apply_pressure(Dev D) {
+  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+  if (b >= D.g.B) return;
+  const int4 bp = D.pos[b];
+  if (bp.w < 0) return;
+  const int c = threadIdx.x & 63;
+  const size_t cell = (size_t)b * BV + c;
+  if (D.child[cell >> 3] != NONE) return;
+  int lx, ly, lz;
+  local_xyz(c, lx, ly, lz);
+  const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+  const int scale = 1 << bp.w;
+  const float alpha = 0.5f * D.ph.rdx / (float)scale;
+  const float pc = D.p[cell];
+  const unsigned long long L = apron_cell(D, (uint32_t)b, bp, ax - 1, ay, az);
+  const unsigned long long R = apron_cell(D, (uint32_t)b, bp, ax + 1, ay, az);
+  const unsigned long long Dn = apron_cell(D, (uint32_t)b, bp, ax, ay - 1, az);
+  const unsigned long long U = apron_cell(D, (uint32_t)b, bp, ax, ay + 1, az);
+  const unsigned long long Bk = apron_cell(D, (uint32_t)b, bp, ax, ay, az - 1);
+  const unsigned long long F = apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1);
+  const float *P = D.p, *W = D.w;
+  D.v[0][cell] = D.v[0][cell] - alpha * (W[R] * (P[R] - pc) + W[L] * (pc - P[L]));
+  D.v[1][cell] = D.v[1][cell] - alpha * (W[U] * (P[U] - pc) + W[Dn] * (pc - P[Dn]));
+  D.v[2][cell] = D.v[2][cell] - alpha * (W[F] * (P[F] - pc) + W[Bk] * (pc - P[Bk]));
+}
+
+// ------------------------------------------------------------------ launchers
+static inline unsigned cta_blocks(long long nblocks) { return (unsigned)((nblocks + 3) / 4); }
+
+void launch_advect_velocity(const Dev &D, cudaStream_t st) {
+  k_advect_velocity<<<cta_blocks(D.g.B), 256, 0, st>>>(D);
+}
+void launch_advect_scalars(const Dev &D, cudaStream_t st) {
+  k_advect_scalars<<<cta_blocks(D.g.B), 256, 0, st>>>(D);
+}
+void launch_sources(const Dev &D, cudaStream_t st) { k_sources<<<cta_blocks(D.g.B), 256, 0, st>>>(D); }
+void launch_add_noise(const Dev &D, unsigned long long seed, float amp, cudaStream_t st) {
+  k_add_noise<<<cta_blocks(D.g.B), 256, 0, st>>>(D, seed, amp);
+}
+void launch_restrict(const Dev &D, const FieldList &fl, cudaStream_t st) {
+  for (int level = 0; level < D.g.levels - 1; level++) {
+    const long long n = 8 * D.g.budget[level];
+    k_restrict<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(D, level, fl);
+  }
+}
+void launch_divergence(const Dev &D, cudaStream_t st) { k_divergence<<<cta_blocks(D.g.B), 256, 0, st>>>(D); }
+void launch_jacobi(const Dev &D, int level, const float *src, float *dst, cudaStream_t st) {
+  k_jacobi<<<cta_blocks(D.g.budget[level]), 256, 0, st>>>(D, level, src, dst);
+}
+void launch_prolongate(const Dev &D, int level, cudaStream_t st) {
+  k_prolongate<<<cta_blocks(D.g.budget[level]), 256, 0, st>>>(D, level);
+}
+void launch_apply_pressure(const Dev &D, cudaStream_t st) {
+  k_apply_pressure<<<cta_blocks(D.g.B), 256, 0, st>>>(D);
+}
+
+}  // namespace dcg

@@ -1,0 +1,162 @@
+// k_sort.cu — stable LSD radix sort of (u32 key, u32 value) pairs, used to
+// rank adaptation candidates on the device (replaces the host-side
+// std::nth_element / std::sort of fluid_simulation_dcgrid.cu:387-408).
+//
+// Four 8-bit passes; each pass: tile histograms -> per-digit column scans ->
+// digit bases -> stable scatter. The scatter ranks equal digits with
+// __match_any_sync inside a warp and a per-digit running offset across warps
+// and rounds, so the order of equal keys is preserved (ties stay in index
+// order, which the selection relies on).
+#include "dcg_kernels.h"
+
+namespace dcg {
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 8;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+
+long long sort_tiles(long long n) { return (n + RS_TILE - 1) / RS_TILE; }
+
+__device__ inline bool gate_off(const long long *active) { return active && *active == 0; }
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint32_t *__restrict__ keys, long long n,
+                                                      int shift, uint32_t *__restrict__ hist,
+                                                      long long ntiles, const long long *active) {
+  if (gate_off(active)) return;
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * RS_TILE;
+  for (int r = 0; r < RS_ITEMS; r++) {
+    const long long i = base + r * RS_THREADS + threadIdx.x;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[(long long)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Block-wide exclusive scan of one value per thread (256 threads); returns
+// the exclusive prefix and writes the block total to *total.
+__device__ inline uint32_t block_exclusive_scan(uint32_t v, uint32_t *total) {
+  __shared__ uint32_t warp_sums[RS_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t s = lane < RS_THREADS / 32 ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < RS_THREADS / 32) warp_sums[lane] = s;
+  }
+  __syncthreads();
+  const uint32_t before = warp == 0 ? 0 : warp_sums[warp - 1];
+  *total = warp_sums[RS_THREADS / 32 - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+// One CTA per digit: exclusive scan of that digit's tile counts, in place.
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scan_cols(uint32_t *__restrict__ hist, long long ntiles,
+                                                           uint32_t *__restrict__ totals,
+                                                           const long long *active) {
+  if (gate_off(active)) return;
+  uint32_t *col = hist + (long long)blockIdx.x * ntiles;
+  uint32_t carry = 0;
+  for (long long t0 = 0; t0 < ntiles; t0 += RS_THREADS) {
+    const long long t = t0 + threadIdx.x;
+    const uint32_t v = t < ntiles ? col[t] : 0;
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan(v, &tot);
+    if (t < ntiles) col[t] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scan_totals(uint32_t *__restrict__ totals,
+                                                             const long long *active) {
+  if (gate_off(active)) return;
+  uint32_t tot;
+  const uint32_t v = totals[threadIdx.x];
+  const uint32_t ex = block_exclusive_scan(v, &tot);
+  totals[threadIdx.x] = ex;
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *__restrict__ kin,
+                                                         const uint32_t *__restrict__ vin,
+                                                         uint32_t *__restrict__ kout,
+                                                         uint32_t *__restrict__ vout, long long n,
+                                                         int shift, const uint32_t *__restrict__ hist,
+                                                         const uint32_t *__restrict__ totals,
+                                                         long long ntiles, const long long *active) {
+  if (gate_off(active)) return;
+  __shared__ uint32_t s_base[256];
+  __shared__ uint32_t s_wcnt[RS_THREADS / 32][256];
+  __shared__ uint32_t s_round[256];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int t = threadIdx.x;
+  s_base[t] = totals[t] + hist[(long long)t * ntiles + blockIdx.x];
+  const long long base = (long long)blockIdx.x * RS_TILE;
+  for (int r = 0; r < RS_ITEMS; r++) {
+    const long long i = base + r * RS_THREADS + t;
+    const bool valid = i < n;
+    const uint32_t k = valid ? kin[i] : 0u;
+    const uint32_t d = valid ? ((k >> shift) & 255u) : (256u + lane);
+#pragma unroll
+    for (int w = 0; w < RS_THREADS / 32; w++) s_wcnt[w][t] = 0;
+    __syncthreads();
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    if (valid && lane == __ffs(peers) - 1) s_wcnt[warp][d] = __popc(peers);
+    __syncthreads();
+    {
+      uint32_t run = 0;
+#pragma unroll
+      for (int w = 0; w < RS_THREADS / 32; w++) {
+        const uint32_t c = s_wcnt[w][t];
+        s_wcnt[w][t] = run;
+        run += c;
+      }
+      s_round[t] = run;
+    }
+    __syncthreads();
+    if (valid) {
+      const uint32_t pos = s_base[d] + s_wcnt[warp][d] + (uint32_t)rank;
+      kout[pos] = k;
+      vout[pos] = vin[i];
+    }
+    __syncthreads();
+    s_base[t] += s_round[t];
+    __syncthreads();
+  }
+}
+
+void launch_radix_sort(uint32_t *keys, uint32_t *vals, long long n, const SortScratch &s,
+                       const long long *active, cudaStream_t st) {
+  if (n <= 0) return;
+  const long long nt = sort_tiles(n);
+  uint32_t *kin = keys, *vin = vals, *kout = s.k1, *vout = s.v1;
+  for (int pass = 0; pass < 4; pass++) {
+    const int shift = 8 * pass;
+    k_rs_hist<<<(unsigned)nt, RS_THREADS, 0, st>>>(kin, n, shift, s.hist, nt, active);
+    k_rs_scan_cols<<<256, RS_THREADS, 0, st>>>(s.hist, nt, s.totals, active);
+    k_rs_scan_totals<<<1, RS_THREADS, 0, st>>>(s.totals, active);
+    k_rs_scatter<<<(unsigned)nt, RS_THREADS, 0, st>>>(kin, vin, kout, vout, n, shift, s.hist,
+                                                     s.totals, nt, active);
+    uint32_t *tk = kin, *tv = vin;
+    kin = kout; vin = vout;
+    kout = tk; vout = tv;
+  }
+  // four passes: the result is back in (keys, vals)
+}
+
+}  // namespace dcg

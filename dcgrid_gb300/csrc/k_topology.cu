@@ -1,0 +1,647 @@
+// k_topology.cu — block table construction, neighbour tables and the
+// GPU-resident adaptation (scores -> device-side ranking -> moves ->
+// refinements -> neighbour rebuild -> value propagation), plus statistics.
+//
+// The reference runs adaptation through host round trips (scores copied to
+// the host, std::nth_element/std::sort, indices copied back,
+// fluid_simulation_dcgrid.cu:348-483). Here every decision is made on the
+// device from counters in device memory, so a whole step has a fixed launch
+// sequence and can be captured in a CUDA graph.
+#include <cfloat>
+
+#include "dcg_kernels.h"
+
+namespace dcg {
+
+// ------------------------------------------------------------------ init
+__global__ void __launch_bounds__(256) k_init_blocks(Dev D) {
+  const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= D.g.B) return;
+  D.pos[b] = make_int4(0, 0, 0, -1);
+  D.parent[b] = NONE;
+  D.flags[b] = 0;
+#pragma unroll
+  for (int c = 0; c < 8; c++) D.child[8 * b + c] = NONE;
+}
+
+// k_dcgrid_activate_level (dcgrid_structure.cu:104-178): dense levels are laid
+// out in (x, y, z) order, z fastest; one thread per cell.
+__global__ void __launch_bounds__(256) k_activate_level(Dev D, int level) {
+  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nb = (long long)D.g.rx[level] * D.g.ry[level] * D.g.rz[level];
+  const long long t = gid >> 6;
+  if (t >= nb) return;
+  const int c = (int)(gid & 63);
+  const int tz = (int)(t % D.g.rz[level]);
+  const int ty = (int)((t / D.g.rz[level]) % D.g.ry[level]);
+  const int tx = (int)(t / ((long long)D.g.rz[level] * D.g.ry[level]));
+  const int px = BW * tx, py = BW * ty, pz = BW * tz;
+  const long long b = D.g.off[level] + t;
+  const int scale = 1 << level;
+  if (c == 0) {
+    D.pos[b] = make_int4(px, py, pz, level);
+    if (level < D.g.levels - 1)
+      D.parent[b] = 8u * dense_index(D.g, px / 2, py / 2, pz / 2, level + 1) +
+                    (uint32_t)((px % (2 * BW)) + (py % (2 * BW)) / 2 + (pz % (2 * BW)) / 4);
+    if (level - 1 >= D.g.sparse)
+      for (int k = 0; k < 8; k++)
+        D.child[8 * b + k] = dense_index(D.g, 2 * px + BW * ((k >> 2) & 1), 2 * py + BW * ((k >> 1) & 1),
+                                         2 * pz + BW * (k & 1), level - 1);
+  }
+  int lx, ly, lz;
+  local_xyz(c, lx, ly, lz);
+  const size_t cell = (size_t)b * BV + c;
+  D.w[cell] = fluidity(D.g, D.ph, px + lx, py + ly, pz + lz, scale);
+}
+
+// Neighbour table: for each allocated block and each of its 26 directions,
+// the finest block at the same or a coarser level that contains the
+// neighbouring block position, or OUT. This equals what the reference's
+// apron refresh (dcgrid_structure.cu:30-92) and activation (:104-178) store
+// for the border apron cells of that direction.
+__global__ void __launch_bounds__(256) k_build_nbr(Dev D, int only_if_touched) {
+  if (only_if_touched && D.ctr[C_TOUCHED] == 0) return;
+  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long b = gid / 27;
+  if (b >= D.g.B) return;
+  const int d = (int)(gid % 27);
+  const int4 bp = D.pos[b];
+  if (bp.w < 0) return;
+  uint32_t e;
+  if (d == 13) {
+    e = (uint32_t)b;
+  } else {
+    const int L = bp.w, scale = 1 << L;
+    const int qx = bp.x + BW * (d / 9 - 1), qy = bp.y + BW * ((d / 3) % 3 - 1), qz = bp.z + BW * (d % 3 - 1);
+    if (qx < 0 || qy < 0 || qz < 0 || qx * scale >= D.g.gx || qy * scale >= D.g.gy || qz * scale >= D.g.gz) {
+      e = OUT;
+    } else {
+      int lev;
+      const uint32_t nb = locate(D, qx, qy, qz, L, lev);
+      e = ((uint32_t)(lev - L) << 28) | nb;
+    }
+  }
+  D.nbr[27 * b + d] = e;
+}
+
+// ------------------------------------------------------------------ scores
+__device__ inline bool level_blocked(const Dev &D, int level) {
+  return (level == 0 && D.load[0] == D.g.full[0]) ||
+         (level > 0 && D.load[level - 1] == D.g.full[level - 1]);
+}
+
+// k_dcgrid_calc_subblock_scores (dcgrid_adaptation.cu:10-40), geometric score.
+__global__ void __launch_bounds__(256) k_scores_geo(Dev D) {
+  const long long sb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (sb >= 8 * D.g.B) {
+    if (sb == 8 * D.g.B) D.ss[sb] = 0.f;
+    return;
+  }
+  const long long b = sb >> 3;
+  const int4 bp = D.pos[b];
+  if (D.child[sb] != NONE || bp.w < 0 || level_blocked(D, bp.w)) {
+    D.ss[sb] = -FLT_MAX;
+    return;
+  }
+  const float sc = (float)(1 << bp.w);
+  const float px = sc * ((float)bp.x + 2.f * (float)((sb >> 2) & 1) + 1.f);
+  const float py = sc * ((float)bp.y + 2.f * (float)((sb >> 1) & 1) + 1.f);
+  const float pz = sc * ((float)bp.z + 2.f * (float)(sb & 1) + 1.f);
+  const float ddx = px - .5f * (float)D.g.gx, ddy = py - .45f * (float)D.g.gy, ddz = pz - .5f * (float)D.g.gz;
+  const float dd = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
+  D.ss[sb] = dd < .2f * (float)D.g.gx ? 0.f : (float)D.g.gx / dd;
+}
+
+// Field criterion (extension): per cell max(|curl v|/vort_t, |grad rho|/grad_t)
+// with the central differences of k_dcgrid_calc_vorticity
+// (dcgrid_fluid.cu:146-172); subblock score = max over its 8 cells, reduced
+// with warp shuffles (a subblock is 8 consecutive lanes).
+__global__ void __launch_bounds__(256) k_scores_fields(Dev D) {
+  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long b = gid >> 6;
+  if (b >= D.g.B) {
+    if (gid == 64 * D.g.B) D.ss[8 * D.g.B] = 0.f;
+    return;
+  }
+  const int c = (int)(gid & 63);
+  const int4 bp = D.pos[b];
+  const long long sb = (long long)b * 8 + (c >> 3);
+  const bool blocked = D.child[sb] != NONE || bp.w < 0 || (bp.w >= 0 && level_blocked(D, bp.w));
+  float m = 0.f;
+  if (!blocked) {
+    int lx, ly, lz;
+    local_xyz(c, lx, ly, lz);
+    const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+    const int scale = 1 << bp.w;
+    const float alpha = 0.5f * D.ph.rdx / (float)scale;
+    const unsigned long long L = apron_cell(D, (uint32_t)b, bp, ax - 1, ay, az);
+    const unsigned long long R = apron_cell(D, (uint32_t)b, bp, ax + 1, ay, az);
+    const unsigned long long Dn = apron_cell(D, (uint32_t)b, bp, ax, ay - 1, az);
+    const unsigned long long U = apron_cell(D, (uint32_t)b, bp, ax, ay + 1, az);
+    const unsigned long long Bk = apron_cell(D, (uint32_t)b, bp, ax, ay, az - 1);
+    const unsigned long long F = apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1);
+    const float *W = D.w;
+    const float wl = W[L], wr = W[R], wd = W[Dn], wu = W[U], wb = W[Bk], wf = W[F];
+    const float *V0 = D.v[0], *V1 = D.v[1], *V2 = D.v[2], *Q = D.q[0];
+    const float ox = alpha * ((wu * V2[U] - wd * V2[Dn]) - (wf * V1[F] - wb * V1[Bk]));
+    const float oy = alpha * ((wf * V0[F] - wb * V0[Bk]) - (wr * V2[R] - wl * V2[L]));
+    const float oz = alpha * ((wr * V1[R] - wl * V1[L]) - (wu * V0[U] - wd * V0[Dn]));
+    const float gxr = alpha * (Q[R] - Q[L]);
+    const float gyr = alpha * (Q[U] - Q[Dn]);
+    const float gzr = alpha * (Q[F] - Q[Bk]);
+    const float om = sqrtf(ox * ox + oy * oy + oz * oz);
+    const float gr = sqrtf(gxr * gxr + gyr * gyr + gzr * gzr);
+    const float a = om / D.ph.vort_t, bb = gr / D.ph.grad_t;
+    m = fmaxf(0.f, a < bb ? bb : a);
+  }
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((c & 7) == 0) D.ss[sb] = blocked ? -FLT_MAX : m;
+}
+
+// k_dcgrid_accumulate_subblock_scores (dcgrid_adaptation.cu:42-63); with
+// ref_compat the reference's ninth summand s[8] is included.
+__global__ void __launch_bounds__(256) k_block_scores(Dev D) {
+  const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= D.g.B) return;
+  D.bs[b] = -FLT_MAX;
+  const int level = D.pos[b].w;
+  if (level < 0 || level_blocked(D, level)) return;
+  const float *s = D.ss + 8 * b;
+  if (s[0] > 0.f && s[1] > 0.f && s[2] > 0.f && s[3] > 0.f && s[4] > 0.f && s[5] > 0.f && s[6] > 0.f &&
+      s[7] > 0.f) {
+    float sum = s[0] + s[1] + s[2] + s[3] + s[4] + s[5] + s[6] + s[7];
+    if (D.g.ref_compat) sum = sum + s[8];
+    D.bs[b] = .125f * sum;
+  }
+}
+
+// ------------------------------------------------------------------ moves
+// Move limit of one level (fluid_simulation_dcgrid.cu:376-385).
+__global__ void k_move_setup(Dev D, int L) {
+  const long long d0 = D.g.budget[L], d1 = 8 * D.g.budget[L + 1];
+  long long l = d0 < d1 ? d0 : d1;
+  l = l < D.load[L] ? l : D.load[L];
+  const long long freeL = D.g.full[L] - D.load[L];
+  l = l < freeL ? l : freeL;
+  if (D.move_limit[L] > 0) l = l < D.move_limit[L] ? l : D.move_limit[L];
+  D.ctr[C_MOVE_LIMIT] = l;
+  D.ctr[C_MATCHES] = l;
+  D.ctr[C_MOVE_BEGIN + L] = D.ctr[C_MOVES];
+  D.ctr[C_MOVE_END + L] = D.ctr[C_MOVES];
+}
+
+// Sort keys: blocks ascending by score, negative scores last; subblocks
+// descending by score. The sort is stable over index-ordered input, so
+// equal keys stay in index order.
+__global__ void __launch_bounds__(256) k_keys_blocks(Dev D, int L, uint32_t *keys, uint32_t *vals) {
+  if (D.ctr[C_MOVE_LIMIT] == 0) return;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= D.g.budget[L]) return;
+  const long long b = D.g.off[L] + i;
+  const float s = D.bs[b];
+  keys[i] = s < 0.f ? 0xFFFFFFFFu : (__float_as_uint(s) & 0x7FFFFFFFu);
+  vals[i] = (uint32_t)b;
+}
+__global__ void __launch_bounds__(256) k_keys_dests(Dev D, int L, uint32_t *keys, uint32_t *vals) {
+  if (D.ctr[C_MOVE_LIMIT] == 0) return;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 8 * D.g.budget[L + 1]) return;
+  const long long sb = 8 * D.g.off[L + 1] + i;
+  const float s = D.ss[sb];
+  uint32_t u = s == 0.f ? 0u : __float_as_uint(s);
+  u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);  // order-preserving map
+  keys[i] = ~u;                                      // descending
+  vals[i] = (uint32_t)sb;
+}
+// First pair that fails the reference's match condition (cu:410-418).
+__global__ void __launch_bounds__(256) k_match(Dev D, const uint32_t *blocks, const uint32_t *dests) {
+  const long long l = D.ctr[C_MOVE_LIMIT];
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < l; m += (long long)gridDim.x * blockDim.x) {
+    const float sb = D.bs[blocks[m]], sd = D.ss[dests[m]];
+    if (!(sb >= 0.f && sd >= 0.f && sb < sd)) atomicMin(&D.ctr[C_MATCHES], m);
+  }
+}
+// Records the matched pairs and protects blocks from moving at the next
+// level: with ref_compat the block of the candidate *after* each match, as
+// the reference's loop does (cu:415-417); otherwise the destination's block.
+__global__ void __launch_bounds__(256) k_commit_moves(Dev D, int L, const uint32_t *blocks,
+                                                      const uint32_t *dests) {
+  const long long l = D.ctr[C_MOVE_LIMIT];
+  if (l == 0) return;
+  const long long matches = D.ctr[C_MATCHES];
+  const long long base = D.ctr[C_MOVE_BEGIN + L];
+  const long long d1 = 8 * D.g.budget[L + 1];
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m <= matches;
+       m += (long long)gridDim.x * blockDim.x) {
+    if (m < matches) {
+      D.moves[2 * (base + m)] = blocks[m];
+      D.moves[2 * (base + m) + 1] = dests[m];
+    }
+    if (D.g.ref_compat) {
+      if (m >= 1 && m < d1) D.bs[dests[m] >> 3] = -FLT_MAX;
+    } else if (m < matches) {
+      D.bs[dests[m] >> 3] = -FLT_MAX;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    D.move_limit[L] = (long long)(unsigned long long)((float)matches * 1.2f);
+    D.ctr[C_MOVES] = base + matches;
+    D.ctr[C_MOVE_END + L] = base + matches;
+  }
+}
+// k_dcgrid_move_blocks (dcgrid_adaptation.cu:65-90), one level at a time from
+// coarse to fine so a block moved into a block that itself moved takes its
+// parent's new position.
+__global__ void __launch_bounds__(256) k_apply_moves(Dev D, int L) {
+  const long long beg = D.ctr[C_MOVE_BEGIN + L], end = D.ctr[C_MOVE_END + L];
+  for (long long m = beg + (long long)blockIdx.x * blockDim.x + threadIdx.x; m < end;
+       m += (long long)gridDim.x * blockDim.x) {
+    const uint32_t b = D.moves[2 * m], dest = D.moves[2 * m + 1];
+    const uint32_t prev = D.parent[b];
+    if (prev != NONE) D.child[prev] = NONE;
+    D.child[dest] = b;
+    D.parent[b] = dest;
+    const uint32_t pb = dest >> 3;
+    const int4 pp = D.pos[pb];
+    const int4 old = D.pos[b];
+    D.pos[b] = make_int4(2 * pp.x + BW * ((dest >> 2) & 1), 2 * pp.y + BW * ((dest >> 1) & 1),
+                         2 * pp.z + BW * (dest & 1), old.w);
+    D.flags[b] |= MOVED;
+    D.flags[pb] |= REFINED;
+    D.touched[m] = b;
+  }
+}
+
+// ------------------------------------------------------------ refinements
+// Refinement limit of one parent level (fluid_simulation_dcgrid.cu:449-453).
+__global__ void k_refine_setup(Dev D, int L) {
+  const unsigned long long a = (unsigned long long)(D.g.budget[L - 1] - D.load[L - 1]);
+  const unsigned long long bb = (unsigned long long)(8 * D.load[L]) - (unsigned long long)D.load[L - 1];
+  const long long limit = (long long)(a < bb ? a : bb);
+  D.ctr[C_MOVE_LIMIT] = limit;
+  D.ctr[C_REF_BEGIN + L - 1] = D.ctr[C_REFINES];
+  D.ctr[C_REF_END + L - 1] = D.ctr[C_REFINES];
+  D.ctr[C_LOAD0 + L - 1] = D.load[L - 1];
+  D.ctr[C_NCAND] = 0;
+}
+
+constexpr int CMP_TILE = 2048;
+
+// Compaction of flagged subblocks (stable, ascending index): tile counts,
+// a single-CTA scan over tiles, then per-tile ranks.
+__device__ inline bool cand_flag(const Dev &D, int L, long long i, const uint8_t *sel) {
+  if (sel) return sel[8 * D.g.off[L] + i] != 0;
+  return D.ss[8 * D.g.off[L] + i] > D.ph.refine_threshold;
+}
+__global__ void __launch_bounds__(256) k_cmp_count(Dev D, int L, const uint8_t *sel, uint32_t *tile_sums) {
+  if (D.ctr[C_MOVE_LIMIT] == 0) return;
+  const long long n = 8 * D.g.budget[L];
+  const long long base = (long long)blockIdx.x * CMP_TILE;
+  int cnt = 0;
+  for (int r = 0; r < CMP_TILE / 256; r++) {
+    const long long i = base + r * 256 + threadIdx.x;
+    if (i < n && cand_flag(D, L, i, sel)) cnt++;
+  }
+  cnt = __reduce_add_sync(0xffffffffu, (unsigned)cnt);
+  __shared__ int ws[8];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < 8; w++) t += ws[w];
+    tile_sums[blockIdx.x] = (uint32_t)t;
+  }
+}
+__global__ void __launch_bounds__(1024) k_cmp_scan(Dev D, uint32_t *tile_sums, long long ntiles) {
+  if (D.ctr[C_MOVE_LIMIT] == 0) return;
+  __shared__ uint32_t ws[32];
+  __shared__ uint32_t carry_s;
+  if (threadIdx.x == 0) carry_s = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (long long t0 = 0; t0 < ntiles; t0 += 1024) {
+    const long long t = t0 + threadIdx.x;
+    const uint32_t v = t < ntiles ? tile_sums[t] : 0;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t s = ws[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += y;
+      }
+      ws[lane] = s;
+    }
+    __syncthreads();
+    const uint32_t carry = carry_s;
+    const uint32_t ex = carry + (warp ? ws[warp - 1] : 0) + x - v;
+    if (t < ntiles) tile_sums[t] = ex;
+    __syncthreads();
+    if (threadIdx.x == 0) carry_s = carry + ws[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) D.ctr[C_NCAND] = carry_s;
+}
+__global__ void __launch_bounds__(256) k_cmp_scatter(Dev D, int L, const uint8_t *sel,
+                                                     const uint32_t *tile_sums, uint32_t *out) {
+  if (D.ctr[C_MOVE_LIMIT] == 0) return;
+  __shared__ uint32_t ws[8];
+  __shared__ uint32_t run_s;
+  const long long n = 8 * D.g.budget[L];
+  const long long base = (long long)blockIdx.x * CMP_TILE;
+  if (threadIdx.x == 0) run_s = tile_sums[blockIdx.x];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int r = 0; r < CMP_TILE / 256; r++) {
+    const long long i = base + r * 256 + threadIdx.x;
+    const bool f = i < n && cand_flag(D, L, i, sel);
+    const uint32_t bal = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) ws[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t before = run_s;
+    for (int w = 0; w < warp; w++) before += ws[w];
+    if (f) out[before + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)(8 * D.g.off[L] + i);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t t = 0;
+      for (int w = 0; w < 8; w++) t += ws[w];
+      run_s += t;
+    }
+    __syncthreads();
+  }
+}
+// Score-ordered selection (ref_compat off): keys of the compacted candidates.
+__global__ void __launch_bounds__(256) k_keys_cands(Dev D, const uint32_t *cand, uint32_t *keys,
+                                                    uint32_t *vals, long long nmax) {
+  const long long n = D.ctr[C_NCAND];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nmax; i += (long long)gridDim.x * blockDim.x) {
+    if (i < n) {
+      const float s = D.ss[cand[i]];
+      uint32_t u = s == 0.f ? 0u : __float_as_uint(s);
+      u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+      keys[i] = ~u;
+      vals[i] = cand[i];
+    } else {
+      keys[i] = 0xFFFFFFFFu;  // pads sort after every candidate
+      vals[i] = 0xFFFFFFFFu;
+    }
+  }
+}
+__global__ void __launch_bounds__(256) k_mark_selected(Dev D, const uint32_t *sorted, uint8_t *sel) {
+  if (D.ctr[C_MOVE_LIMIT] == 0) return;
+  const long long n = D.ctr[C_NCAND], limit = D.ctr[C_MOVE_LIMIT];
+  const long long keep = n < limit ? n : limit;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < keep; i += (long long)gridDim.x * blockDim.x)
+    sel[sorted[i]] = 1;
+}
+// Records the kept candidates of one level and assigns new block indices in
+// ascending subblock order. ref_compat keeps the `limit` largest subblock
+// indices (the reference's nth_element over indices, cu:464-466).
+__global__ void __launch_bounds__(256) k_record_refines(Dev D, int L, const uint32_t *cand, int compat_tail) {
+  const long long limit = D.ctr[C_MOVE_LIMIT];
+  if (limit == 0) return;
+  const long long n = D.ctr[C_NCAND];
+  const long long keep = n < limit ? n : limit;
+  const long long first = compat_tail ? n - keep : 0;
+  const long long base = D.ctr[C_REF_BEGIN + L - 1];
+  const long long load0 = D.ctr[C_LOAD0 + L - 1];
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < keep; r += (long long)gridDim.x * blockDim.x) {
+    D.refines[2 * (base + r)] = cand[first + r];
+    D.refines[2 * (base + r) + 1] = (uint32_t)(D.g.off[L - 1] + load0 + r);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    D.ctr[C_REFINES] = base + keep;
+    D.ctr[C_REF_END + L - 1] = base + keep;
+  }
+}
+// k_dcgrid_refine_subblocks + insertBlock (dcgrid_adaptation.cu:145-178,
+// dcgrid_utils.cuh:99-140) for every recorded refinement.
+__global__ void __launch_bounds__(256) k_apply_refines(Dev D) {
+  const long long nr = D.ctr[C_REFINES], nm = D.ctr[C_MOVES];
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < nr; m += (long long)gridDim.x * blockDim.x) {
+    const uint32_t sb = D.refines[2 * m], cb = D.refines[2 * m + 1];
+    const uint32_t pb = sb >> 3;
+    const int4 pp = D.pos[pb];
+    const int cl = pp.w - 1;
+    if (cl < 0 || (long long)cb >= D.g.off[cl] + D.g.budget[cl]) {
+      set_err(D, 1u);
+      D.touched[nm + m] = NONE;
+      continue;
+    }
+    D.pos[cb] = make_int4(2 * pp.x + BW * ((sb >> 2) & 1), 2 * pp.y + BW * ((sb >> 1) & 1),
+                          2 * pp.z + BW * (sb & 1), cl);
+    D.parent[cb] = sb;
+    D.child[sb] = cb;
+    D.flags[pb] |= REFINED;
+    D.flags[cb] |= MOVED;
+    D.touched[nm + m] = cb;
+  }
+}
+__global__ void k_finish_refines(Dev D) {
+  for (int L = 1; L < D.g.levels; L++) {
+    const long long n = D.ctr[C_REF_END + L - 1] - D.ctr[C_REF_BEGIN + L - 1];
+    D.load[L - 1] += n;
+  }
+  D.ctr[C_TOUCHED] = D.ctr[C_MOVES] + D.ctr[C_REFINES];
+}
+
+// k_dcgrid_propagate_values (dcgrid_adaptation.cu:92-143): new or moved blocks
+// of one level take 27/9/3/1 interpolations of their parent's apron.
+__global__ void __launch_bounds__(256) k_propagate(Dev D, int level) {
+  const long long nt = D.ctr[C_TOUCHED];
+  const int c = threadIdx.x & 63;
+  for (long long t = (long long)blockIdx.x * 4 + (threadIdx.x >> 6); t < nt; t += (long long)gridDim.x * 4) {
+    const uint32_t b = D.touched[t];
+    if (b == NONE) continue;
+    const int4 bp = D.pos[b];
+    if (bp.w != level) continue;
+    const uint32_t par = D.parent[b];
+    if (par == NONE) continue;
+    const uint32_t pb = par >> 3;
+    const int4 pbp = D.pos[pb];
+    int lx, ly, lz;
+    local_xyz(c, lx, ly, lz);
+    const int x = bp.x + lx, y = bp.y + ly, z = bp.z + lz;
+    const int ax = 1 + (x / 2) % BW, ay = 1 + (y / 2) % BW, az = 1 + (z / 2) % BW;
+    const int i = x % 2 ? 1 : -1, j = y % 2 ? 1 : -1, k = z % 2 ? 1 : -1;
+    const unsigned long long i000 = apron_cell(D, pb, pbp, ax, ay, az);
+    const unsigned long long i001 = apron_cell(D, pb, pbp, ax, ay, az + k);
+    const unsigned long long i010 = apron_cell(D, pb, pbp, ax, ay + j, az);
+    const unsigned long long i100 = apron_cell(D, pb, pbp, ax + i, ay, az);
+    const unsigned long long i011 = apron_cell(D, pb, pbp, ax, ay + j, az + k);
+    const unsigned long long i101 = apron_cell(D, pb, pbp, ax + i, ay, az + k);
+    const unsigned long long i110 = apron_cell(D, pb, pbp, ax + i, ay + j, az);
+    const unsigned long long i111 = apron_cell(D, pb, pbp, ax + i, ay + j, az + k);
+    const size_t cell = (size_t)b * BV + c;
+    auto tri = [&](const float *f) {
+      return (27.f / 64.f) * f[i000] + (9.f / 64.f) * (f[i001] + f[i010] + f[i100]) +
+             (3.f / 64.f) * (f[i011] + f[i101] + f[i110]) + (1.f / 64.f) * f[i111];
+    };
+    float qv[3], vv[3];
+    for (int kq = 0; kq < D.g.nq; kq++) qv[kq] = tri(D.q[kq]);
+    for (int d = 0; d < 3; d++) vv[d] = tri(D.v[d]);
+    __syncwarp();
+    for (int kq = 0; kq < D.g.nq; kq++) D.q[kq][cell] = qv[kq];
+    for (int d = 0; d < 3; d++) D.v[d][cell] = vv[d];
+    D.w[cell] = fluidity(D.g, D.ph, x, y, z, 1 << level);
+  }
+}
+
+static unsigned grid_for(long long n, int threads = 256) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+void launch_init_blocks(const Dev &D, cudaStream_t st) {
+  k_init_blocks<<<grid_for(D.g.B), 256, 0, st>>>(D);
+}
+void launch_activate_level(const Dev &D, int level, cudaStream_t st) {
+  const long long nb = (long long)D.g.rx[level] * D.g.ry[level] * D.g.rz[level];
+  k_activate_level<<<grid_for(nb * 64), 256, 0, st>>>(D, level);
+}
+void launch_build_nbr(const Dev &D, bool only_if_touched, cudaStream_t st) {
+  k_build_nbr<<<grid_for(D.g.B * 27), 256, 0, st>>>(D, only_if_touched ? 1 : 0);
+}
+
+static void launch_scores(const Dev &D, cudaStream_t st) {
+  if (D.ph.criterion == 0)
+    k_scores_geo<<<grid_for(8 * D.g.B + 1), 256, 0, st>>>(D);
+  else
+    k_scores_fields<<<grid_for(64 * D.g.B + 1), 256, 0, st>>>(D);
+}
+
+// FluidSimulationDCGrid::adaptTopology (fluid_simulation_dcgrid.cu:320-346)
+// as a fixed sequence of launches.
+void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *vals, uint32_t *keys2,
+                  uint32_t *vals2, int sms, cudaStream_t st) {
+  const unsigned gs = (unsigned)(sms > 0 ? sms * 4 : 512);
+  cudaMemsetAsync(D.ctr, 0, sizeof(long long) * C_COUNT, st);
+  cudaMemsetAsync(D.flags, 0, (size_t)D.g.B, st);
+  // moveBlocks
+  launch_scores(D, st);
+  k_block_scores<<<grid_for(D.g.B), 256, 0, st>>>(D);
+  for (int L = 0; L < D.g.levels - 1; L++) {
+    const long long d0 = D.g.budget[L], d1 = 8 * D.g.budget[L + 1];
+    k_move_setup<<<1, 1, 0, st>>>(D, L);
+    k_keys_blocks<<<grid_for(d0), 256, 0, st>>>(D, L, keys, vals);
+    launch_radix_sort(keys, vals, d0, s, D.ctr + C_MOVE_LIMIT, st);
+    k_keys_dests<<<grid_for(d1), 256, 0, st>>>(D, L, keys2, vals2);
+    launch_radix_sort(keys2, vals2, d1, s, D.ctr + C_MOVE_LIMIT, st);
+    k_match<<<gs, 256, 0, st>>>(D, vals, vals2);
+    k_commit_moves<<<gs, 256, 0, st>>>(D, L, vals, vals2);
+  }
+  for (int L = D.g.levels - 2; L >= 0; L--) k_apply_moves<<<gs, 256, 0, st>>>(D, L);
+  // refineSubblocks
+  launch_scores(D, st);
+  uint8_t *sel = reinterpret_cast<uint8_t *>(keys2);  // 8*B bytes, reused as selection flags
+  for (int L = 1; L < D.g.levels; L++) {
+    const long long n8 = 8 * D.g.budget[L];
+    const long long nt = (n8 + CMP_TILE - 1) / CMP_TILE;
+    k_refine_setup<<<1, 1, 0, st>>>(D, L);
+    k_cmp_count<<<(unsigned)nt, 256, 0, st>>>(D, L, nullptr, s.tile_sums);
+    k_cmp_scan<<<1, 1024, 0, st>>>(D, s.tile_sums, nt);
+    k_cmp_scatter<<<(unsigned)nt, 256, 0, st>>>(D, L, nullptr, s.tile_sums, vals);
+    if (D.g.ref_compat) {
+      k_record_refines<<<gs, 256, 0, st>>>(D, L, vals, 1);
+    } else {
+      k_keys_cands<<<gs, 256, 0, st>>>(D, vals, keys, vals2, n8);
+      launch_radix_sort(keys, vals2, n8, s, D.ctr + C_MOVE_LIMIT, st);
+      cudaMemsetAsync(sel, 0, (size_t)8 * D.g.B, st);
+      k_mark_selected<<<gs, 256, 0, st>>>(D, vals2, sel);
+      k_cmp_count<<<(unsigned)nt, 256, 0, st>>>(D, L, sel, s.tile_sums);
+      k_cmp_scan<<<1, 1024, 0, st>>>(D, s.tile_sums, nt);
+      k_cmp_scatter<<<(unsigned)nt, 256, 0, st>>>(D, L, sel, s.tile_sums, vals);
+      k_record_refines<<<gs, 256, 0, st>>>(D, L, vals, 0);
+    }
+  }
+  k_apply_refines<<<gs, 256, 0, st>>>(D);
+  k_finish_refines<<<1, 1, 0, st>>>(D);
+  // neighbour tables + value propagation for touched blocks
+  launch_build_nbr(D, true, st);
+  for (int L = D.g.levels - 2; L >= 0; L--) k_propagate<<<gs, 256, 0, st>>>(D, L);
+}
+
+// ------------------------------------------------------------------ stats
+// k_dcgrid_debug_stats (dcgrid_structure.cu:224-251) plus mass and leaf
+// counts; warp-shuffle reductions, one double atomic per warp.
+__global__ void __launch_bounds__(256) k_stats(Dev D) {
+  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+  double res = 0.0, mass = 0.0;
+  int lev = -1;
+  if (b < D.g.B) {
+    const int4 bp = D.pos[b];
+    const int c = threadIdx.x & 63;
+    const size_t cell = (size_t)b * BV + c;
+    if (bp.w >= 0 && D.child[cell >> 3] == NONE) {
+      lev = bp.w;
+      int lx, ly, lz;
+      local_xyz(c, lx, ly, lz);
+      const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+      const int scale = 1 << bp.w;
+      const double alpha = (double)D.ph.rdx * (double)D.ph.rdx / (double)(scale * scale);
+      const float *P = D.p;
+      const double lap = (double)P[apron_cell(D, (uint32_t)b, bp, ax - 1, ay, az)] +
+                         P[apron_cell(D, (uint32_t)b, bp, ax + 1, ay, az)] +
+                         P[apron_cell(D, (uint32_t)b, bp, ax, ay - 1, az)] +
+                         P[apron_cell(D, (uint32_t)b, bp, ax, ay + 1, az)] +
+                         P[apron_cell(D, (uint32_t)b, bp, ax, ay, az - 1)] +
+                         P[apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1)] - 6.0 * P[cell];
+      res = (double)scale * fabs((double)D.div[cell] - lap * alpha);
+      mass = (double)D.q[0][cell] * (double)D.w[cell] * scale * scale * scale;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    res += __shfl_xor_sync(0xffffffffu, res, o);
+    mass += __shfl_xor_sync(0xffffffffu, mass, o);
+  }
+  // a warp covers half of one block, so all its leaf cells share one level
+  const unsigned leafmask = __ballot_sync(0xffffffffu, lev >= 0);
+  const int lvl0 = __shfl_sync(0xffffffffu, lev, leafmask ? __ffs(leafmask) - 1 : 0);
+  if ((threadIdx.x & 31) == 0) {
+    if (res != 0.0) atomicAdd(&D.red[0], res);
+    if (mass != 0.0) atomicAdd(&D.red[1], mass);
+    if (leafmask) atomicAdd(&D.red[2 + lvl0], (double)__popc(leafmask));
+  }
+}
+void launch_stats(const Dev &D, cudaStream_t st) {
+  cudaMemsetAsync(D.red, 0, sizeof(double) * 32, st);
+  k_stats<<<(unsigned)((D.g.B + 3) / 4), 256, 0, st>>>(D);
+}
+
+// Dense resampling: every finest cell takes the leaf value that covers it.
+__global__ void __launch_bounds__(256) k_to_dense(Dev D, const float *src, float *dst) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)D.g.gx * D.g.gy * D.g.gz;
+  if (i >= n) return;
+  const int x = (int)(i % D.g.gx), y = (int)((i / D.g.gx) % D.g.gy), z = (int)(i / ((long long)D.g.gx * D.g.gy));
+  int lev;
+  const uint32_t b = locate(D, x, y, z, 0, lev);
+  const int4 bp = D.pos[b];
+  dst[i] = src[(size_t)b * BV + local_of((x >> lev) - bp.x, (y >> lev) - bp.y, (z >> lev) - bp.z)];
+}
+void launch_fields_to_dense(const Dev &D, const float *src, float *dst, cudaStream_t st) {
+  const long long n = (long long)D.g.gx * D.g.gy * D.g.gz;
+  k_to_dense<<<grid_for(n), 256, 0, st>>>(D, src, dst);
+}
+
+// The reference-format 216-entry apron table, derived from neighbour tables.
+__global__ void __launch_bounds__(216) k_apron_table(Dev D, long long *dst) {
+  const long long b = blockIdx.x;
+  const int a = threadIdx.x;
+  const int4 bp = D.pos[b];
+  if (bp.w < 0) {
+    dst[b * 216 + a] = -1;
+    return;
+  }
+  dst[b * 216 + a] = (long long)apron_cell(D, (uint32_t)b, bp, a / 36, (a / 6) % 6, a % 6);
+}
+void launch_apron_table(const Dev &D, long long *dst, cudaStream_t st) {
+  k_apron_table<<<(unsigned)D.g.B, 216, 0, st>>>(D, dst);
+}
+
+}  // namespace dcg

@@ -1,0 +1,319 @@
+"""Python host API over the C ABI (libdcgrid_gb300.so).
+
+Mirrors the reference's simulation interface (src/fluid_simulation.h:4-27):
+FluidSimulationDCGrid(size, maxNumBlocks) and FluidSimulationUniform(size)
+with init/reset/adaptTopology/advectVelocity/project/projectLocal/
+advectDensity/debugStats, plus field and topology accessors the reference
+does not expose. Errors raise DcgError carrying the C status code; the
+reference would exit(1) instead.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import capi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdcgrid_gb300.so")
+_lib = None
+
+
+class DcgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{capi.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib():
+    """Loads the in-tree CUDA library. There is no fallback: a missing library
+    is an error (build it with dcgrid_gb300.build.build())."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing; run dcgrid_gb300.build.build() first")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.dcg_default_params.argtypes = [C.POINTER(capi.DcgParams), C.c_int32, C.c_int32, C.c_int32, C.c_int64]
+        L.dcg_default_params.restype = None
+        L.dcg_create.argtypes = [C.POINTER(capi.DcgParams), C.c_int32, C.POINTER(vp)]
+        for name in ["dcg_destroy", "dcg_reset", "dcg_advect_velocity", "dcg_adapt", "dcg_project",
+                     "dcg_project_local", "dcg_advect_scalars", "dcg_sync"]:
+            getattr(L, name).argtypes = [vp]
+        L.dcg_set_params.argtypes = [vp, C.POINTER(capi.DcgParams)]
+        L.dcg_set_mode.argtypes = [C.POINTER(vp), C.c_int32]
+        L.dcg_set_stream.argtypes = [vp, vp]
+        L.dcg_get_info.argtypes = [vp, C.POINTER(capi.DcgInfo)]
+        L.dcg_last_error_string.argtypes = [vp]
+        L.dcg_last_error_string.restype = C.c_char_p
+        L.dcg_step.argtypes = [vp, C.c_int32]
+        L.dcg_add_velocity_noise.argtypes = [vp, C.c_uint64, C.c_float]
+        L.dcg_get_field.argtypes = [vp, C.c_int32, vp, C.c_int32]
+        L.dcg_set_field.argtypes = [vp, C.c_int32, vp, C.c_int32]
+        L.dcg_get_dense.argtypes = [vp, C.c_int32, vp, C.c_int32]
+        L.dcg_get_topology.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.dcg_set_topology.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.dcg_get_apron.argtypes = [vp, vp]
+        L.dcg_get_last_adapt.argtypes = [vp, vp, C.POINTER(C.c_int64), vp, C.POINTER(C.c_int64)]
+        L.dcg_get_stats.argtypes = [vp, C.POINTER(capi.DcgStats)]
+        L.dcg_set_graphs.argtypes = [vp, C.c_int32]
+        L.dcg_time_kernel.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_float),
+                                      C.POINTER(C.c_double)]
+        L.dcg_launches_per_step.argtypes = [vp, C.POINTER(C.c_int64)]
+        L.dcg_set_emission.argtypes = [vp, vp, C.c_int32]
+        for name in ["dcg_sizeof_params", "dcg_sizeof_info", "dcg_sizeof_stats"]:
+            getattr(L, name).restype = C.c_size_t
+            getattr(L, name).argtypes = []
+        _lib = L
+    return _lib
+
+
+def default_params(gx, gy, gz, max_blocks):
+    p = capi.DcgParams()
+    lib().dcg_default_params(C.byref(p), gx, gy, gz, max_blocks)
+    return p
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _field_id(field):
+    return capi.FIELD_NAMES[field] if isinstance(field, str) else int(field)
+
+
+class Simulation:
+    """One simulation handle (adaptive or uniform)."""
+
+    def __init__(self, params, mode=capi.MODE_ADAPTIVE):
+        self.L = lib()
+        self.params = params
+        h = C.c_void_p()
+        rc = self.L.dcg_create(C.byref(params), mode, C.byref(h))
+        if rc != capi.DCG_OK:
+            raise DcgError(rc, "dcg_create failed")
+        self.h = h
+        self.mode = mode
+        self.info = capi.DcgInfo()
+        self._chk(self.L.dcg_get_info(self.h, C.byref(self.info)), "get_info")
+
+    # -- lifecycle --------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.dcg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _chk(self, rc, what):
+        if rc != capi.DCG_OK:
+            msg = self.L.dcg_last_error_string(self.h).decode() if self.h else ""
+            raise DcgError(rc, f"{what}: {msg}")
+
+    def reset(self):
+        self._chk(self.L.dcg_reset(self.h), "reset")
+
+    def set_params(self, params):
+        self._chk(self.L.dcg_set_params(self.h, C.byref(params)), "set_params")
+        self.params = params
+
+    def set_mode(self, mode):
+        """The reference's adaptive/uniform switch: recreate, state dropped."""
+        self._chk(self.L.dcg_set_mode(C.byref(self.h), mode), "set_mode")
+        self.mode = mode
+        self._chk(self.L.dcg_get_info(self.h, C.byref(self.info)), "get_info")
+
+    def set_stream(self, stream_ptr):
+        self._chk(self.L.dcg_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")
+
+    def set_graphs(self, on):
+        self._chk(self.L.dcg_set_graphs(self.h, 1 if on else 0), "set_graphs")
+
+    # -- the step and its stages ------------------------------------------
+    def step(self, n=1):
+        self._chk(self.L.dcg_step(self.h, n), "step")
+
+    def advect_velocity(self):
+        self._chk(self.L.dcg_advect_velocity(self.h), "advect_velocity")
+
+    def adapt(self):
+        self._chk(self.L.dcg_adapt(self.h), "adapt")
+
+    def project(self):
+        self._chk(self.L.dcg_project(self.h), "project")
+
+    def project_local(self):
+        self._chk(self.L.dcg_project_local(self.h), "project_local")
+
+    def advect_scalars(self):
+        self._chk(self.L.dcg_advect_scalars(self.h), "advect_scalars")
+
+    def sync(self):
+        self._chk(self.L.dcg_sync(self.h), "sync")
+
+    def set_emission(self, field):
+        """Emission field (emission_n^3, x fastest) from a host array or a CUDA
+        torch tensor (pinned host tensors are copied asynchronously)."""
+        if hasattr(field, "data_ptr"):
+            where = capi.DEVICE if field.is_cuda else capi.HOST
+            self._chk(self.L.dcg_set_emission(self.h, C.c_void_p(field.data_ptr()), where), "set_emission")
+            return
+        a = np.ascontiguousarray(field, np.float32)
+        self._emis_keep = a
+        self._chk(self.L.dcg_set_emission(self.h, _ptr(a), capi.HOST), "set_emission")
+
+    def add_velocity_noise(self, seed, amplitude):
+        self._chk(self.L.dcg_add_velocity_noise(self.h, seed, amplitude), "noise")
+
+    # -- access -----------------------------------------------------------
+    @property
+    def num_cells(self):
+        return int(self.info.num_cells)
+
+    def get_field(self, field, out=None):
+        """Host copy (float32 numpy) in the canonical layout, or, when `out` is a
+        CUDA torch tensor, a device-to-device copy into it."""
+        fid = _field_id(field)
+        if out is not None and hasattr(out, "data_ptr") and out.is_cuda:
+            self._chk(self.L.dcg_get_field(self.h, fid, C.c_void_p(out.data_ptr()), capi.DEVICE), "get_field")
+            return out
+        a = np.empty(self.num_cells, np.float32) if out is None else out
+        self._chk(self.L.dcg_get_field(self.h, fid, _ptr(a), capi.HOST), "get_field")
+        return a
+
+    def set_field(self, field, values):
+        fid = _field_id(field)
+        if hasattr(values, "data_ptr") and values.is_cuda:
+            self._chk(self.L.dcg_set_field(self.h, fid, C.c_void_p(values.data_ptr()), capi.DEVICE), "set_field")
+            return
+        a = np.ascontiguousarray(values, np.float32)
+        self._chk(self.L.dcg_set_field(self.h, fid, _ptr(a), capi.HOST), "set_field")
+
+    def get_dense(self, field):
+        p = self.params
+        a = np.empty(p.gx * p.gy * p.gz, np.float32)
+        self._chk(self.L.dcg_get_dense(self.h, _field_id(field), _ptr(a), capi.HOST), "get_dense")
+        return a.reshape(p.gz, p.gy, p.gx)
+
+    def get_topology(self):
+        B = int(self.info.max_blocks)
+        lv = int(self.info.levels)
+        pos = np.empty(4 * B, np.int32)
+        parent = np.empty(B, np.uint32)
+        child = np.empty(8 * B, np.uint32)
+        flags = np.empty(B, np.uint8)
+        load = np.zeros(16, np.int64)
+        ml = np.zeros(16, np.int64)
+        self._chk(self.L.dcg_get_topology(self.h, _ptr(pos), _ptr(parent), _ptr(child), _ptr(flags),
+                                          _ptr(load), _ptr(ml)), "get_topology")
+        return dict(pos=pos.reshape(B, 4), parent=parent, child=child.reshape(B, 8), flags=flags,
+                    load=load[:lv], move_limit=ml[:lv])
+
+    def set_topology(self, topo):
+        pos = np.ascontiguousarray(topo["pos"], np.int32)
+        parent = np.ascontiguousarray(topo["parent"], np.uint32)
+        child = np.ascontiguousarray(topo["child"], np.uint32)
+        load = np.zeros(16, np.int64)
+        load[: len(topo["load"])] = topo["load"]
+        ml = np.zeros(16, np.int64)
+        if "move_limit" in topo:
+            ml[: len(topo["move_limit"])] = topo["move_limit"]
+        self._chk(self.L.dcg_set_topology(self.h, _ptr(pos), _ptr(parent), _ptr(child), _ptr(load), _ptr(ml)),
+                  "set_topology")
+
+    def get_apron(self):
+        B = int(self.info.max_blocks)
+        a = np.empty(216 * B, np.int64)
+        self._chk(self.L.dcg_get_apron(self.h, _ptr(a)), "get_apron")
+        return a.reshape(B, 216)
+
+    def get_last_adapt(self):
+        nm, nr = C.c_int64(), C.c_int64()
+        self._chk(self.L.dcg_get_last_adapt(self.h, None, C.byref(nm), None, C.byref(nr)), "last_adapt")
+        moves = np.empty(2 * nm.value, np.int64)
+        refines = np.empty(2 * nr.value, np.int64)
+        self._chk(self.L.dcg_get_last_adapt(self.h, _ptr(moves), C.byref(nm), _ptr(refines), C.byref(nr)),
+                  "last_adapt")
+        return moves.reshape(-1, 2), refines.reshape(-1, 2)
+
+    def time_kernel(self, which, level=0, reps=20):
+        """(mean ms per launch, algorithmic bytes per launch) of one kernel."""
+        ms, by = C.c_float(), C.c_double()
+        self._chk(self.L.dcg_time_kernel(self.h, which, level, reps, C.byref(ms), C.byref(by)), "time_kernel")
+        return float(ms.value), float(by.value)
+
+    def launches_per_step(self):
+        n = C.c_int64()
+        self._chk(self.L.dcg_launches_per_step(self.h, C.byref(n)), "launches_per_step")
+        return int(n.value)
+
+    def stats(self):
+        st = capi.DcgStats()
+        self._chk(self.L.dcg_get_stats(self.h, C.byref(st)), "stats")
+        return st
+
+
+class FluidSimulationDCGrid(Simulation):
+    """FluidSimulationDCGrid(const int3 &size, const size_t &maxNumBlocks)
+    (src/dcgrid/fluid_simulation_dcgrid.h:7) with the reference's method names."""
+
+    def __init__(self, size, maxNumBlocks, params=None):
+        p = params if params is not None else default_params(size[0], size[1], size[2], maxNumBlocks)
+        p.gx, p.gy, p.gz = size
+        p.max_blocks = maxNumBlocks
+        super().__init__(p, capi.MODE_ADAPTIVE)
+
+    def init(self):
+        self.reset()
+
+    def adaptTopology(self):
+        self.adapt()
+
+    def advectVelocity(self):
+        self.advect_velocity()
+
+    def projectLocal(self):
+        self.project_local()
+
+    def advectDensity(self):
+        self.advect_scalars()
+
+    def debugStats(self):
+        return self.stats().residual
+
+
+class FluidSimulationUniform(Simulation):
+    """FluidSimulationUniform(const int3 &size) (fluid_simulation_uniform.h:7)."""
+
+    def __init__(self, size, params=None):
+        p = params if params is not None else default_params(size[0], size[1], size[2], 0)
+        p.gx, p.gy, p.gz = size
+        super().__init__(p, capi.MODE_UNIFORM)
+
+    def init(self):
+        self.reset()
+
+    def adaptTopology(self):
+        self.adapt()
+
+    def advectVelocity(self):
+        self.advect_velocity()
+
+    def projectLocal(self):
+        self.project_local()
+
+    def advectDensity(self):
+        self.advect_scalars()
+
+    def debugStats(self):
+        return self.stats().mass

@@ -111,7 +111,13 @@ typedef struct dcg_params {
   uint32_t terrain_seed;
 
   int32_t precision;         /* DCG_PRECISION_*                              */
-  int32_t reserved[8];
+
+  /* extension: an emission_n^3 density-emission field (set with
+   * dcg_set_emission) spanning x, z and the bottom emission_band cells in y;
+   * leaf cells there gain dt * E(trilinear) of density every step. */
+  int32_t emission_n;        /* 0 = no emission field                        */
+  float emission_band;       /* finest cells                                 */
+  int32_t reserved[6];
 } dcg_params;
 
 /* Fills *p with the reference's defaults (src/data/sim_params.cpp:4-34) for a
@@ -196,6 +202,11 @@ int dcg_project_local(dcg_sim *sim);       /* projectLocal                      
 int dcg_advect_scalars(dcg_sim *sim);      /* advectDensity (+ temperature, vapor, sources) */
 int dcg_sync(dcg_sim *sim);                /* wait for the handle's stream; read device error word */
 
+/* Sets the emission field (emission_n^3 floats, x fastest) from host or
+ * device memory. The copy is ordered on the handle's stream before later
+ * steps; the step reads it in place, so it may change between steps. */
+int dcg_set_emission(dcg_sim *sim, const float *field, int32_t where);
+
 /* Adds seeded uniform noise in [-amplitude, amplitude] to every velocity
  * component of every allocated cell (deterministic counter-based hash). */
 int dcg_add_velocity_noise(dcg_sim *sim, uint64_t seed, float amplitude);
@@ -236,6 +247,23 @@ int dcg_get_last_adapt(dcg_sim *sim, int64_t *moves, int64_t *n_moves,
                        int64_t *refines, int64_t *n_refines);
 
 int dcg_get_stats(dcg_sim *sim, dcg_stats *stats);
+
+/* ---- extras without a counterpart in the reference -------------------- */
+/* dcg_step replays a captured CUDA graph of the whole step (default on). */
+int dcg_set_graphs(dcg_sim *sim, int32_t on);
+/* Times `reps` launches of one kernel on the current state with CUDA events
+ * on the handle's stream; *avg_ms = mean duration of one launch, *bytes =
+ * algorithmic bytes of one launch. which: 0 = Jacobi sweep of `level`,
+ * 1 = velocity advection, 2 = scalar advection, 3 = divergence. */
+int dcg_time_kernel(dcg_sim *sim, int32_t which, int32_t level, int32_t reps,
+                    float *avg_ms, double *bytes);
+/* Number of kernel launches one dcg_step performs (kernel nodes of the
+ * captured step graph; 0 before the first graph capture). */
+int dcg_launches_per_step(dcg_sim *sim, int64_t *n);
+/* sizeof of the ABI structs, for binding checks. */
+size_t dcg_sizeof_params(void);
+size_t dcg_sizeof_info(void);
+size_t dcg_sizeof_stats(void);
 
 #ifdef __cplusplus
 }

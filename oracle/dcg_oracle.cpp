@@ -112,6 +112,7 @@ struct Base {
   virtual int set_field(int f, const double *src) = 0;
   virtual int get_dense(int f, double *dst) = 0;
   virtual int stats(dcg_stats *st) = 0;
+  virtual int set_emission(const double *src) = 0;
   int fail(int code, const char *msg) {
     err = msg;
     return code;
@@ -227,6 +228,31 @@ template <typename R> struct Physics {
     const R cz = ((R)z + (R)0.5f) * s - (R)P->src_center[2];
     return cx * cx + cy * cy + cz * cz < (R)P->src_radius * (R)P->src_radius;
   }
+  // Emission field (extension): trilinear sample of the n^3 field over the
+  // domain's x, z and the bottom emission_band cells in y; 0 outside the band.
+  const std::vector<R> *em = nullptr;
+  static R lerp(R a, R b, R t) { return a + (b - a) * t; }
+  R emission_at(int x, int y, int z, int scale) const {
+    const int n = P->emission_n;
+    if (n <= 0 || !em || em->empty()) return 0;
+    const R s = (R)scale;
+    const R yw = ((R)y + (R)0.5f) * s;
+    if (!(yw < (R)P->emission_band)) return 0;
+    const R xw = ((R)x + (R)0.5f) * s, zw = ((R)z + (R)0.5f) * s;
+    const R top = (R)(n - 1);
+    const R u = clampr(xw * ((R)n / (R)gx) - (R)0.5f, (R)0, top);
+    const R v = clampr(yw * ((R)n / (R)P->emission_band) - (R)0.5f, (R)0, top);
+    const R w = clampr(zw * ((R)n / (R)gz) - (R)0.5f, (R)0, top);
+    const int i0 = (int)std::floor(u), j0 = (int)std::floor(v), k0 = (int)std::floor(w);
+    const int i1 = i0 + 1 < n ? i0 + 1 : n - 1, j1 = j0 + 1 < n ? j0 + 1 : n - 1, k1 = k0 + 1 < n ? k0 + 1 : n - 1;
+    const R fu = u - (R)i0, fv = v - (R)j0, fw = w - (R)k0;
+    auto at = [&](int i, int j, int k) { return (*em)[((size_t)k * n + j) * n + i]; };
+    const R e00 = lerp(at(i0, j0, k0), at(i1, j0, k0), fu);
+    const R e10 = lerp(at(i0, j1, k0), at(i1, j1, k0), fu);
+    const R e01 = lerp(at(i0, j0, k1), at(i1, j0, k1), fu);
+    const R e11 = lerp(at(i0, j1, k1), at(i1, j1, k1), fu);
+    return lerp(lerp(e00, e10, fv), lerp(e01, e11, fv), fw);
+  }
   R src_value(int k) const {
     return k == 0 ? (R)P->src_density : (k == 1 ? (R)P->src_temperature : (R)P->src_vapor);
   }
@@ -249,6 +275,13 @@ template <typename R> struct DC : Base {
   std::vector<float> ss, bs;
   std::vector<int64_t> lastMoves, lastRefines, touched;
   int64_t lastMovedCount = 0, lastRefinedCount = 0;
+  std::vector<R> emis;
+  int set_emission(const double *src) override {
+    const int n = P.emission_n;
+    if (n <= 0) return fail(DCG_E_INVALID, "created with emission_n = 0");
+    emis.assign(src, src + (size_t)n * n * n);
+    return DCG_OK;
+  }
 
   R rdx() const { return ph.rdx; }
 
@@ -266,6 +299,8 @@ template <typename R> struct DC : Base {
     rdx_f = 1.f / P.dx;
     ph.P = &P; ph.rdx = (R)rdx_f; ph.dt = (R)P.dt; ph.dx = (R)P.dx;
     ph.gx = gx; ph.gy = gy; ph.gz = gz;
+    if (P.emission_n > 0) emis.assign((size_t)P.emission_n * P.emission_n * P.emission_n, (R)0);
+    ph.em = &emis;
     const int minDim = std::min(gx, std::min(gy, gz));
     int cellSize = 2;
     levels = 1;
@@ -635,6 +670,8 @@ template <typename R> struct DC : Base {
           for (int k = 0; k < nq; k++) tq[k][cell] = sample_scalar(s, k);
           int x, y, z;
           local_xyz(c, x, y, z);
+          if (P.emission_n > 0)
+            tq[0][cell] = tq[0][cell] + ph.dt * ph.emission_at(bx[b] + x, by[b] + y, bz[b] + z, 1 << lvl[b]);
           if (ph.in_source(bx[b] + x, by[b] + y, bz[b] + z, 1 << lvl[b]))
             for (int k = 0; k < nq; k++) tq[k][cell] = ph.src_value(k);
         } else {
@@ -1253,6 +1290,13 @@ template <typename R> struct UG : Base {
   int gx = 0, gy = 0, gz = 0, levels = 0;
   size_t nc = 0, nmip = 0;
   int nq = 1;
+  std::vector<R> emis;
+  int set_emission(const double *src) override {
+    const int n = P.emission_n;
+    if (n <= 0) return fail(DCG_E_INVALID, "created with emission_n = 0");
+    emis.assign(src, src + (size_t)n * n * n);
+    return DCG_OK;
+  }
   std::vector<R> q[3], v[3], w, p, pt, dv, tv[3], tq[3];
 
   // mipmapCells / mipmapIdx (src/utils/grid_math.cuh:24-52)
@@ -1280,6 +1324,8 @@ template <typename R> struct UG : Base {
     rdx_f = 1.f / P.dx;
     ph.P = &P; ph.rdx = (R)rdx_f; ph.dt = (R)P.dt; ph.dx = (R)P.dx;
     ph.gx = gx; ph.gy = gy; ph.gz = gz;
+    if (P.emission_n > 0) emis.assign((size_t)P.emission_n * P.emission_n * P.emission_n, (R)0);
+    ph.em = &emis;
     // FluidSimulationUniform ctor (fluid_simulation_uniform.cu:6-18)
     const int minDim = std::min(gx, std::min(gy, gz));
     int cellSize = 2;
@@ -1432,6 +1478,7 @@ template <typename R> struct UG : Base {
                 const R qc = ph.q_bc(q[k][s.idx[c]], k, cx, cy, cz, 1);
                 out = (c == 0) ? qc * s.wt[c] : out + qc * s.wt[c];
               }
+            if (k == 0 && P.emission_n > 0) out = out + ph.dt * ph.emission_at(x, y, z, 1);
             tq[k][i] = out;
           }
           if (ph.in_source(x, y, z, 1))
@@ -1811,6 +1858,9 @@ int dcgo_get_scores(dcgo_sim *s, float *subblock, float *block) {
     if (block) std::copy(d.bs.begin(), d.bs.end(), block);
     return DCG_OK;
   });
+}
+int dcgo_set_emission(dcgo_sim *s, const double *src) {
+  return s && src ? s->impl->set_emission(src) : DCG_E_INVALID;
 }
 int dcgo_get_stats(dcgo_sim *s, dcg_stats *st) { return s && st ? s->impl->stats(st) : DCG_E_INVALID; }
 

@@ -71,6 +71,7 @@ int dcgo_adapt_replay(dcgo_sim *s, const int64_t *moves, int64_t n_moves,
 /* Subblock / block scores of the current state (float, 8*B and B entries). */
 int dcgo_get_scores(dcgo_sim *s, float *subblock, float *block);
 int dcgo_get_stats(dcgo_sim *s, dcg_stats *st);
+int dcgo_set_emission(dcgo_sim *s, const double *src);
 
 #ifdef __cplusplus
 }

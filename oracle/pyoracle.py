@@ -53,6 +53,7 @@ def lib():
         L.dcgo_adapt_replay.argtypes = [vp, vp, C.c_int64, vp, C.c_int64]
         L.dcgo_get_scores.argtypes = [vp, vp, vp]
         L.dcgo_get_stats.argtypes = [vp, C.POINTER(capi.DcgStats)]
+        L.dcgo_set_emission.argtypes = [vp, vp]
         _lib = L
     return _lib
 
@@ -111,6 +112,10 @@ class OracleSim:
     @property
     def num_cells(self):
         return int(self.info.num_cells)
+
+    def set_emission(self, field):
+        a = np.ascontiguousarray(field, dtype=np.float64).reshape(-1)
+        self._chk(self.L.dcgo_set_emission(self.h, _ptr(a)), "set_emission")
 
     def get_field(self, field):
         fid = capi.FIELD_NAMES[field] if isinstance(field, str) else field

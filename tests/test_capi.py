@@ -1,0 +1,53 @@
+"""CPU checks of the C-ABI library: it loads, exports every function
+include/dcg.h declares, the ctypes struct mirrors match the C layouts, and
+the Python default parameters equal dcg_default_params. No compute calls."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from dcgrid_gb300 import capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", h)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            names |= set(re.findall(r"\b(dcg_[a-z0-9_]+)\s*\(", txt))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol(dcg_lib):
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(dcg_lib, n)]
+    assert not missing, missing
+
+
+def test_struct_layouts(dcg_lib):
+    assert dcg_lib.dcg_sizeof_params() == C.sizeof(capi.DcgParams)
+    assert dcg_lib.dcg_sizeof_info() == C.sizeof(capi.DcgInfo)
+    assert dcg_lib.dcg_sizeof_stats() == C.sizeof(capi.DcgStats)
+
+
+def test_python_defaults_match_c_defaults(dcg_lib):
+    from dcgrid_gb300 import sim
+    a = sim.default_params(256, 256, 256, 40000)
+    b = capi.default_params(256, 256, 256, 40000)
+    assert capi.params_to_dict(a) == pytest.approx(capi.params_to_dict(b))
+
+
+def test_null_handles_are_rejected(dcg_lib):
+    assert dcg_lib.dcg_step(None, 1) == capi.DCG_E_INVALID
+    assert dcg_lib.dcg_destroy(None) == capi.DCG_E_INVALID
+    assert dcg_lib.dcg_create(None, 0, None) == capi.DCG_E_INVALID
+
+
+def test_oracle_exports(oracle_lib):
+    for n in ["dcgo_create", "dcgo_step", "dcgo_get_field", "dcgo_apron_mismatches", "dcgo_adapt_replay"]:
+        assert hasattr(oracle_lib, n)

@@ -1,0 +1,250 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle on the same
+inputs.
+
+* FP32 path vs the oracle's float mirror of the reference arithmetic: bit-exact,
+  stage by stage, for fields, block table, neighbour-derived apron tables and
+  adaptation decisions.
+* FP32 path vs the FP64 oracle: relative L2 error per field within 1e-4.
+"""
+import numpy as np
+import pytest
+
+from dcgrid_gb300 import capi
+from tests import scenarios
+
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("cuda_ok", "dcg_lib", "oracle_lib")]
+
+NONE = 0xFFFFFFFF
+
+
+def gpu(p, mode=capi.MODE_ADAPTIVE):
+    from dcgrid_gb300 import Simulation
+    return Simulation(p, mode)
+
+
+def orc(p, prec="float", mode=capi.MODE_ADAPTIVE):
+    from oracle.pyoracle import OracleSim
+    return OracleSim(p, mode=mode, precision=prec)
+
+
+def field_names(p):
+    f = ["density", "vel_x", "vel_y", "vel_z", "fluidity", "pressure", "pressure_tmp", "divergence"]
+    if p.n_scalars == 3:
+        f += ["temperature", "vapor"]
+    return f
+
+
+def topo_diffs(g, o):
+    tg, to = g.get_topology(), o.get_topology()
+    out = []
+    alloc = to["pos"][:, 3] >= 0
+    if not np.array_equal(tg["pos"][:, 3], to["pos"][:, 3]):
+        out.append(f"levels differ in {(tg['pos'][:, 3] != to['pos'][:, 3]).sum()} blocks")
+    if not np.array_equal(tg["pos"][alloc], to["pos"][alloc]):
+        out.append(f"positions differ in {(tg['pos'][alloc] != to['pos'][alloc]).any(1).sum()} blocks")
+    if not np.array_equal(tg["parent"][alloc], to["parent"][alloc]):
+        out.append("parents differ")
+    if not np.array_equal(tg["child"][alloc], to["child"][alloc]):
+        out.append("children differ")
+    if not np.array_equal(tg["load"], to["load"]):
+        out.append(f"loads differ {tg['load']} vs {to['load']}")
+    if not np.array_equal(tg["move_limit"], to["move_limit"]):
+        out.append(f"move limits differ {tg['move_limit']} vs {to['move_limit']}")
+    return out, alloc
+
+
+def field_diffs(g, o, p, alloc):
+    cells = np.repeat(alloc, 64)
+    out = []
+    for f in field_names(p):
+        a = g.get_field(f)[cells]
+        b = o.get_field(f)[cells].astype(np.float32)
+        bad = ~((a == b) | (np.isnan(a) & np.isnan(b)))
+        if bad.any():
+            d = np.abs(a.astype(np.float64) - b.astype(np.float64))[bad]
+            out.append(f"{f}: {bad.sum()} cells differ, max |diff| {d.max():.3g}")
+    return out
+
+
+def compare(g, o, p, where):
+    td, alloc = topo_diffs(g, o)
+    assert not td, f"{where}: {td}"
+    fd = field_diffs(g, o, p, alloc)
+    assert not fd, f"{where}: {fd}"
+
+
+SCENARIOS = {
+    "ref_default": lambda: scenarios.ref_default(32, 64, 32, 600),
+    "ref_sphere": lambda: scenarios.sphere_obstacle(64, 128, 64, 3000),
+    "ref_nocompat": lambda: (lambda p: (setattr(p, "ref_compat", 0), p)[1])(scenarios.ref_default(64, 128, 64, 3000)),
+    "plume": lambda: scenarios.plume(32, 64, 32, None, 2, 20),
+    "cloud": lambda: scenarios.cloud(64, 1500, 3, 10, 0),
+    "cloud_compat": lambda: scenarios.cloud(64, 1500, 3, 10, 1),
+}
+
+
+@pytest.mark.parametrize("name", list(SCENARIOS))
+def test_stagewise_bitexact_vs_float_oracle(name):
+    p = SCENARIOS[name]()
+    g, o = gpu(p), orc(p)
+    compare(g, o, p, "after init")
+    for s in (g, o):
+        s.add_velocity_noise(11, 0.5 if name.startswith("cloud") else 0.01)
+    compare(g, o, p, "after noise")
+    topo_changes = 0
+    for step in range(4):
+        for stage in ["advect_velocity", "adapt", "project", "advect_scalars"]:
+            getattr(g, stage)()
+            getattr(o, stage)()
+            g.sync()
+            compare(g, o, p, f"step {step} {stage}")
+            if stage == "adapt":
+                mg, rg = g.get_last_adapt()
+                mo, ro = o.get_last_adapt()
+                assert np.array_equal(mg, mo), f"step {step}: moves differ"
+                assert np.array_equal(rg, ro), f"step {step}: refinements differ"
+                topo_changes += len(mg) + len(rg)
+    if name.startswith("cloud") or name == "ref_nocompat":
+        assert topo_changes > 0
+
+
+@pytest.mark.parametrize("name", ["ref_default", "ref_sphere", "cloud"])
+def test_apron_tables_match_reference_format(name):
+    p = SCENARIOS[name]()
+    g, o = gpu(p), orc(p)
+    for s in (g, o):
+        s.add_velocity_noise(2, 0.5)
+        s.step(3)
+    ag, ao = g.get_apron(), o.get_apron()
+    alloc = o.get_topology()["pos"][:, 3] >= 0
+    assert np.array_equal(ag[alloc], ao[alloc])
+
+
+def test_graph_step_equals_stage_calls():
+    p = scenarios.cloud(64, 1500, 3, 10, 0)
+    a, b = gpu(p), gpu(p)
+    b.set_graphs(False)
+    for s in (a, b):
+        s.add_velocity_noise(4, 0.5)
+    a.step(5)
+    for _ in range(5):
+        b.advect_velocity(); b.adapt(); b.project(); b.advect_scalars()
+    b.sync()
+    for f in field_names(p):
+        assert np.array_equal(a.get_field(f), b.get_field(f)), f
+    ta, tb = a.get_topology(), b.get_topology()
+    assert np.array_equal(ta["pos"], tb["pos"]) and np.array_equal(ta["child"], tb["child"])
+
+
+@pytest.mark.parametrize("name", ["plume", "ref_default"])
+def test_fp32_vs_fp64_oracle(name):
+    """FP32 GPU path against the FP64 oracle: relative L2 error <= 1e-4 per field
+    after 5 steps (same topology: geometric refinement is field independent)."""
+    p = SCENARIOS[name]()
+    g, o = gpu(p), orc(p, "double")
+    for s in (g, o):
+        s.add_velocity_noise(0, 0.01)
+        s.step(5)
+    g.sync()
+    td, alloc = topo_diffs(g, o)
+    assert not td
+    cells = np.repeat(alloc, 64)
+    for f in ["density", "vel_x", "vel_y", "vel_z", "pressure"]:
+        a = g.get_field(f)[cells].astype(np.float64)
+        b = o.get_field(f)[cells]
+        nb = np.linalg.norm(b)
+        if nb == 0:
+            assert np.linalg.norm(a) == 0
+            continue
+        assert np.linalg.norm(a - b) / nb <= 1e-4, f
+
+
+def test_uniform_mode_bitexact():
+    p = scenarios.plume(32, 64, 32, None, 0, 10)
+    p.levels = 0
+    g, o = gpu(p, capi.MODE_UNIFORM), orc(p, "float", capi.MODE_UNIFORM)
+    for s in (g, o):
+        s.add_velocity_noise(9, 0.1)
+    for step in range(3):
+        for stage in ["advect_velocity", "adapt", "project", "advect_scalars"]:
+            getattr(g, stage)()
+            getattr(o, stage)()
+        g.sync()
+        for f in ["density", "temperature", "vel_x", "vel_y", "vel_z", "pressure"]:
+            a, b = g.get_field(f), o.get_field(f).astype(np.float32)
+            assert np.array_equal(a, b), f"step {step} {f}: {(a != b).sum()} cells differ"
+
+
+def test_uniform_reference_counts_and_project_local():
+    p = scenarios.ref_default(32, 64, 32, 0)
+    g, o = gpu(p, capi.MODE_UNIFORM), orc(p, "float", capi.MODE_UNIFORM)
+    for s in (g, o):
+        s.step(2)
+        s.project_local()
+    g.sync()
+    for f in ["density", "vel_y", "pressure"]:
+        assert np.array_equal(g.get_field(f), o.get_field(f).astype(np.float32)), f
+
+
+def test_project_local_bitexact():
+    p = scenarios.plume(32, 64, 32, None, 2, 10)
+    g, o = gpu(p), orc(p)
+    for s in (g, o):
+        s.add_velocity_noise(1, 0.2)
+        s.project_local()
+    g.sync()
+    compare(g, o, p, "project_local")
+
+
+def test_dense_and_stats_match():
+    p = scenarios.cloud(64, 1500, 3, 10, 0)
+    g, o = gpu(p), orc(p)
+    for s in (g, o):
+        s.add_velocity_noise(3, 0.5)
+        s.step(3)
+    g.sync()
+    assert np.array_equal(g.get_dense("density"), o.get_dense("density").astype(np.float32))
+    sg, so = g.stats(), o.stats()
+    assert list(sg.leaf_cells) == list(so.leaf_cells)
+    assert sg.active_cells == so.active_cells
+    assert sg.mass == pytest.approx(so.mass, rel=1e-9)
+    assert sg.residual == pytest.approx(so.residual, rel=1e-9)
+    assert sg.device_error == 0
+
+
+def test_device_resident_field_access():
+    import torch
+    p = scenarios.plume(32, 64, 32, None, 2, 10)
+    g = gpu(p)
+    t = torch.empty(g.num_cells, dtype=torch.float32, device="cuda")
+    g.get_field("fluidity", out=t)
+    torch.cuda.synchronize()
+    assert np.array_equal(t.cpu().numpy(), g.get_field("fluidity"))
+    t.fill_(0.25)
+    g.set_field("density", t)
+    assert (g.get_field("density") == 0.25).all()
+
+
+def test_mode_switch_recreates():
+    from dcgrid_gb300 import Simulation
+    p = scenarios.ref_default(32, 64, 32, 600)
+    s = Simulation(p)
+    s.step(1)
+    s.set_mode(capi.MODE_UNIFORM)
+    assert s.info.mode == capi.MODE_UNIFORM and s.info.num_cells == 32 * 64 * 32
+    s.step(1)
+    s.set_mode(capi.MODE_ADAPTIVE)
+    assert s.info.max_blocks == 600
+
+
+def test_invalid_configurations_return_status():
+    from dcgrid_gb300 import DcgError, Simulation
+    p = scenarios.ref_default(32, 64, 32, 1)
+    with pytest.raises(DcgError) as e:
+        Simulation(p)
+    assert e.value.code == capi.DCG_E_BUDGET
+    p = scenarios.ref_default(40, 64, 32, 600)
+    p.levels = 4
+    with pytest.raises(DcgError) as e:
+        Simulation(p)
+    assert e.value.code == capi.DCG_E_INVALID
