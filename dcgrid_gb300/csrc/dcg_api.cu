@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -931,3 +932,76 @@ size_t dcg_sizeof_info(void) { return sizeof(dcg_info); }
 size_t dcg_sizeof_stats(void) { return sizeof(dcg_stats); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Dense read-out without device allocation.
+//
+// dcg_get_dense stages the resampled volume in a device buffer that it
+// cudaMallocs on its first call. Some callers cannot allocate at that point:
+// code running while a stream is being captured into a CUDA graph (an
+// allocation there breaks or invalidates the capture), hosts that hand the
+// library a fixed device-memory budget up front, and real-time loops that must
+// not hit the allocator's synchronisation. dcg_get_dense_noalloc runs the same
+// resampling kernel but stages through the fixed array below, so the call
+// itself allocates nothing.
+//
+// The array is a file-scope __device__ variable: every GPU that loads this
+// library holds its 4 MiB until the process exits. In host code its name is
+// only a host-side shadow, not a device address, so the kernel is given the
+// address that cudaGetSymbolAddress returns, looked up once per device with
+// that device current.
+namespace {
+constexpr size_t kDenseScratchCells = size_t(1) << 20;  // 4 MiB of float
+static __device__ __align__(256) float g_dense_scratch[kDenseScratchCells];
+
+std::mutex g_scratch_mu;
+float *g_scratch_ptr[64] = {};
+
+int dense_scratch_for_device(int device, float **out, std::string &err) {
+  if (device < 0 || device >= 64) {
+    err = "device ordinal out of range for the no-allocation scratch";
+    return DCG_E_INVALID;
+  }
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_ptr[device]) {
+    int prev = -1;
+    cudaError_t e = cudaGetDevice(&prev);
+    if (e == cudaSuccess && prev != device) e = cudaSetDevice(device);
+    void *p = nullptr;
+    if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_dense_scratch);
+    if (prev >= 0 && prev != device) cudaSetDevice(prev);
+    if (e != cudaSuccess) {
+      err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+      return DCG_E_CUDA;
+    }
+    g_scratch_ptr[device] = static_cast<float *>(p);
+  }
+  *out = g_scratch_ptr[device];
+  return DCG_OK;
+}
+}  // namespace
+
+extern "C" int dcg_get_dense_noalloc(dcg_sim *s, int32_t field, float *dst, int32_t where) {
+  if (bad(s) || !dst) return DCG_E_INVALID;
+  if (s->mode == DCG_MODE_UNIFORM) return dcg_get_field(s, field, dst, where);  // no staging needed
+  float *src = field_ptr(s, field);
+  if (!src) return s->fail(DCG_E_NOT_FOUND, "no such field");
+  const size_t n = (size_t)s->P.gx * s->P.gy * s->P.gz;
+  if (n > kDenseScratchCells) {
+    char buf[160];
+    std::snprintf(buf, sizeof buf,
+                  "dense volume of %zu cells exceeds the %zu-cell scratch of dcg_get_dense_noalloc; "
+                  "use dcg_get_dense", n, kDenseScratchCells);
+    return s->fail(DCG_E_INVALID, buf);
+  }
+  float *scratch = nullptr;
+  int rc = dense_scratch_for_device(s->device, &scratch, s->err);
+  if (rc) return rc;
+  // The kernel writes every one of the n staged cells, so nothing needs zeroing.
+  launch_fields_to_dense(s->D, src, scratch, s->stream);
+  rc = s->cuda(cudaMemcpyAsync(dst, scratch, n * 4,
+                               where == DCG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s->stream),
+               "get_dense_noalloc");
+  if (rc) return rc;
+  return s->sync("get_dense_noalloc");
+}

@@ -221,6 +221,18 @@ int dcg_set_field(dcg_sim *sim, int32_t field, const float *src, int32_t where);
 /* Dense gx*gy*gz x-fastest resampling: each finest cell takes the value of the
  * leaf cell that covers it. */
 int dcg_get_dense(dcg_sim *sim, int32_t field, float *dst, int32_t where);
+/* Same result as dcg_get_dense, but the call allocates no device memory.
+ * No counterpart in the reference. dcg_get_dense cudaMallocs a staging buffer
+ * on its first call; callers that cannot allocate at that moment - code that
+ * runs while a stream is being captured into a CUDA graph, hosts that give the
+ * library a fixed memory budget up front, loops that must not wait on the
+ * allocator - use this variant. It stages through a fixed device array of
+ * 2^20 floats (4 MiB, held by every GPU that loads the library until exit),
+ * so domains of more than 2^20 finest cells are rejected with DCG_E_INVALID.
+ * The first call on a device looks the array up (cudaGetSymbolAddress), so
+ * make that first call before any stream capture. All calls on a device share
+ * the array: calls that overlap on the GPU (other streams or handles) race. */
+int dcg_get_dense_noalloc(dcg_sim *sim, int32_t field, float *dst, int32_t where);
 
 /* Block table, host buffers sized by dcg_info.max_blocks:
  *   pos[4*b] = x, y, z (level-local cells), level (-1 = free)
