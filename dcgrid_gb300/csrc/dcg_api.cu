@@ -56,6 +56,7 @@ struct dcg_sim {
   std::map<int, cudaGraphExec_t> graphs;
   bool use_graphs = true;
   long long kernels_per_step = 0;
+  int ls_grid = 0;  // CTAs of the cooperative level solve (0 = per-sweep launches)
 
   int fail(int code, const std::string &msg) {
     err = msg;
@@ -226,6 +227,8 @@ struct dcg_sim {
     if ((rc = alloc(&D.ctr, C_COUNT))) return rc;
     if ((rc = alloc(&D.err, 4))) return rc;
     if ((rc = alloc(&D.red, 32))) return rc;
+    if ((rc = alloc(&D.bar, 2))) return rc;
+    ls_grid = level_solve_grid(sms);
     if (P.emission_n > 0) {
       const size_t ne = (size_t)P.emission_n * P.emission_n * P.emission_n;
       if ((rc = alloc(&emis, ne))) return rc;
@@ -266,6 +269,7 @@ struct dcg_sim {
     cudaMemsetAsync(D.nbr, 0xff, (size_t)27 * D.g.B * 4, stream);
     cudaMemsetAsync(D.ctr, 0, sizeof(long long) * C_COUNT, stream);
     cudaMemsetAsync(D.err, 0, 4, stream);
+    cudaMemsetAsync(D.bar, 0, 8, stream);
     long long load[MAXL] = {0}, ml[MAXL] = {0};
     for (int l = 0; l < D.g.levels; l++) load[l] = D.g.budget[l] == D.g.full[l] ? D.g.budget[l] : 0;
     if ((rc = cuda(cudaMemcpyAsync(D.load, load, sizeof(load), cudaMemcpyHostToDevice, stream), "load"))) return rc;
@@ -313,7 +317,12 @@ struct dcg_sim {
     launch_divergence(D, stream);
     restrict_div();
     const int top = D.g.levels - 1;
-    if (local) {
+    if (ls_grid > 0) {
+      // one cooperative launch per level: prolongation (not for the coarsest
+      // level, nor in projectLocal) and all of the level's sweeps
+      const int sweeps = local ? 2 * P.jacobi_iters : P.jacobi_iters;
+      for (int l = top; l >= 0; l--) launch_level_solve(D, l, (!local && l < top) ? 1 : 0, sweeps, ls_grid, stream);
+    } else if (local) {
       const int pairs = P.jacobi_iters;
       for (int l = top; l >= 0; l--)
         for (int i = 0; i < pairs; i++) {
@@ -894,9 +903,11 @@ int dcg_time_kernel(dcg_sim *s, int32_t which, int32_t level, int32_t reps, floa
         break;
       case 1: launch_advect_velocity(s->D, s->stream); break;
       case 2: launch_advect_scalars(s->D, s->stream); break;
+      case 4: launch_level_solve(s->D, level, 0, s->P.jacobi_iters, s->ls_grid, s->stream); break;
       default: launch_divergence(s->D, s->stream); break;
     }
   };
+  if (which == 4 && s->ls_grid <= 0) return s->fail(DCG_E_INVALID, "no cooperative level solve on this device");
   launch(0);  // warm
   cudaEventRecord(e0, s->stream);
   for (int i = 0; i < reps; i++) launch(i);
@@ -915,6 +926,7 @@ int dcg_time_kernel(dcg_sim *s, int32_t which, int32_t level, int32_t reps, floa
       case 0: *bytes = 12.0 * cells_level; break;                  // p r, div r, p~ w
       case 1: *bytes = 24.0 * cells_all; break;                    // v r, v w
       case 2: *bytes = (12.0 + 8.0 * nq) * cells_all; break;       // v r, q r/w
+      case 4: *bytes = 12.0 * cells_level * s->P.jacobi_iters; break;  // per sweep: p r, div r, p~ w
       default: *bytes = 16.0 * cells_all; break;                   // v r, div w
     }
   }

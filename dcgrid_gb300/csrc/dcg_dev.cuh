@@ -88,7 +88,40 @@ struct Dev {
   long long *ctr;          // C_COUNT counters
   uint32_t *err;           // device error word
   double *red;             // reductions (stats)
+  uint32_t *bar;           // grid barrier {arrivals, generation}
 };
+
+// Grid-wide barrier for cooperative launches (all CTAs co-resident). The wait
+// is bounded: after 2^22 polls the CTA records DCG_DEVERR_TIMEOUT (8) in the
+// error word and continues; once that bit is set every later barrier returns
+// at once, so a broken barrier costs one bounded wait and never hangs the GPU.
+__device__ inline void grid_barrier(const Dev &D, unsigned nctas) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *gen = D.bar + 1;
+    volatile unsigned *err = D.err;
+    if ((*err & 8u) == 0) {
+      const unsigned g = *gen;
+      __threadfence();
+      if (atomicAdd(D.bar, 1u) == nctas - 1) {
+        atomicExch(D.bar, 0u);
+        __threadfence();
+        atomicAdd(D.bar + 1, 1u);
+      } else {
+        unsigned spins = 0;
+        while (*gen == g) {
+          __nanosleep(32);
+          if (++spins > (1u << 22) || (*err & 8u)) {
+            atomicOr(D.err, 8u);
+            break;
+          }
+        }
+      }
+      __threadfence();
+    }
+  }
+  __syncthreads();
+}
 
 // ---------------------------------------------------------------- index math
 __host__ __device__ inline int spread2(int d, int off) { return ((d & 1) | ((d << 2) & 8)) << off; }

@@ -321,6 +321,112 @@ __global__ void __launch_bounds__(256) k_prolongate(Dev D, int level) {
       (27.f * p000 + 9.f * (p001 + p010 + p100) + 3.f * (p011 + p101 + p110) + p111) / 64.f;
 }
 
+// One cell of k_prolongate, addressed by its global cell index.
+__device__ inline void prolong_cell(const Dev &D, long long cell) {
+  const uint32_t b = (uint32_t)(cell >> 6);
+  const uint32_t par = D.parent[b];
+  if (par == NONE) return;
+  const int4 bp = D.pos[b];
+  const uint32_t pb = par >> 3;
+  const int4 pbp = D.pos[pb];
+  int lx, ly, lz;
+  local_xyz((int)(cell & 63), lx, ly, lz);
+  const int x = bp.x + lx, y = bp.y + ly, z = bp.z + lz;
+  const int ax = 1 + (x / 2) % BW, ay = 1 + (y / 2) % BW, az = 1 + (z / 2) % BW;
+  const int i = x % 2 ? 1 : -1, j = y % 2 ? 1 : -1, k = z % 2 ? 1 : -1;
+  const float *P = D.p;
+  const float p000 = P[apron_cell(D, pb, pbp, ax, ay, az)];
+  const float p001 = P[apron_cell(D, pb, pbp, ax, ay, az + k)];
+  const float p010 = P[apron_cell(D, pb, pbp, ax, ay + j, az)];
+  const float p100 = P[apron_cell(D, pb, pbp, ax + i, ay, az)];
+  const float p011 = P[apron_cell(D, pb, pbp, ax, ay + j, az + k)];
+  const float p101 = P[apron_cell(D, pb, pbp, ax + i, ay, az + k)];
+  const float p110 = P[apron_cell(D, pb, pbp, ax + i, ay + j, az)];
+  const float p111 = P[apron_cell(D, pb, pbp, ax + i, ay + j, az + k)];
+  D.p[cell] = (27.f * p000 + 9.f * (p001 + p010 + p100) + 3.f * (p011 + p101 + p110) + p111) / 64.f;
+}
+
+// The six Jacobi neighbours (L, R, D, U, B, F) of a cell, as global cell indices.
+struct Nb6 {
+  uint32_t i0, i1, i2, i3, i4, i5;
+};
+__device__ inline Nb6 jacobi_neighbours(const Dev &D, long long cell) {
+  const uint32_t b = (uint32_t)(cell >> 6);
+  const int4 bp = D.pos[b];
+  int lx, ly, lz;
+  local_xyz((int)(cell & 63), lx, ly, lz);
+  const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+  Nb6 n;
+  n.i0 = (uint32_t)apron_cell(D, b, bp, ax - 1, ay, az);
+  n.i1 = (uint32_t)apron_cell(D, b, bp, ax + 1, ay, az);
+  n.i2 = (uint32_t)apron_cell(D, b, bp, ax, ay - 1, az);
+  n.i3 = (uint32_t)apron_cell(D, b, bp, ax, ay + 1, az);
+  n.i4 = (uint32_t)apron_cell(D, b, bp, ax, ay, az - 1);
+  n.i5 = (uint32_t)apron_cell(D, b, bp, ax, ay, az + 1);
+  return n;
+}
+__device__ inline float jacobi_update(const float *__restrict__ src, const Nb6 &n, float ad) {
+  return (src[n.i0] + src[n.i1] + src[n.i2] + src[n.i3] + src[n.i4] + src[n.i5] - ad) / 6.f;
+}
+
+constexpr int LS_CACHE = 4;
+
+// The solve of one level of the cascade (fluid_simulation_dcgrid.cu:281-290)
+// in one cooperative launch: optional prolongation from the parent level, then
+// `sweeps` Jacobi sweeps (ping-pong p -> p~ -> p, as k_dcgrid_jacobi/_inv)
+// separated by grid barriers. The level's topology is fixed during the solve,
+// so each thread resolves the six neighbour cells of its (at most LS_CACHE)
+// cells once and keeps them and alpha*div in registers; a sweep is then six
+// loads and one store per cell. Levels with more cells than the grid covers
+// in LS_CACHE rounds resolve neighbours in every sweep. Arithmetic is that of
+// k_jacobi, so results are identical.
+template <int CACHE>
+__global__ void __launch_bounds__(256) k_level_solve(Dev D, int level, int prolong, int sweeps) {
+  const unsigned nctas = gridDim.x;
+  const long long ncell = D.load[level] * 64;
+  const long long base = D.g.off[level] * 64;
+  const long long stride = (long long)nctas * 256;
+  const long long first = (long long)blockIdx.x * 256 + threadIdx.x;
+  const int rounds = (int)((ncell + stride - 1) / stride);
+  const int s = 1 << level;
+  const float alpha = (float)(s * s) * D.ph.dx * D.ph.dx;
+  if (prolong) {
+    for (long long lc = first; lc < ncell; lc += stride) prolong_cell(D, base + lc);
+    if (sweeps > 0) grid_barrier(D, nctas);
+  }
+  if (sweeps <= 0) return;
+  if (CACHE > 0 && rounds <= CACHE) {
+    Nb6 nb[CACHE > 0 ? CACHE : 1];
+    float ad[CACHE > 0 ? CACHE : 1];
+    bool on[CACHE > 0 ? CACHE : 1];
+#pragma unroll
+    for (int r = 0; r < CACHE; r++) {
+      const long long lc = first + r * stride;
+      on[r] = r < rounds && lc < ncell;
+      if (on[r]) {
+        nb[r] = jacobi_neighbours(D, base + lc);
+        ad[r] = alpha * D.div[base + lc];
+      }
+    }
+    for (int it = 0; it < sweeps; it++) {
+      const float *__restrict__ src = (it & 1) ? D.pt : D.p;
+      float *__restrict__ dst = (it & 1) ? D.p : D.pt;
+#pragma unroll
+      for (int r = 0; r < CACHE; r++)
+        if (on[r]) dst[base + first + r * stride] = jacobi_update(src, nb[r], ad[r]);
+      if (it + 1 < sweeps) grid_barrier(D, nctas);
+    }
+  } else {
+    for (int it = 0; it < sweeps; it++) {
+      const float *__restrict__ src = (it & 1) ? D.pt : D.p;
+      float *__restrict__ dst = (it & 1) ? D.p : D.pt;
+      for (long long lc = first; lc < ncell; lc += stride)
+        dst[base + lc] = jacobi_update(src, jacobi_neighbours(D, base + lc), alpha * D.div[base + lc]);
+      if (it + 1 < sweeps) grid_barrier(D, nctas);
+    }
+  }
+}
+
 // k_dcgrid_apply_pressure (dcgrid_fluid.cu:232-259) on leaf cells.
 __global__ void __launch_bounds__(256) k_apply_pressure(Dev D) {
   const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
@@ -376,6 +482,33 @@ void launch_prolongate(const Dev &D, int level, cudaStream_t st) {
 }
 void launch_apply_pressure(const Dev &D, cudaStream_t st) {
   k_apply_pressure<<<cta_blocks(D.g.B), 256, 0, st>>>(D);
+}
+// Both variants are launched with the grid of the cached one (the smaller
+// per-SM occupancy), so either fits co-resident.
+int level_solve_grid(int sms) {
+  int a = 0, b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_level_solve<LS_CACHE>, 256, 0) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_level_solve<0>, 256, 0) != cudaSuccess) return 0;
+  return (a < b ? a : b) * sms;
+}
+void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int grid, cudaStream_t st) {
+  // cells of the level are known only on the device; the cached variant
+  // falls back to per-sweep neighbour resolution when they exceed its rounds,
+  // and the uncached variant serves budgets that cannot fit at all.
+  const long long max_cells = D.g.budget[level] * 64;
+  const bool cached = max_cells <= (long long)grid * 256 * LS_CACHE * 4;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cached) cudaLaunchKernelEx(&cfg, k_level_solve<LS_CACHE>, D, level, prolong, sweeps);
+  else cudaLaunchKernelEx(&cfg, k_level_solve<0>, D, level, prolong, sweeps);
 }
 
 }  // namespace dcg
