@@ -400,3 +400,152 @@ class RefDCGrid:
             density=self._d2h("density", np.float32, N), vel_x=vel[:, 0].copy(), vel_y=vel[:, 1].copy(),
             vel_z=vel[:, 2].copy(), fluidity=self._d2h("fluidity", np.float32, N),
             divergence=tmp[:N].copy(), pressure=tmp[N:2 * N].copy(), pressure_tmp=tmp[2 * N:3 * N].copy())
+
+    def apply_decisions(self, moves, refines):
+        """adaptTopology (cu:320-346) with the candidate lists given instead of
+        ranked: moves = (block, destination subblock) pairs, refines = subblocks."""
+        self.d.launch("k_dcgrid_calc_vorticity", self.B, 64, self.g)
+        self._memset("blockFlags", 0)
+        touched = 0
+        n = len(moves)
+        if n:
+            self._h2d("blockIdx", np.array([m[0] for m in moves], np.uint64))
+            self._h2d("destIdx", np.array([m[1] for m in moves], np.uint64))
+            self.d.launch("k_dcgrid_move_blocks", self.gridSize, 256, self.g, self.buf["blockIdx"].data_ptr(),
+                          self.buf["destIdx"].data_ptr(), C.c_uint64(n))
+            self.d.sync()
+            self._h2d("touched", np.array([m[0] for m in moves], np.uint64))
+            touched = n
+            self._memset("hashKey", 0xFF)
+            self._memset("hashVal", 0xFF)
+            self.d.launch("k_dcgrid_refill_hash_table", self.gridSize, 256, self.g)
+        r = len(refines)
+        if r:
+            self._h2d("destIdx", np.array(refines, np.uint64))
+            self.d.launch("k_dcgrid_refine_subblocks", idiv_up(r, 256), 256, self.g, self.buf["destIdx"].data_ptr(),
+                          C.c_uint64(r), C.c_uint64(touched), self.buf["touched"].data_ptr())
+            touched += r
+        if touched:
+            self.d.launch("k_dcgrid_refresh_apron_indices", self.B, 216, self.g)
+            for level in range(self.levels - 2, -1, -1):
+                self.d.launch("k_dcgrid_propagate_values", touched, 64, self.g, self.buf["touched"].data_ptr(),
+                              C.c_int(level))
+        self.d.sync()
+
+
+class UniformGridStruct(C.Structure):
+    """struct UniformGrid (src/uniformgrid/uniformgrid.h:31-46)"""
+    _fields_ = [(n, C.c_uint64) for n in ["density", "velocity", "fluidity", "pressure", "temporary",
+                                          "t_velocity", "t_pressure", "divergence", "t_density"]]
+
+
+class RefUniform:
+    """FluidSimulationUniform (fluid_simulation_uniform.cu:6-176) over the
+    reference's uniform-grid kernels."""
+
+    def __init__(self, drv, params):
+        import torch
+        self.d, self.t, self.p = drv, torch, params
+        size = (params.gx, params.gy, params.gz)
+        minDim = min(size)
+        cellSize, lv = 2, 1
+        while all(s % cellSize == 0 for s in size) and cellSize * 4 <= minDim:
+            lv += 1
+            cellSize *= 2
+        self.levels = lv
+        bs = (8, 8, 4)
+        self.blockSize = bs
+        self.gridSize = tuple(idiv_up(size[i], bs[i]) for i in range(3))
+        ms = list(size)
+        self.bsl, self.gsl = [], []
+        for _ in range(lv):
+            b = tuple(min(bs[i], ms[i]) for i in range(3))
+            self.bsl.append(b)
+            self.gsl.append(tuple(idiv_up(ms[i], b[i]) for i in range(3)))
+            ms = [m // 2 for m in ms]
+        self.numCells = size[0] * size[1] * size[2]
+        s, mip = 1, 0
+        while all(x % s == 0 for x in size):
+            mip += self.numCells // (s * s * s)
+            s *= 2
+        self.mip = mip
+        N = self.numCells
+        u8 = lambda n: torch.zeros(max(int(n), 16), dtype=torch.uint8, device="cuda")
+        self.buf = dict(density=u8(4 * N), velocity=u8(12 * N), pressure=u8(4 * mip), fluidity=u8(4 * mip),
+                        temporary=u8(12 * N))
+        self.h = UniformGridStruct()
+        for n in ["density", "velocity", "fluidity", "pressure", "temporary"]:
+            setattr(self.h, n, self.buf[n].data_ptr())
+        raw = bytes(self.h)
+        self.d_grid = u8(len(raw))
+        self.d_grid[: len(raw)].copy_(torch.frombuffer(bytearray(raw), dtype=torch.uint8))
+        sp = sim_params_from(params)
+        ptr, sz = drv.global_ptr("params")
+        drv._chk(drv.cu.cuMemcpyHtoD_v2(C.c_uint64(ptr), C.byref(sp), C.c_size_t(sz)), "params")
+        self.d.launch("k_uniform_init_aliasses", 1, 1, self.g)
+        self.d.sync()
+        self.reset()
+
+    @property
+    def g(self):
+        return self.d_grid.data_ptr()
+
+    def reset(self):
+        for n in ["density", "velocity", "pressure", "fluidity"]:
+            self.buf[n].fill_(0)
+        self.adaptTopology()
+        self.d.launch("k_uniform_init", self.gridSize, self.blockSize, self.g)
+        self.d.sync()
+
+    def adaptTopology(self):
+        for l in range(self.levels):
+            self.d.launch("k_uniform_set_solidity_ratio", self.gsl[l], self.bsl[l], self.g, C.c_int(l))
+        self.d.sync()
+
+    def advectVelocity(self):
+        self.d.launch("k_uniform_advect_velocity", self.gridSize, self.blockSize, self.g)
+        self.buf["velocity"].copy_(self.buf["temporary"])
+        self.d.sync()
+
+    def _jacobi(self, level, pairs):
+        for _ in range(pairs):
+            self.d.launch("k_uniform_jacobi", self.gsl[level], self.bsl[level], self.g, C.c_int(level))
+            self.d.launch("k_uniform_jacobi_inv", self.gsl[level], self.bsl[level], self.g, C.c_int(level))
+
+    def project(self):
+        self.d.launch("k_uniform_calc_divergence", self.gridSize, self.blockSize, self.g)
+        for l in range(1, self.levels):
+            self.d.launch("k_uniform_restrict", self.gsl[l], self.bsl[l], self.g, C.c_int(l))
+        self._jacobi(self.levels - 1, 2)
+        for l in range(self.levels - 2, -1, -1):
+            self.d.launch("k_uniform_prolongate", self.gsl[l], self.bsl[l], self.g, C.c_int(l))
+            self._jacobi(l, 1)
+        self.d.launch("k_uniform_apply_pressure", self.gridSize, self.blockSize, self.g)
+        self.d.sync()
+
+    def projectLocal(self):
+        self.d.launch("k_uniform_calc_divergence", self.gridSize, self.blockSize, self.g)
+        self._jacobi(0, 5)
+        self.d.launch("k_uniform_apply_pressure", self.gridSize, self.blockSize, self.g)
+        self.d.sync()
+
+    def advectDensity(self):
+        self.d.launch("k_uniform_advect_density", self.gridSize, self.blockSize, self.g)
+        self.buf["density"][: 4 * self.numCells].copy_(self.buf["temporary"][: 4 * self.numCells])
+        self.d.sync()
+
+    def step(self, n=1):
+        for _ in range(n):
+            self.advectVelocity()
+            self.adaptTopology()
+            self.project()
+            self.advectDensity()
+
+    def snapshot(self):
+        N, mip = self.numCells, self.mip
+        f = lambda name, n: self.buf[name][: 4 * n].cpu().numpy().view(np.float32).copy()
+        vel = self.buf["velocity"].cpu().numpy().view(np.float32).reshape(N, 3)
+        tmp = self.buf["temporary"].cpu().numpy().view(np.float32)
+        return dict(density=f("density", N), vel_x=vel[:, 0].copy(), vel_y=vel[:, 1].copy(),
+                    vel_z=vel[:, 2].copy(), fluidity=f("fluidity", N), pressure=f("pressure", N),
+                    pressure_tmp=tmp[:N].copy(), divergence=tmp[mip:mip + N].copy())
