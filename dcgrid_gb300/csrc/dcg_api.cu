@@ -9,6 +9,7 @@
 // stream, and dcg_step replays a captured CUDA graph of the whole step.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -57,6 +58,7 @@ struct dcg_sim {
   bool use_graphs = true;
   long long kernels_per_step = 0;
   int ls_grid = 0;  // CTAs of the cooperative level solve (0 = per-sweep launches)
+  int ls_epoch = 2; // sweep ordering: 0 flat grid barrier, 1 neighbour epochs, 2 two-level barrier
 
   int fail(int code, const std::string &msg) {
     err = msg;
@@ -227,8 +229,11 @@ struct dcg_sim {
     if ((rc = alloc(&D.ctr, C_COUNT))) return rc;
     if ((rc = alloc(&D.err, 4))) return rc;
     if ((rc = alloc(&D.red, 32))) return rc;
-    if ((rc = alloc(&D.bar, 2))) return rc;
+    if ((rc = alloc(&D.bar, 64 + 32 * 18))) return rc;
+    if ((rc = alloc(&D.epoch, B))) return rc;
     ls_grid = level_solve_grid(sms);
+    if (const char *m = std::getenv("DCG_SOLVE_SYNC"))
+      ls_epoch = std::strcmp(m, "epoch") == 0 ? 1 : (std::strcmp(m, "barrier") == 0 ? 0 : 2);
     if (P.emission_n > 0) {
       const size_t ne = (size_t)P.emission_n * P.emission_n * P.emission_n;
       if ((rc = alloc(&emis, ne))) return rc;
@@ -269,7 +274,7 @@ struct dcg_sim {
     cudaMemsetAsync(D.nbr, 0xff, (size_t)27 * D.g.B * 4, stream);
     cudaMemsetAsync(D.ctr, 0, sizeof(long long) * C_COUNT, stream);
     cudaMemsetAsync(D.err, 0, 4, stream);
-    cudaMemsetAsync(D.bar, 0, 8, stream);
+    cudaMemsetAsync(D.bar, 0, 4 * (64 + 32 * 18), stream);
     long long load[MAXL] = {0}, ml[MAXL] = {0};
     for (int l = 0; l < D.g.levels; l++) load[l] = D.g.budget[l] == D.g.full[l] ? D.g.budget[l] : 0;
     if ((rc = cuda(cudaMemcpyAsync(D.load, load, sizeof(load), cudaMemcpyHostToDevice, stream), "load"))) return rc;
@@ -321,7 +326,7 @@ struct dcg_sim {
       // one cooperative launch per level: prolongation (not for the coarsest
       // level, nor in projectLocal) and all of the level's sweeps
       const int sweeps = local ? 2 * P.jacobi_iters : P.jacobi_iters;
-      for (int l = top; l >= 0; l--) launch_level_solve(D, l, (!local && l < top) ? 1 : 0, sweeps, ls_grid, stream);
+      for (int l = top; l >= 0; l--) launch_level_solve(D, l, (!local && l < top) ? 1 : 0, sweeps, ls_grid, ls_epoch, stream);
     } else if (local) {
       const int pairs = P.jacobi_iters;
       for (int l = top; l >= 0; l--)
@@ -903,7 +908,7 @@ int dcg_time_kernel(dcg_sim *s, int32_t which, int32_t level, int32_t reps, floa
         break;
       case 1: launch_advect_velocity(s->D, s->stream); break;
       case 2: launch_advect_scalars(s->D, s->stream); break;
-      case 4: launch_level_solve(s->D, level, 0, s->P.jacobi_iters, s->ls_grid, s->stream); break;
+      case 4: launch_level_solve(s->D, level, 0, s->P.jacobi_iters, s->ls_grid, s->ls_epoch, s->stream); break;
       default: launch_divergence(s->D, s->stream); break;
     }
   };

@@ -89,7 +89,52 @@ struct Dev {
   uint32_t *err;           // device error word
   double *red;             // reductions (stats)
   uint32_t *bar;           // grid barrier {arrivals, generation}
+  uint32_t *epoch;         // per block: sweeps completed in the running level solve
 };
+
+// Two-level grid barrier: CTAs arrive on one of 16 group counters (separate
+// 128-byte lines); the last of each group arrives on the top counter, and the
+// last there releases everyone through the generation word. Same bounded wait
+// and timeout rule as grid_barrier. Layout (u32, from bar + 64): [0]
+// generation, [32*(1+g)] group g counter, [32*17] top counter.
+__device__ inline void grid_barrier_tree(const Dev &D, unsigned nctas) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned *tb = D.bar + 64;
+    volatile unsigned *gen = tb;
+    volatile unsigned *err = D.err;
+    if ((*err & 8u) == 0) {
+      const unsigned g = *gen;
+      const unsigned grp = blockIdx.x & 15u;
+      const unsigned members = (nctas >> 4) + ((grp < (nctas & 15u)) ? 1u : 0u);
+      const unsigned groups = nctas < 16u ? nctas : 16u;
+      __threadfence();
+      bool release = false;
+      if (atomicAdd(tb + 32 * (1 + grp), 1u) == members - 1) {
+        atomicExch(tb + 32 * (1 + grp), 0u);
+        if (atomicAdd(tb + 32 * 17, 1u) == groups - 1) {
+          atomicExch(tb + 32 * 17, 0u);
+          release = true;
+        }
+      }
+      if (release) {
+        __threadfence();
+        atomicAdd(tb, 1u);
+      } else {
+        unsigned spins = 0;
+        while (*gen == g) {
+          __nanosleep(32);
+          if (++spins > (1u << 22) || (*err & 8u)) {
+            atomicOr(D.err, 8u);
+            break;
+          }
+        }
+      }
+      __threadfence();
+    }
+  }
+  __syncthreads();
+}
 
 // Grid-wide barrier for cooperative launches (all CTAs co-resident). The wait
 // is bounded: after 2^22 polls the CTA records DCG_DEVERR_TIMEOUT (8) in the

@@ -35,7 +35,7 @@ void launch_prolongate(const Dev &D, int level, cudaStream_t st);
 void launch_apply_pressure(const Dev &D, cudaStream_t st);
 // cooperative persistent solve of one level (prolongation + sweeps)
 int level_solve_grid(int sms);
-void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int grid, cudaStream_t st);
+void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int grid, int epoch_sync, cudaStream_t st);
 
 // k_topology.cu
 void launch_init_blocks(const Dev &D, cudaStream_t st);

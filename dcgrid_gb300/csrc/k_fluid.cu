@@ -365,64 +365,140 @@ __device__ inline Nb6 jacobi_neighbours(const Dev &D, long long cell) {
   n.i5 = (uint32_t)apron_cell(D, b, bp, ax, ay, az + 1);
   return n;
 }
-__device__ inline float jacobi_update(const float *__restrict__ src, const Nb6 &n, float ad) {
-  return (src[n.i0] + src[n.i1] + src[n.i2] + src[n.i3] + src[n.i4] + src[n.i5] - ad) / 6.f;
+// Loads go through L2 (__ldcg): inside one persistent launch the ping-pong
+// buffers are rewritten by other SMs, so no SM may serve them from its L1.
+__device__ inline float jacobi_update(const float *src, const Nb6 &n, float ad) {
+  return (__ldcg(src + n.i0) + __ldcg(src + n.i1) + __ldcg(src + n.i2) + __ldcg(src + n.i3) + __ldcg(src + n.i4) +
+          __ldcg(src + n.i5) - ad) / 6.f;
+}
+
+__device__ inline uint32_t ld_acquire_u32(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ inline void st_release_u32(uint32_t *p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Neighbour epochs: epoch[b] = sweeps block b has completed in the current
+// level solve. Before sweep k (1-based) of a CTA's blocks, their same-level
+// face neighbours must have completed sweep k-1: then the values read are
+// current and nobody still reads the buffer being written. Coarser neighbours
+// are constant during the solve and need no wait. Thread i < 24*rounds polls
+// face i%6 of block i/6 of the CTA; the wait is bounded (2^22 polls) and
+// records DCG_DEVERR_TIMEOUT (8) when exceeded. Writes are ordered before the
+// release store by bar.sync; the acquire load orders later reads the same way.
+__device__ inline long long cta_block(long long off, int j, unsigned nctas) {
+  return off + 4 * ((long long)(j >> 2) * nctas + blockIdx.x) + (j & 3);
+}
+__device__ inline void wait_neighbours(const Dev &D, long long off, long long blk_end, int rounds, unsigned nctas,
+                                       uint32_t need) {
+  const int t = threadIdx.x;
+  if (need > 0 && t < 24 * rounds) {
+    const long long b = cta_block(off, t / 6, nctas);
+    if (b < blk_end) {
+      const int f = t % 6;
+      const int dir = f == 0 ? 4 : f == 1 ? 22 : f == 2 ? 10 : f == 3 ? 16 : f == 4 ? 12 : 14;
+      const uint32_t e = D.nbr[27 * b + dir];
+      if (e != OUT && (e >> 28) == 0 && (e & NBR_MASK) != (uint32_t)b) {
+        const uint32_t *ep = D.epoch + (e & NBR_MASK);
+        unsigned spins = 0;
+        while (ld_acquire_u32(ep) < need) {
+          if (++spins > (1u << 22) || (*(volatile uint32_t *)D.err & 8u)) {
+            atomicOr(D.err, 8u);
+            break;
+          }
+          __nanosleep(20);
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+__device__ inline void publish_blocks(const Dev &D, long long off, long long blk_end, int rounds, unsigned nctas,
+                                      uint32_t done) {
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t < 4 * rounds) {
+    const long long b = cta_block(off, t, nctas);
+    if (b < blk_end) st_release_u32(D.epoch + b, done);
+  }
 }
 
 constexpr int LS_CACHE = 4;
 
 // The solve of one level of the cascade (fluid_simulation_dcgrid.cu:281-290)
 // in one cooperative launch: optional prolongation from the parent level, then
-// `sweeps` Jacobi sweeps (ping-pong p -> p~ -> p, as k_dcgrid_jacobi/_inv)
-// separated by grid barriers. The level's topology is fixed during the solve,
-// so each thread resolves the six neighbour cells of its (at most LS_CACHE)
-// cells once and keeps them and alpha*div in registers; a sweep is then six
-// loads and one store per cell. Levels with more cells than the grid covers
-// in LS_CACHE rounds resolve neighbours in every sweep. Arithmetic is that of
-// k_jacobi, so results are identical.
+// `sweeps` Jacobi sweeps (ping-pong p -> p~ -> p, as k_dcgrid_jacobi/_inv).
+// Work split: CTA c owns the level's blocks 4*(r*grid + c) .. +3 in round r.
+// One grid barrier follows prolongation and the epoch reset; sweeps are then
+// ordered block by block through neighbour epochs instead of grid barriers.
+// The level's topology is fixed during the solve, so each thread resolves the
+// six neighbour cells of its (at most LS_CACHE) cells once and keeps them and
+// alpha*div in registers; a sweep is then six loads and one store per cell.
+// Levels with more cells than the grid covers in LS_CACHE rounds resolve
+// neighbours in every sweep. Arithmetic is that of k_jacobi (identical results).
 template <int CACHE>
-__global__ void __launch_bounds__(256) k_level_solve(Dev D, int level, int prolong, int sweeps) {
+__global__ void __launch_bounds__(256) k_level_solve(Dev D, int level, int prolong, int sweeps, int epoch_sync) {
   const unsigned nctas = gridDim.x;
-  const long long ncell = D.load[level] * 64;
-  const long long base = D.g.off[level] * 64;
+  const long long nblk = D.load[level];
+  const long long ncell = nblk * 64;
+  const long long off = D.g.off[level];
+  const long long base = off * 64;
   const long long stride = (long long)nctas * 256;
   const long long first = (long long)blockIdx.x * 256 + threadIdx.x;
   const int rounds = (int)((ncell + stride - 1) / stride);
   const int s = 1 << level;
   const float alpha = (float)(s * s) * D.ph.dx * D.ph.dx;
-  if (prolong) {
+  for (long long b = first; b < nblk; b += stride) D.epoch[off + b] = 0u;
+  if (prolong)
     for (long long lc = first; lc < ncell; lc += stride) prolong_cell(D, base + lc);
-    if (sweeps > 0) grid_barrier(D, nctas);
-  }
   if (sweeps <= 0) return;
+  // epoch_sync: 0 = flat grid barrier, 1 = neighbour epochs, 2 = two-level barrier
+  auto barrier = [&]() {
+    if (epoch_sync == 2) grid_barrier_tree(D, nctas);
+    else grid_barrier(D, nctas);
+  };
+  barrier();
+  const long long blk_end = off + nblk;
   if (CACHE > 0 && rounds <= CACHE) {
-    Nb6 nb[CACHE > 0 ? CACHE : 1];
-    float ad[CACHE > 0 ? CACHE : 1];
-    bool on[CACHE > 0 ? CACHE : 1];
-#pragma unroll
-    for (int r = 0; r < CACHE; r++) {
+    // neighbour indices and alpha*div of the thread's cells, [round][k][thread]
+    __shared__ uint32_t s_nb[CACHE > 0 ? CACHE : 1][6][256];
+    __shared__ float s_ad[CACHE > 0 ? CACHE : 1][256];
+    const int t = threadIdx.x;
+    for (int r = 0; r < rounds; r++) {
       const long long lc = first + r * stride;
-      on[r] = r < rounds && lc < ncell;
-      if (on[r]) {
-        nb[r] = jacobi_neighbours(D, base + lc);
-        ad[r] = alpha * D.div[base + lc];
+      if (lc < ncell) {
+        const Nb6 n = jacobi_neighbours(D, base + lc);
+        s_nb[r][0][t] = n.i0; s_nb[r][1][t] = n.i1; s_nb[r][2][t] = n.i2;
+        s_nb[r][3][t] = n.i3; s_nb[r][4][t] = n.i4; s_nb[r][5][t] = n.i5;
+        s_ad[r][t] = alpha * D.div[base + lc];
       }
     }
     for (int it = 0; it < sweeps; it++) {
-      const float *__restrict__ src = (it & 1) ? D.pt : D.p;
-      float *__restrict__ dst = (it & 1) ? D.p : D.pt;
-#pragma unroll
-      for (int r = 0; r < CACHE; r++)
-        if (on[r]) dst[base + first + r * stride] = jacobi_update(src, nb[r], ad[r]);
-      if (it + 1 < sweeps) grid_barrier(D, nctas);
+      const float *src = (it & 1) ? D.pt : D.p;
+      float *dst = (it & 1) ? D.p : D.pt;
+      if (epoch_sync == 1) wait_neighbours(D, off, blk_end, rounds, nctas, (uint32_t)it);
+      for (int r = 0; r < rounds; r++) {
+        const long long lc = first + r * stride;
+        if (lc < ncell) {
+          const Nb6 n = {s_nb[r][0][t], s_nb[r][1][t], s_nb[r][2][t], s_nb[r][3][t], s_nb[r][4][t], s_nb[r][5][t]};
+          dst[base + lc] = jacobi_update(src, n, s_ad[r][t]);
+        }
+      }
+      if (epoch_sync == 1) publish_blocks(D, off, blk_end, rounds, nctas, (uint32_t)it + 1);
+      else if (it + 1 < sweeps) barrier();
     }
   } else {
+    // too many rounds for the caches: neighbours resolved every sweep, and a
+    // grid barrier between sweeps (epochs would need 24 pollers per block)
     for (int it = 0; it < sweeps; it++) {
-      const float *__restrict__ src = (it & 1) ? D.pt : D.p;
-      float *__restrict__ dst = (it & 1) ? D.p : D.pt;
+      const float *src = (it & 1) ? D.pt : D.p;
+      float *dst = (it & 1) ? D.p : D.pt;
       for (long long lc = first; lc < ncell; lc += stride)
         dst[base + lc] = jacobi_update(src, jacobi_neighbours(D, base + lc), alpha * D.div[base + lc]);
-      if (it + 1 < sweeps) grid_barrier(D, nctas);
+      if (it + 1 < sweeps) barrier();
     }
   }
 }
@@ -491,7 +567,7 @@ int level_solve_grid(int sms) {
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_level_solve<0>, 256, 0) != cudaSuccess) return 0;
   return (a < b ? a : b) * sms;
 }
-void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int grid, cudaStream_t st) {
+void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int grid, int epoch_sync, cudaStream_t st) {
   // cells of the level are known only on the device; the cached variant
   // falls back to per-sweep neighbour resolution when they exceed its rounds,
   // and the uncached variant serves budgets that cannot fit at all.
@@ -507,8 +583,8 @@ void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int gr
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (cached) cudaLaunchKernelEx(&cfg, k_level_solve<LS_CACHE>, D, level, prolong, sweeps);
-  else cudaLaunchKernelEx(&cfg, k_level_solve<0>, D, level, prolong, sweeps);
+  if (cached) cudaLaunchKernelEx(&cfg, k_level_solve<LS_CACHE>, D, level, prolong, sweeps, epoch_sync);
+  else cudaLaunchKernelEx(&cfg, k_level_solve<0>, D, level, prolong, sweeps, epoch_sync == 2 ? 2 : 0);
 }
 
 }  // namespace dcg
