@@ -33,7 +33,8 @@ REFINE_GEOMETRIC = 0
 REFINE_FIELDS = 1
 
 PRECISION_FP32 = 0
-PRECISION_MIXED = 1
+PRECISION_MIXED = 1       # BF16 scalars
+PRECISION_MIXED_FP16 = 2  # FP16 scalars
 
 FIELD_DENSITY = 0
 FIELD_VEL_X = 1

@@ -47,6 +47,8 @@ struct dcg_sim {
   float *emis = nullptr;  // emission_n^3 field
   long long *apron_tmp = nullptr;
   float *vbuf[2][3] = {}, *qbuf[2][3] = {};
+  uint16_t *qhbuf[2][3] = {};  // 16-bit scalar storage (mixed precision)
+  float *conv_tmp = nullptr;   // FP32 staging for access to 16-bit fields
   int vpar = 0, qpar = 0;
 
   // uniform
@@ -102,6 +104,8 @@ struct dcg_sim {
     for (int k = 0; k < 3; k++) {
       D.q[k] = qbuf[qpar][k];
       D.tq[k] = qbuf[qpar ^ 1][k];
+      D.qh[k] = qhbuf[qpar][k];
+      D.tqh[k] = qhbuf[qpar ^ 1][k];
       U.q[k] = uqbuf[qpar][k];
       U.tq[k] = uqbuf[qpar ^ 1][k];
     }
@@ -151,7 +155,8 @@ struct dcg_sim {
     if (P.jacobi_iters < 0 || (P.jacobi_iters & 1))
       return fail(DCG_E_INVALID, "jacobi_iters must be even and >= 0");
     if (P.n_scalars != 1 && P.n_scalars != 3) return fail(DCG_E_INVALID, "n_scalars must be 1 or 3");
-    if (P.precision != DCG_PRECISION_FP32 && P.precision != DCG_PRECISION_MIXED)
+    if (P.precision != DCG_PRECISION_FP32 && P.precision != DCG_PRECISION_MIXED &&
+        P.precision != DCG_PRECISION_MIXED_FP16)
       return fail(DCG_E_INVALID, "unknown precision");
     return DCG_OK;
   }
@@ -200,7 +205,7 @@ struct dcg_sim {
     g.B = B;
     g.nq = P.n_scalars;
     g.ref_compat = P.ref_compat;
-    g.mixed = P.precision == DCG_PRECISION_MIXED;
+    g.mixed = P.precision == DCG_PRECISION_MIXED ? 1 : (P.precision == DCG_PRECISION_MIXED_FP16 ? 2 : 0);
     fill_phys(D.ph);
 
     const size_t nc = (size_t)B * BV;
@@ -214,8 +219,13 @@ struct dcg_sim {
     for (int par = 0; par < 2; par++) {
       for (int d = 0; d < 3; d++)
         if ((rc = alloc(&vbuf[par][d], nc))) return rc;
-      for (int k = 0; k < P.n_scalars; k++)
-        if ((rc = alloc(&qbuf[par][k], nc))) return rc;
+      for (int k = 0; k < P.n_scalars; k++) {
+        if (g.mixed) {
+          if ((rc = alloc(&qhbuf[par][k], nc))) return rc;
+        } else if ((rc = alloc(&qbuf[par][k], nc))) {
+          return rc;
+        }
+      }
     }
     if ((rc = alloc(&D.w, nc))) return rc;
     if ((rc = alloc(&D.p, nc))) return rc;
@@ -265,7 +275,10 @@ struct dcg_sim {
     const size_t nc = (size_t)D.g.B * BV;
     for (int par = 0; par < 2; par++) {
       for (int d = 0; d < 3; d++) cudaMemsetAsync(vbuf[par][d], 0, nc * 4, stream);
-      for (int k = 0; k < P.n_scalars; k++) cudaMemsetAsync(qbuf[par][k], 0, nc * 4, stream);
+      for (int k = 0; k < P.n_scalars; k++) {
+        if (qbuf[par][k]) cudaMemsetAsync(qbuf[par][k], 0, nc * 4, stream);
+        if (qhbuf[par][k]) cudaMemsetAsync(qhbuf[par][k], 0, nc * 2, stream);
+      }
     }
     cudaMemsetAsync(D.w, 0, nc * 4, stream);
     cudaMemsetAsync(D.p, 0, nc * 4, stream);
@@ -300,7 +313,10 @@ struct dcg_sim {
   void restrict_q() {
     FieldList fl{};
     fl.n = P.n_scalars;
-    for (int k = 0; k < P.n_scalars; k++) fl.f[k] = D.q[k];
+    for (int k = 0; k < P.n_scalars; k++) {
+      fl.f[k] = D.g.mixed ? static_cast<void *>(D.qh[k]) : static_cast<void *>(D.q[k]);
+      fl.mode[k] = D.g.mixed;
+    }
     launch_restrict(D, fl, stream);
   }
   void restrict_div() {
@@ -563,9 +579,9 @@ int dcg_create(const dcg_params *params, int32_t mode, dcg_sim **out) {
     return DCG_E_CUDA;
   }
   s->own_stream = true;
-  if (params->precision == DCG_PRECISION_MIXED) {
+  if (params->precision != DCG_PRECISION_FP32 && mode == DCG_MODE_UNIFORM) {
     delete s;
-    return DCG_E_INVALID;  // mixed storage is provided by the batched path only
+    return DCG_E_INVALID;  // 16-bit scalar storage is implemented for the adaptive grid
   }
   const int rc = mode == DCG_MODE_ADAPTIVE ? s->create_adaptive() : s->create_uniform();
   if (rc) {
@@ -717,21 +733,32 @@ int dcg_add_velocity_noise(dcg_sim *s, uint64_t seed, float amplitude) {
   return s->check_launch("noise");
 }
 
-static float *field_ptr(dcg_sim *s, int f) {
+// A field's storage: pointer and format (0 FP32, 1 BF16, 2 FP16).
+struct FieldRef {
+  void *p;
+  int mode;
+};
+static FieldRef field_ref(dcg_sim *s, int f) {
   const bool a = s->mode == DCG_MODE_ADAPTIVE;
+  const int m = a ? s->D.g.mixed : 0;
+  auto scalar = [&](int k) -> FieldRef {
+    if (k >= s->P.n_scalars) return {nullptr, 0};
+    if (!a) return {s->U.q[k], 0};
+    return m ? FieldRef{s->D.qh[k], m} : FieldRef{s->D.q[k], 0};
+  };
   switch (f) {
-    case DCG_FIELD_DENSITY: return a ? s->D.q[0] : s->U.q[0];
-    case DCG_FIELD_VEL_X: return a ? s->D.v[0] : s->U.v[0];
-    case DCG_FIELD_VEL_Y: return a ? s->D.v[1] : s->U.v[1];
-    case DCG_FIELD_VEL_Z: return a ? s->D.v[2] : s->U.v[2];
-    case DCG_FIELD_FLUIDITY: return a ? s->D.w : s->U.w;
-    case DCG_FIELD_PRESSURE: return a ? s->D.p : s->U.p;
-    case DCG_FIELD_PRESSURE_TMP: return a ? s->D.pt : s->U.pt;
-    case DCG_FIELD_DIVERGENCE: return a ? s->D.div : s->U.div;
-    case DCG_FIELD_TEMPERATURE: return s->P.n_scalars > 1 ? (a ? s->D.q[1] : s->U.q[1]) : nullptr;
-    case DCG_FIELD_VAPOR: return s->P.n_scalars > 2 ? (a ? s->D.q[2] : s->U.q[2]) : nullptr;
+    case DCG_FIELD_DENSITY: return scalar(0);
+    case DCG_FIELD_VEL_X: return {a ? s->D.v[0] : s->U.v[0], 0};
+    case DCG_FIELD_VEL_Y: return {a ? s->D.v[1] : s->U.v[1], 0};
+    case DCG_FIELD_VEL_Z: return {a ? s->D.v[2] : s->U.v[2], 0};
+    case DCG_FIELD_FLUIDITY: return {a ? s->D.w : s->U.w, 0};
+    case DCG_FIELD_PRESSURE: return {a ? s->D.p : s->U.p, 0};
+    case DCG_FIELD_PRESSURE_TMP: return {a ? s->D.pt : s->U.pt, 0};
+    case DCG_FIELD_DIVERGENCE: return {a ? s->D.div : s->U.div, 0};
+    case DCG_FIELD_TEMPERATURE: return scalar(1);
+    case DCG_FIELD_VAPOR: return scalar(2);
   }
-  return nullptr;
+  return {nullptr, 0};
 }
 static size_t field_cells(dcg_sim *s) {
   return s->mode == DCG_MODE_ADAPTIVE ? (size_t)s->D.g.B * BV : (size_t)s->U.nc;
@@ -739,33 +766,47 @@ static size_t field_cells(dcg_sim *s) {
 
 int dcg_get_field(dcg_sim *s, int32_t field, float *dst, int32_t where) {
   if (bad(s) || !dst) return DCG_E_INVALID;
-  float *src = field_ptr(s, field);
-  if (!src) return s->fail(DCG_E_NOT_FOUND, "no such field");
-  const size_t n = field_cells(s) * sizeof(float);
-  int rc = s->cuda(cudaMemcpyAsync(dst, src, n, where == DCG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                   s->stream), "get_field");
+  const FieldRef r = field_ref(s, field);
+  if (!r.p) return s->fail(DCG_E_NOT_FOUND, "no such field");
+  const size_t cells = field_cells(s), n = cells * sizeof(float);
+  int rc;
+  const float *src = static_cast<const float *>(r.p);
+  if (r.mode) {  // 16-bit storage: widen into an FP32 staging buffer
+    if (!s->conv_tmp && (rc = s->alloc(&s->conv_tmp, cells))) return rc;
+    launch_h16_to_f32(static_cast<const uint16_t *>(r.p), s->conv_tmp, (long long)cells, r.mode, s->stream);
+    src = s->conv_tmp;
+  }
+  rc = s->cuda(cudaMemcpyAsync(dst, src, n, where == DCG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                               s->stream), "get_field");
   if (rc) return rc;
   return s->sync("get_field");
 }
 int dcg_set_field(dcg_sim *s, int32_t field, const float *src, int32_t where) {
   if (bad(s) || !src) return DCG_E_INVALID;
-  float *dst = field_ptr(s, field);
-  if (!dst) return s->fail(DCG_E_NOT_FOUND, "no such field");
-  const size_t n = field_cells(s) * sizeof(float);
-  int rc = s->cuda(cudaMemcpyAsync(dst, src, n, where == DCG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                                   s->stream), "set_field");
+  const FieldRef r = field_ref(s, field);
+  if (!r.p) return s->fail(DCG_E_NOT_FOUND, "no such field");
+  const size_t cells = field_cells(s), n = cells * sizeof(float);
+  int rc;
+  float *dst = static_cast<float *>(r.p);
+  if (r.mode) {
+    if (!s->conv_tmp && (rc = s->alloc(&s->conv_tmp, cells))) return rc;
+    dst = s->conv_tmp;
+  }
+  rc = s->cuda(cudaMemcpyAsync(dst, src, n, where == DCG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               s->stream), "set_field");
   if (rc) return rc;
+  if (r.mode) launch_f32_to_h16(s->conv_tmp, static_cast<uint16_t *>(r.p), (long long)cells, r.mode, s->stream);
   return s->sync("set_field");
 }
 int dcg_get_dense(dcg_sim *s, int32_t field, float *dst, int32_t where) {
   if (bad(s) || !dst) return DCG_E_INVALID;
   if (s->mode == DCG_MODE_UNIFORM) return dcg_get_field(s, field, dst, where);
-  float *src = field_ptr(s, field);
-  if (!src) return s->fail(DCG_E_NOT_FOUND, "no such field");
+  const FieldRef r = field_ref(s, field);
+  if (!r.p) return s->fail(DCG_E_NOT_FOUND, "no such field");
   const size_t n = (size_t)s->P.gx * s->P.gy * s->P.gz;
   int rc;
   if (!s->dense_tmp && (rc = s->alloc(&s->dense_tmp, n))) return rc;
-  launch_fields_to_dense(s->D, src, s->dense_tmp, s->stream);
+  launch_fields_to_dense(s->D, r.p, r.mode, s->dense_tmp, s->stream);
   rc = s->cuda(cudaMemcpyAsync(dst, s->dense_tmp, n * 4,
                                where == DCG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s->stream),
                "get_dense");
@@ -1001,8 +1042,8 @@ int dense_scratch_for_device(int device, float **out, std::string &err) {
 extern "C" int dcg_get_dense_noalloc(dcg_sim *s, int32_t field, float *dst, int32_t where) {
   if (bad(s) || !dst) return DCG_E_INVALID;
   if (s->mode == DCG_MODE_UNIFORM) return dcg_get_field(s, field, dst, where);  // no staging needed
-  float *src = field_ptr(s, field);
-  if (!src) return s->fail(DCG_E_NOT_FOUND, "no such field");
+  const FieldRef src = field_ref(s, field);
+  if (!src.p) return s->fail(DCG_E_NOT_FOUND, "no such field");
   const size_t n = (size_t)s->P.gx * s->P.gy * s->P.gz;
   if (n > kDenseScratchCells) {
     char buf[160];
@@ -1015,7 +1056,7 @@ extern "C" int dcg_get_dense_noalloc(dcg_sim *s, int32_t field, float *dst, int3
   int rc = dense_scratch_for_device(s->device, &scratch, s->err);
   if (rc) return rc;
   // The kernel writes every one of the n staged cells, so nothing needs zeroing.
-  launch_fields_to_dense(s->D, src, scratch, s->stream);
+  launch_fields_to_dense(s->D, src.p, src.mode, scratch, s->stream);
   rc = s->cuda(cudaMemcpyAsync(dst, scratch, n * 4,
                                where == DCG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s->stream),
                "get_dense_noalloc");

@@ -17,6 +17,8 @@
 // the coarse cell that contains the apron cell (dcgrid_structure.cu:85-91).
 #pragma once
 #include <cstdint>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace dcg {
@@ -80,6 +82,7 @@ struct Dev {
   uint8_t *flags;
   long long *load, *move_limit;
   float *q[3], *tq[3], *v[3], *tv[3];
+  uint16_t *qh[3], *tqh[3];  // scalar storage when g.mixed != 0 (1 = BF16, 2 = FP16)
   float *w, *p, *pt, *div;
   float *ss, *bs;          // subblock / block scores (8B+1, B)
   uint32_t *moves;         // (block, dest) pairs
@@ -396,5 +399,26 @@ __device__ inline float emission_at(const Geom &g, const Phys &P, int x, int y, 
 }
 
 __device__ inline void set_err(const Dev &D, uint32_t bits) { atomicOr(D.err, bits); }
+
+// ---------------------------------------------------------------- scalar storage
+// Scalars are stored as FP32, BF16 (mode 1) or FP16 (mode 2); compute is FP32.
+// Conversions to 16 bits round to nearest even.
+__device__ inline float h16_to_f(uint16_t h, int mode) {
+  return mode == 1 ? __bfloat162float(__ushort_as_bfloat16(h)) : __half2float(__ushort_as_half(h));
+}
+__device__ inline uint16_t f_to_h16(float v, int mode) {
+  return mode == 1 ? __bfloat16_as_ushort(__float2bfloat16_rn(v)) : __half_as_ushort(__float2half_rn(v));
+}
+__device__ inline float q_ld(const Dev &D, int k, size_t i) {
+  return D.g.mixed ? h16_to_f(D.qh[k][i], D.g.mixed) : D.q[k][i];
+}
+__device__ inline void q_st(const Dev &D, int k, size_t i, float v) {
+  if (D.g.mixed) D.qh[k][i] = f_to_h16(v, D.g.mixed);
+  else D.q[k][i] = v;
+}
+__device__ inline void tq_st(const Dev &D, int k, size_t i, float v) {
+  if (D.g.mixed) D.tqh[k][i] = f_to_h16(v, D.g.mixed);
+  else D.tq[k][i] = v;
+}
 
 }  // namespace dcg

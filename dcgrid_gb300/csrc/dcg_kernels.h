@@ -7,7 +7,8 @@
 namespace dcg {
 
 struct FieldList {
-  float *f[6];
+  void *f[6];
+  int mode[6];  // 0 = FP32, 1 = BF16, 2 = FP16 storage
   int n;
 };
 
@@ -44,7 +45,9 @@ void launch_build_nbr(const Dev &D, bool only_if_touched, cudaStream_t st);
 void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *vals,
                   uint32_t *keys2, uint32_t *vals2, int sms, cudaStream_t st);
 void launch_stats(const Dev &D, cudaStream_t st);
-void launch_fields_to_dense(const Dev &D, const float *src, float *dst, cudaStream_t st);
+void launch_fields_to_dense(const Dev &D, const void *src, int mode, float *dst, cudaStream_t st);
+void launch_h16_to_f32(const uint16_t *src, float *dst, long long n, int mode, cudaStream_t st);
+void launch_f32_to_h16(const float *src, uint16_t *dst, long long n, int mode, cudaStream_t st);
 void launch_apron_table(const Dev &D, long long *dst, cudaStream_t st);
 
 // k_uniform.cu — uniform (dense, mip-mapped) grid

@@ -123,8 +123,8 @@ __global__ void __launch_bounds__(256) k_advect_velocity(Dev D) {
       }
     }
     if (D.ph.buoy_a != 0.f || D.ph.buoy_b != 0.f) {
-      float f = -D.ph.buoy_a * D.q[0][cell];
-      if (D.g.nq > 1) f = f + D.ph.buoy_b * (D.q[1][cell] - D.ph.t_amb);
+      float f = -D.ph.buoy_a * q_ld(D, 0, cell);
+      if (D.g.nq > 1) f = f + D.ph.buoy_b * (q_ld(D, 1, cell) - D.ph.t_amb);
       o1 = o1 + D.ph.dt * f;
     }
   }
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(256) k_advect_scalars(Dev D) {
         for (int k = 0; k < 8; k++) {
           int x, y, z;
           corner_of(s, k, x, y, z);
-          const float qc = q_bc(D.g, D.ph, D.q[kq][s.idx[k]], kq, x, y, z, s.scale);
+          const float qc = q_bc(D.g, D.ph, q_ld(D, kq, s.idx[k]), kq, x, y, z, s.scale);
           acc = (k == 0) ? qc * s.wt[0] : acc + qc * s.wt[k];
         }
         o[kq] = acc;
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(256) k_advect_scalars(Dev D) {
         for (int kq = 0; kq < nq; kq++) o[kq] = D.ph.src_val[kq];
     }
   }
-  for (int kq = 0; kq < nq; kq++) D.tq[kq][cell] = o[kq];
+  for (int kq = 0; kq < nq; kq++) tq_st(D, kq, cell, o[kq]);
 }
 
 // Source cells set on every leaf cell (used once at initialisation).
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(256) k_sources(Dev D) {
   int lx, ly, lz;
   local_xyz(c, lx, ly, lz);
   if (in_source(D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w))
-    for (int kq = 0; kq < D.g.nq; kq++) D.q[kq][cell] = D.ph.src_val[kq];
+    for (int kq = 0; kq < D.g.nq; kq++) q_st(D, kq, cell, D.ph.src_val[kq]);
 }
 
 // Seeded velocity noise on every allocated cell.
@@ -216,12 +216,28 @@ __global__ void __launch_bounds__(256) k_restrict(Dev D, int level, FieldList fl
   const size_t pc = (size_t)par * 8 + s;
   const size_t base = (size_t)b * BV + 8 * s;
   for (int f = 0; f < fl.n; f++) {
-    const float4 a = *reinterpret_cast<const float4 *>(fl.f[f] + base);
-    const float4 c = *reinterpret_cast<const float4 *>(fl.f[f] + base + 4);
+    float v[8];
+    if (fl.mode[f] == 0) {
+      const float *F = static_cast<const float *>(fl.f[f]);
+      const float4 a = *reinterpret_cast<const float4 *>(F + base);
+      const float4 c = *reinterpret_cast<const float4 *>(F + base + 4);
+      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = c.x; v[5] = c.y; v[6] = c.z; v[7] = c.w;
+    } else {
+      const uint16_t *H = static_cast<const uint16_t *>(fl.f[f]);
+      const uint4 u = *reinterpret_cast<const uint4 *>(H + base);  // 8 x 16 bit
+      const uint32_t w4[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        v[2 * i] = h16_to_f((uint16_t)(w4[i] & 0xFFFFu), fl.mode[f]);
+        v[2 * i + 1] = h16_to_f((uint16_t)(w4[i] >> 16), fl.mode[f]);
+      }
+    }
     float acc = 0.f;
-    acc = acc + a.x; acc = acc + a.y; acc = acc + a.z; acc = acc + a.w;
-    acc = acc + c.x; acc = acc + c.y; acc = acc + c.z; acc = acc + c.w;
-    fl.f[f][pc] = acc * 0.125f;
+#pragma unroll
+    for (int i = 0; i < 8; i++) acc = acc + v[i];
+    const float mean = acc * 0.125f;
+    if (fl.mode[f] == 0) static_cast<float *>(fl.f[f])[pc] = mean;
+    else static_cast<uint16_t *>(fl.f[f])[pc] = f_to_h16(mean, fl.mode[f]);
   }
 }
 

@@ -142,13 +142,13 @@ __global__ void __launch_bounds__(256) k_scores_fields(Dev D) {
     const unsigned long long F = apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1);
     const float *W = D.w;
     const float wl = W[L], wr = W[R], wd = W[Dn], wu = W[U], wb = W[Bk], wf = W[F];
-    const float *V0 = D.v[0], *V1 = D.v[1], *V2 = D.v[2], *Q = D.q[0];
+    const float *V0 = D.v[0], *V1 = D.v[1], *V2 = D.v[2];
     const float ox = alpha * ((wu * V2[U] - wd * V2[Dn]) - (wf * V1[F] - wb * V1[Bk]));
     const float oy = alpha * ((wf * V0[F] - wb * V0[Bk]) - (wr * V2[R] - wl * V2[L]));
     const float oz = alpha * ((wr * V1[R] - wl * V1[L]) - (wu * V0[U] - wd * V0[Dn]));
-    const float gxr = alpha * (Q[R] - Q[L]);
-    const float gyr = alpha * (Q[U] - Q[Dn]);
-    const float gzr = alpha * (Q[F] - Q[Bk]);
+    const float gxr = alpha * (q_ld(D, 0, R) - q_ld(D, 0, L));
+    const float gyr = alpha * (q_ld(D, 0, U) - q_ld(D, 0, Dn));
+    const float gzr = alpha * (q_ld(D, 0, F) - q_ld(D, 0, Bk));
     const float om = sqrtf(ox * ox + oy * oy + oz * oz);
     const float gr = sqrtf(gxr * gxr + gyr * gyr + gzr * gzr);
     const float a = om / D.ph.vort_t, bb = gr / D.ph.grad_t;
@@ -483,11 +483,16 @@ __global__ void __launch_bounds__(256) k_propagate(Dev D, int level) {
       return (27.f / 64.f) * f[i000] + (9.f / 64.f) * (f[i001] + f[i010] + f[i100]) +
              (3.f / 64.f) * (f[i011] + f[i101] + f[i110]) + (1.f / 64.f) * f[i111];
     };
+    auto triq = [&](int k) {
+      return (27.f / 64.f) * q_ld(D, k, i000) +
+             (9.f / 64.f) * (q_ld(D, k, i001) + q_ld(D, k, i010) + q_ld(D, k, i100)) +
+             (3.f / 64.f) * (q_ld(D, k, i011) + q_ld(D, k, i101) + q_ld(D, k, i110)) +
+             (1.f / 64.f) * q_ld(D, k, i111);
+    };
     float qv[3], vv[3];
-    for (int kq = 0; kq < D.g.nq; kq++) qv[kq] = tri(D.q[kq]);
+    for (int kq = 0; kq < D.g.nq; kq++) qv[kq] = triq(kq);
     for (int d = 0; d < 3; d++) vv[d] = tri(D.v[d]);
-    __syncwarp();
-    for (int kq = 0; kq < D.g.nq; kq++) D.q[kq][cell] = qv[kq];
+    for (int kq = 0; kq < D.g.nq; kq++) q_st(D, kq, cell, qv[kq]);
     for (int d = 0; d < 3; d++) D.v[d][cell] = vv[d];
     D.w[cell] = fluidity(D.g, D.ph, x, y, z, 1 << level);
   }
@@ -592,7 +597,7 @@ __global__ void __launch_bounds__(256) k_stats(Dev D) {
                          P[apron_cell(D, (uint32_t)b, bp, ax, ay, az - 1)] +
                          P[apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1)] - 6.0 * P[cell];
       res = (double)scale * fabs((double)D.div[cell] - lap * alpha);
-      mass = (double)D.q[0][cell] * (double)D.w[cell] * scale * scale * scale;
+      mass = (double)q_ld(D, 0, cell) * (double)D.w[cell] * scale * scale * scale;
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -614,7 +619,8 @@ void launch_stats(const Dev &D, cudaStream_t st) {
 }
 
 // Dense resampling: every finest cell takes the leaf value that covers it.
-__global__ void __launch_bounds__(256) k_to_dense(Dev D, const float *src, float *dst) {
+// `mode` is the storage format of src (0 FP32, 1 BF16, 2 FP16).
+__global__ void __launch_bounds__(256) k_to_dense(Dev D, const void *src, int mode, float *dst) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long n = (long long)D.g.gx * D.g.gy * D.g.gz;
   if (i >= n) return;
@@ -622,11 +628,28 @@ __global__ void __launch_bounds__(256) k_to_dense(Dev D, const float *src, float
   int lev;
   const uint32_t b = locate(D, x, y, z, 0, lev);
   const int4 bp = D.pos[b];
-  dst[i] = src[(size_t)b * BV + local_of((x >> lev) - bp.x, (y >> lev) - bp.y, (z >> lev) - bp.z)];
+  const size_t c = (size_t)b * BV + local_of((x >> lev) - bp.x, (y >> lev) - bp.y, (z >> lev) - bp.z);
+  dst[i] = mode ? h16_to_f(static_cast<const uint16_t *>(src)[c], mode) : static_cast<const float *>(src)[c];
 }
-void launch_fields_to_dense(const Dev &D, const float *src, float *dst, cudaStream_t st) {
+void launch_fields_to_dense(const Dev &D, const void *src, int mode, float *dst, cudaStream_t st) {
   const long long n = (long long)D.g.gx * D.g.gy * D.g.gz;
-  k_to_dense<<<grid_for(n), 256, 0, st>>>(D, src, dst);
+  k_to_dense<<<grid_for(n), 256, 0, st>>>(D, src, mode, dst);
+}
+
+// Conversions between FP32 and 16-bit scalar storage (field access).
+__global__ void __launch_bounds__(256) k_h16_to_f32(const uint16_t *src, float *dst, long long n, int mode) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = h16_to_f(src[i], mode);
+}
+__global__ void __launch_bounds__(256) k_f32_to_h16(const float *src, uint16_t *dst, long long n, int mode) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = f_to_h16(src[i], mode);
+}
+void launch_h16_to_f32(const uint16_t *src, float *dst, long long n, int mode, cudaStream_t st) {
+  k_h16_to_f32<<<grid_for(n), 256, 0, st>>>(src, dst, n, mode);
+}
+void launch_f32_to_h16(const float *src, uint16_t *dst, long long n, int mode, cudaStream_t st) {
+  k_f32_to_h16<<<grid_for(n), 256, 0, st>>>(src, dst, n, mode);
 }
 
 // The reference-format 216-entry apron table, derived from neighbour tables.

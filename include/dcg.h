@@ -54,8 +54,15 @@ enum {
   DCG_REFINE_FIELDS = 1     /* extension: |curl v| and |grad rho| thresholds */
 };
 
-/* ---- storage precision of the advected scalars ------------------------ */
-enum { DCG_PRECISION_FP32 = 0, DCG_PRECISION_MIXED = 1 };
+/* ---- storage precision of the advected scalars ------------------------
+ * Scalars (density, temperature, vapor) are stored in the given format and
+ * computed in FP32; velocity, pressure and fluidity stay FP32. Conversions
+ * round to nearest even. */
+enum {
+  DCG_PRECISION_FP32 = 0,
+  DCG_PRECISION_MIXED = 1,      /* BF16 scalars */
+  DCG_PRECISION_MIXED_FP16 = 2  /* FP16 scalars */
+};
 
 /*
  * Simulation parameters. Units follow the reference's SimParams

@@ -66,6 +66,24 @@ template <typename R> inline R clampr(R v, R a, R b) {
   return v < a ? a : (v > b ? b : v);
 }
 
+// 16-bit storage of the advected scalars (DCG_PRECISION_MIXED*): the value is
+// rounded to nearest even in BF16 (1) or FP16 (2) and widened back.
+inline float round_bf16(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7F800000u) == 0x7F800000u) return f;  // inf / nan unchanged
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  u &= 0xFFFF0000u;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+inline float round_fp16(float f) { return (float)(_Float16)f; }
+template <typename R> inline R store_q(R v, int precision) {
+  if (precision == DCG_PRECISION_MIXED) return (R)round_bf16((float)v);
+  if (precision == DCG_PRECISION_MIXED_FP16) return (R)round_fp16((float)v);
+  return v;
+}
+
 // Seeded value noise used by the terrain extension. Lattice values come from
 // a 32-bit integer hash; (h >> 8) * 2^-24 is exact in float and double.
 inline uint32_t hash32(uint32_t seed, int32_t i, int32_t k, int32_t o) {
@@ -496,7 +514,8 @@ template <typename R> struct DC : Base {
   // ---------------- restriction ----------------
   // accumulate<T> + k_dcgrid_accumulate_* (dcgrid_structure.cu:188-222),
   // launched per level from fine to coarse (fluid_simulation_dcgrid.cu:496-515).
-  void accumulate(std::vector<R> *const *fields, int nf) {
+  // `scalars`: the fields are advected scalars (stored in the scalar format).
+  void accumulate(std::vector<R> *const *fields, int nf, bool scalars = false) {
     for (int level = 0; level < levels - 1; level++) {
 #pragma omp parallel for schedule(static)
       for (int64_t b = off[level]; b < off[level] + maxL[level]; b++) {
@@ -507,7 +526,7 @@ template <typename R> struct DC : Base {
             std::vector<R> &ch = *fields[f];
             R acc = 0;
             for (int i = 0; i < 8; i++) acc = acc + ch[(size_t)b * BV + 8 * s + i];
-            ch[pc] = acc * (R)0.125f;
+            ch[pc] = scalars ? store_q(acc * (R)0.125f, P.precision) : acc * (R)0.125f;
           }
         }
       }
@@ -519,7 +538,7 @@ template <typename R> struct DC : Base {
   }
   void accumulate_q() {
     std::vector<R> *f[3] = {&q[0], &q[1], &q[2]};
-    accumulate(f, nq);
+    accumulate(f, nq, true);
   }
   void accumulate_div() {
     std::vector<R> *f[1] = {&dv};
@@ -648,7 +667,7 @@ template <typename R> struct DC : Base {
         int x, y, z;
         local_xyz(c, x, y, z);
         if (ph.in_source(bx[b] + x, by[b] + y, bz[b] + z, 1 << lvl[b]))
-          for (int k = 0; k < nq; k++) q[k][cell] = ph.src_value(k);
+          for (int k = 0; k < nq; k++) q[k][cell] = store_q(ph.src_value(k), P.precision);
       }
     }
   }
@@ -674,6 +693,7 @@ template <typename R> struct DC : Base {
             tq[0][cell] = tq[0][cell] + ph.dt * ph.emission_at(bx[b] + x, by[b] + y, bz[b] + z, 1 << lvl[b]);
           if (ph.in_source(bx[b] + x, by[b] + y, bz[b] + z, 1 << lvl[b]))
             for (int k = 0; k < nq; k++) tq[k][cell] = ph.src_value(k);
+          for (int k = 0; k < nq; k++) tq[k][cell] = store_q(tq[k][cell], P.precision);
         } else {
           for (int k = 0; k < nq; k++) tq[k][cell] = 0;
         }
@@ -1102,7 +1122,7 @@ template <typename R> struct DC : Base {
           return (R)(27.f / 64.f) * f[i000] + (R)(9.f / 64.f) * (f[i001] + f[i010] + f[i100]) +
                  (R)(3.f / 64.f) * (f[i011] + f[i101] + f[i110]) + (R)(1.f / 64.f) * f[i111];
         };
-        for (int kq = 0; kq < nq; kq++) q[kq][cell] = tri(q[kq]);
+        for (int kq = 0; kq < nq; kq++) q[kq][cell] = store_q(tri(q[kq]), P.precision);
         for (int d = 0; d < 3; d++) v[d][cell] = tri(v[d]);
         w[cell] = ph.fluidity(x, y, z, scale);
       }
@@ -1197,7 +1217,10 @@ template <typename R> struct DC : Base {
   int set_field(int f, const double *src) override {
     auto *fp = field_ptr(f);
     if (!fp) return fail(DCG_E_NOT_FOUND, "no such field");
-    for (size_t i = 0; i < fp->size(); i++) (*fp)[i] = (R)src[i];
+    const bool narrow = P.precision != DCG_PRECISION_FP32 &&
+                        (f == DCG_FIELD_DENSITY || f == DCG_FIELD_TEMPERATURE || f == DCG_FIELD_VAPOR);
+    for (size_t i = 0; i < fp->size(); i++)
+      (*fp)[i] = narrow ? store_q((R)(float)src[i], P.precision) : (R)src[i];
     return DCG_OK;
   }
   int get_dense(int f, double *dst) override {

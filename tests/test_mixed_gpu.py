@@ -1,0 +1,74 @@
+"""Mixed precision: advected scalars stored in BF16 or FP16, FP32 compute.
+
+* The GPU path equals the oracle's float mirror with the same 16-bit storage
+  rounding, bit for bit, stage by stage.
+* Against the FP64 oracle (driven with the GPU's adaptation decisions, so both
+  share one topology) the relative L2 error per field is reported; FP16 storage
+  keeps density within 1e-3 after 30 steps of the cloud scene.
+"""
+import numpy as np
+import pytest
+
+from dcgrid_gb300 import capi
+from tests import scenarios
+from tests.test_parity_gpu import compare, field_names, gpu, orc
+
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("cuda_ok", "dcg_lib", "oracle_lib")]
+
+
+@pytest.mark.parametrize("prec", [capi.PRECISION_MIXED, capi.PRECISION_MIXED_FP16], ids=["bf16", "fp16"])
+@pytest.mark.parametrize("scene", ["cloud", "plume"])
+def test_mixed_bitexact_vs_float_oracle(prec, scene):
+    p = scenarios.cloud(64, 1500, 3, 10, 0) if scene == "cloud" else scenarios.plume(32, 64, 32, None, 2, 10)
+    p.precision = prec
+    g, o = gpu(p), orc(p)
+    for s in (g, o):
+        s.add_velocity_noise(5, 0.5)
+    compare(g, o, p, "after noise")
+    for step in range(3):
+        for stage in ["advect_velocity", "adapt", "project", "advect_scalars"]:
+            getattr(g, stage)()
+            getattr(o, stage)()
+            g.sync()
+            compare(g, o, p, f"step {step} {stage}")
+
+
+def rel_errors(prec, steps):
+    p = scenarios.cloud(64, 1500, 3, 20, 0)
+    p.precision = prec
+    q = scenarios.cloud(64, 1500, 3, 20, 0)
+    g, o = gpu(p), orc(q, "double")
+    for s in (g, o):
+        s.add_velocity_noise(3, 0.5)
+    for _ in range(steps):
+        g.advect_velocity()
+        o.advect_velocity()
+        g.adapt()
+        moves, refines = g.get_last_adapt()
+        o.adapt_replay(moves, refines)
+        g.project()
+        o.project()
+        g.advect_scalars()
+        o.advect_scalars()
+    g.sync()
+    alloc = np.repeat(o.get_topology()["pos"][:, 3] >= 0, 64)
+    out = {}
+    for f in ["density", "temperature", "vapor", "vel_x", "vel_y", "vel_z", "pressure"]:
+        a = g.get_field(f)[alloc].astype(np.float64)
+        b = o.get_field(f)[alloc]
+        out[f] = float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+    return out
+
+
+@pytest.mark.parametrize("prec,bound", [(capi.PRECISION_FP32, 1e-5), (capi.PRECISION_MIXED_FP16, 1e-3)],
+                         ids=["fp32", "fp16"])
+def test_error_vs_fp64_oracle(prec, bound):
+    err = rel_errors(prec, 30)
+    print("relative L2 error vs FP64 oracle after 30 steps:", {k: f"{v:.2e}" for k, v in err.items()})
+    assert err["density"] <= bound, err
+
+
+def test_bf16_error_is_reported():
+    err = rel_errors(capi.PRECISION_MIXED, 30)
+    print("bf16 relative L2 error vs FP64 oracle after 30 steps:", {k: f"{v:.2e}" for k, v in err.items()})
+    assert err["density"] < 2e-2  # bf16 storage: a few 1e-3; reported, not within the 1e-3 bar
