@@ -5,9 +5,9 @@ include/dcg.h); this package holds its sources (csrc/), the build script and
 a ctypes host API mirroring the reference's simulation interface.
 """
 from . import capi
-from .capi import DcgInfo, DcgParams, DcgStats
-from .sim import (DcgError, FluidSimulationDCGrid, FluidSimulationUniform, Simulation,
+from .capi import DcgInfo, DcgParams, DcgStats, DcgTuning
+from .sim import (Batch, DcgError, FluidSimulationDCGrid, FluidSimulationUniform, Simulation,
                   default_params, lib)
 
-__all__ = ["capi", "DcgParams", "DcgInfo", "DcgStats", "DcgError", "Simulation",
+__all__ = ["capi", "DcgParams", "DcgInfo", "DcgStats", "DcgTuning", "DcgError", "Simulation", "Batch",
            "FluidSimulationDCGrid", "FluidSimulationUniform", "default_params", "lib"]

@@ -121,6 +121,19 @@ class DcgStats(C.Structure):
     ]
 
 
+class DcgTuning(C.Structure):
+    _fields_ = [
+        ("tile", C.c_int32 * 4), ("solve_cache", C.c_int32),
+        ("solve_ctas_per_sm", C.c_int32), ("solve_barrier", C.c_int32),
+        ("reserved", C.c_int32 * 5), ("solve_ms", C.c_float), ("cells_ms", C.c_float * 4),
+    ]
+
+
+def tuning_to_dict(t):
+    return {"tile": list(t.tile), "solve_cache": t.solve_cache, "solve_ctas_per_sm": t.solve_ctas_per_sm,
+            "solve_barrier": t.solve_barrier, "solve_ms": t.solve_ms, "cells_ms": list(t.cells_ms)}
+
+
 def default_params(gx, gy, gz, max_blocks):
     """The reference's SimParams defaults (src/data/sim_params.cpp:4-34) and its
     hard-wired solver/adaptation constants; mirrors dcg_default_params()."""

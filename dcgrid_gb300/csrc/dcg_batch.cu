@@ -1,0 +1,482 @@
+// dcg_batch.cu — many independent adaptive simulations stepped together.
+//
+// The reference runs one simulation per process (its parameters live in one
+// global __constant__ block, src/utils/sim_utils.h:5-6). A batch holds n member
+// simulations (dcg_sim objects with their own pools) and issues each field
+// stage of the step (fluid_simulation_dcgrid.cu:263-346 order) as one launch
+// over all members: the members' device descriptors travel in the kernel
+// parameters, and a CTA picks its member from the cumulative CTA counts.
+// The pressure cascade is one cooperative launch per round over the members'
+// concatenated cells of one level; p and p~ of all members are slices of two
+// batch arenas so the solve addresses them with one base pointer. Member
+// adaptations (sorts and selections of one simulation's blocks) run as
+// parallel branches of the captured step graph. Per-member arithmetic is the
+// single simulation's, so results are bit-identical to standalone runs.
+#include <chrono>
+
+#include "dcg_sim.h"
+
+struct dcg_batch {
+  std::vector<dcg_sim *> m;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::vector<cudaStream_t> aux;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr;
+  int device = 0, sms = 148;
+  std::string err;
+  std::vector<void *> allocs;
+  size_t bytes = 0;
+  float *p_arena = nullptr, *pt_arena = nullptr;
+  uint32_t *bar = nullptr, *errw = nullptr;
+  std::vector<unsigned long long> arena_off;
+  int maxtop = 0, iters = 0;
+  dcg_tuning tune{};
+  int solve_grid = 0;
+  std::map<int, cudaGraphExec_t> graphs;
+  long long kernels_per_step = 0;
+
+  int fail(int code, const std::string &msg) {
+    err = msg;
+    return code;
+  }
+  int cuda(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return DCG_OK;
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return DCG_E_CUDA;
+  }
+  template <typename T> int alloc(T **p, size_t count) {
+    void *q = nullptr;
+    const size_t nbytes = std::max<size_t>(count * sizeof(T), 256);
+    cudaError_t e = cudaMalloc(&q, nbytes);
+    if (e != cudaSuccess) return cuda(e, "cudaMalloc");
+    allocs.push_back(q);
+    bytes += nbytes;
+    *p = reinterpret_cast<T *>(q);
+    return DCG_OK;
+  }
+  void drop_graphs() {
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+  }
+  ~dcg_batch() {
+    if (stream) cudaStreamSynchronize(stream);
+    drop_graphs();
+    for (dcg_sim *s : m) delete s;
+    for (void *p : allocs) cudaFree(p);
+    for (cudaStream_t a : aux) cudaStreamDestroy(a);
+    for (cudaEvent_t e : joins) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (own_stream && stream) cudaStreamDestroy(stream);
+  }
+
+  int n() const { return (int)m.size(); }
+  int groups() const { return (n() + BMAX - 1) / BMAX; }
+
+  int set_solve_config() {
+    if (tune.solve_cache != 0 && tune.solve_cache != 4 && tune.solve_cache != 8)
+      return fail(DCG_E_INVALID, "solve_cache must be 0, 4 or 8");
+    for (int k = 0; k < 4; k++)
+      if (tune.tile[k] != 2 && tune.tile[k] != 4 && tune.tile[k] != 8)
+        return fail(DCG_E_INVALID, "tiles must be 2, 4 or 8 blocks");
+    solve_grid = batch_solve_grid(sms, tune.solve_cache, tune.solve_ctas_per_sm);
+    if (solve_grid <= 0) return fail(DCG_E_CUDA, "cooperative level solve cannot be resident");
+    return DCG_OK;
+  }
+
+  // ------------------------------------------------------------ stage launches
+  void cells(int stage) {
+    for (int g = 0; g < groups(); g++) {
+      CellBatch P{};
+      P.n = std::min(BMAX, n() - g * BMAX);
+      for (int i = 0; i < P.n; i++) P.d[i] = m[g * BMAX + i]->D;
+      launch_cells_batch(stage, P, tune.tile[stage], stream);
+    }
+  }
+  // field: 0 velocity, 1 scalars, 2 divergence
+  void restrict_fields(int field) {
+    int maxl = 0;
+    for (dcg_sim *s : m) maxl = std::max(maxl, s->D.g.levels);
+    for (int level = 0; level < maxl - 1; level++)
+      for (int g = 0; g < groups(); g++) {
+        RestrictBatch P{};
+        P.n = std::min(BMAX, n() - g * BMAX);
+        P.level = level;
+        for (int i = 0; i < P.n; i++) {
+          const dcg_sim *s = m[g * BMAX + i];
+          P.d[i] = s->D;
+          FieldList &fl = P.fl[i];
+          if (field == 0) {
+            fl.n = 3;
+            for (int d = 0; d < 3; d++) fl.f[d] = s->D.v[d];
+          } else if (field == 1) {
+            fl.n = s->P.n_scalars;
+            for (int k = 0; k < fl.n; k++) {
+              fl.f[k] = s->D.g.mixed ? static_cast<void *>(s->D.qh[k]) : static_cast<void *>(s->D.q[k]);
+              fl.mode[k] = s->D.g.mixed;
+            }
+          } else {
+            fl.n = 1;
+            fl.f[0] = s->D.div;
+          }
+        }
+        launch_restrict_batch(P, stream);
+      }
+  }
+  void solve(int grid, int cache, int tree) {
+    for (int round = 0; round <= maxtop; round++)
+      for (int g = 0; g < groups(); g++) {
+        SolveBatch P{};
+        P.n = std::min(BMAX, n() - g * BMAX);
+        P.maxtop = maxtop;
+        P.prolong = 1;
+        P.p = p_arena;
+        P.pt = pt_arena;
+        P.bar = bar;
+        P.err = errw;
+        for (int i = 0; i < P.n; i++) {
+          P.d[i] = m[g * BMAX + i]->D;
+          P.arena[i] = arena_off[g * BMAX + i];
+        }
+        launch_level_solve_batch(P, round, iters, grid, cache, tree, stream);
+      }
+  }
+  void flip_v() {
+    for (dcg_sim *s : m) {
+      s->vpar ^= 1;
+      s->bind_parity();
+    }
+  }
+  void flip_q() {
+    for (dcg_sim *s : m) {
+      s->qpar ^= 1;
+      s->bind_parity();
+    }
+  }
+  void adapt_branches() {
+    cudaEventRecord(fork, stream);
+    for (int i = 0; i < n(); i++) {
+      cudaStreamWaitEvent(aux[i], fork, 0);
+      dcg_sim *s = m[i];
+      launch_adapt(s->D, s->S, s->keys, s->vals, s->keys2, s->vals2, s->sms, aux[i]);
+      cudaEventRecord(joins[i], aux[i]);
+    }
+    for (int i = 0; i < n(); i++) cudaStreamWaitEvent(stream, joins[i], 0);
+  }
+  // Simulation::updateSimulation (simulation.cpp:104-112) for every member
+  void step_once() {
+    cells(0);  // advect velocity (+ buoyancy)
+    flip_v();
+    restrict_fields(0);
+    adapt_branches();
+    cells(2);  // divergence
+    restrict_fields(2);
+    solve(solve_grid, tune.solve_cache, tune.solve_barrier);
+    cells(3);  // apply pressure
+    restrict_fields(0);
+    cells(1);  // advect scalars (+ sources, emission)
+    flip_q();
+    restrict_fields(1);
+  }
+
+  int step(int count) {
+    for (int i = 0; i < count; i++) {
+      const int key = m[0]->vpar * 2 + m[0]->qpar;
+      auto it = graphs.find(key);
+      int rc;
+      if (it == graphs.end()) {
+        cudaGraph_t g = nullptr;
+        if ((rc = cuda(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "capture"))) return rc;
+        step_once();
+        if ((rc = cuda(cudaStreamEndCapture(stream, &g), "end capture"))) return rc;
+        size_t nn = 0;
+        if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn > 0) {
+          std::vector<cudaGraphNode_t> nodes(nn);
+          cudaGraphGetNodes(g, nodes.data(), &nn);
+          long long nk = 0;
+          for (auto nd : nodes) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) nk++;
+          }
+          kernels_per_step = nk;
+        }
+        cudaGraphExec_t ge = nullptr;
+        rc = cuda(cudaGraphInstantiate(&ge, g, 0), "instantiate");
+        cudaGraphDestroy(g);
+        if (rc) return rc;
+        graphs[key] = ge;
+        // step_once() advanced the members' parities while capturing
+        if ((rc = cuda(cudaGraphLaunch(ge, stream), "graph launch"))) return rc;
+      } else {
+        if ((rc = cuda(cudaGraphLaunch(it->second, stream), "graph launch"))) return rc;
+        flip_v();
+        flip_q();
+      }
+      for (dcg_sim *s : m) s->steps++;
+    }
+    return cuda(cudaGetLastError(), "batch step");
+  }
+
+  int reset() {
+    int rc;
+    if ((rc = cuda(cudaStreamSynchronize(stream), "sync"))) return rc;
+    cudaMemsetAsync(bar, 0, 4 * (64 + 32 * 18), stream);
+    cudaMemsetAsync(errw, 0, 4, stream);
+    for (dcg_sim *s : m)
+      if ((rc = s->reset_adaptive())) return fail(rc, "member reset: " + s->err);
+    return cuda(cudaStreamSynchronize(stream), "reset");
+  }
+
+  int sync() {
+    int rc;
+    if ((rc = cuda(cudaStreamSynchronize(stream), "sync"))) return rc;
+    if ((rc = cuda(cudaGetLastError(), "sync"))) return rc;
+    uint32_t e = 0;
+    if ((rc = cuda(cudaMemcpy(&e, errw, 4, cudaMemcpyDeviceToHost), "err word"))) return rc;
+    if (e) {
+      char buf[64];
+      std::snprintf(buf, sizeof buf, "batch device error word 0x%x", e);
+      return fail(DCG_E_DEVICE, buf);
+    }
+    for (int i = 0; i < n(); i++) {
+      if ((rc = cuda(cudaMemcpy(&e, m[i]->D.err, 4, cudaMemcpyDeviceToHost), "err word"))) return rc;
+      if (e) {
+        char buf[80];
+        std::snprintf(buf, sizeof buf, "member %d device error word 0x%x", i, e);
+        return fail(DCG_E_DEVICE, buf);
+      }
+    }
+    return DCG_OK;
+  }
+
+  // CUDA-event time of fn() averaged over reps (one warm call first)
+  template <class F> float time_ms(int reps, F fn) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    fn();
+    cudaEventRecord(e0, stream);
+    for (int r = 0; r < reps; r++) fn();
+    cudaEventRecord(e1, stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms / (float)reps;
+  }
+
+  int autotune(int spinup, int reps, dcg_tuning *out) {
+    int rc;
+    if ((rc = reset())) return rc;
+    if ((rc = step(spinup))) return rc;
+    if ((rc = sync())) return rc;
+    // cell stages: every tile, each stage independently
+    const int tiles[3] = {2, 4, 8};
+    dcg_tuning best = tune;
+    for (int stage = 0; stage < 4; stage++) {
+      float best_ms = 1e30f;
+      for (int tile : tiles) {
+        tune.tile[stage] = tile;
+        const float ms = time_ms(reps, [&] { cells(stage); });
+        if (ms < best_ms) {
+          best_ms = ms;
+          best.tile[stage] = tile;
+        }
+      }
+      best.cells_ms[stage] = best_ms;
+      tune.tile[stage] = best.tile[stage];
+    }
+    // level solve: cache depth x CTAs per SM x barrier kind
+    float best_solve = 1e30f;
+    for (int cache : {0, 4, 8}) {
+      const int occ = batch_solve_grid(sms, cache, 0) / std::max(1, sms);
+      for (int k = 1; k <= occ; k++)
+        for (int tree = 0; tree < 2; tree++) {
+          const int grid = batch_solve_grid(sms, cache, k);
+          const float ms = time_ms(reps, [&] { solve(grid, cache, tree); });
+          if (ms < best_solve) {
+            best_solve = ms;
+            best.solve_cache = cache;
+            best.solve_ctas_per_sm = k;
+            best.solve_barrier = tree;
+          }
+        }
+    }
+    best.solve_ms = best_solve;
+    if ((rc = sync())) return rc;
+    tune = best;
+    if ((rc = set_solve_config())) return rc;
+    drop_graphs();
+    if ((rc = reset())) return rc;
+    if (out) *out = tune;
+    return DCG_OK;
+  }
+
+  int time_solve(int reps, float *avg_ms, double *bytes_out) {
+    int rc;
+    if ((rc = sync())) return rc;
+    double cells_sweeps = 0;
+    for (dcg_sim *s : m) {
+      long long load[MAXL];
+      if ((rc = cuda(cudaMemcpy(load, s->D.load, sizeof(load), cudaMemcpyDeviceToHost), "load"))) return rc;
+      for (int l = 0; l < s->D.g.levels; l++) cells_sweeps += 64.0 * (double)load[l] * iters;
+    }
+    *avg_ms = time_ms(reps, [&] { solve(solve_grid, tune.solve_cache, tune.solve_barrier); });
+    if (bytes_out) *bytes_out = 12.0 * cells_sweeps;
+    return sync();
+  }
+};
+
+static int bad(const dcg_batch *b) { return b == nullptr; }
+
+extern "C" {
+
+int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
+  if (!params || !out || n <= 0) return DCG_E_INVALID;
+  *out = nullptr;
+  dcg_batch *b = new dcg_batch();
+  cudaError_t e = cudaGetDevice(&b->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    delete b;
+    return DCG_E_CUDA;
+  }
+  b->own_stream = true;
+  b->iters = params[0].jacobi_iters;
+  // arenas for p and p~: member i's planes start at cell arena_off[i]
+  unsigned long long cells = 0;
+  for (int i = 0; i < n; i++) {
+    if (params[i].jacobi_iters != b->iters) {
+      delete b;
+      return DCG_E_INVALID;  // one sweep schedule per batch
+    }
+    if (params[i].max_blocks <= 0 || params[i].max_blocks >= (1ll << 28)) {
+      delete b;
+      return DCG_E_INVALID;
+    }
+    b->arena_off.push_back(cells);
+    cells += (unsigned long long)params[i].max_blocks * BV;
+  }
+  if (cells >= (1ull << 32)) {
+    delete b;
+    return DCG_E_INVALID;  // arena cells are addressed with 32-bit indices
+  }
+  int rc;
+  if ((rc = b->alloc(&b->p_arena, cells)) || (rc = b->alloc(&b->pt_arena, cells)) ||
+      (rc = b->alloc(&b->bar, 64 + 32 * 18)) || (rc = b->alloc(&b->errw, 4))) {
+    delete b;
+    return rc;
+  }
+  cudaMemset(b->bar, 0, 4 * (64 + 32 * 18));
+  cudaMemset(b->errw, 0, 4);
+  for (int i = 0; i < n; i++) {
+    dcg_sim *s = new dcg_sim();
+    s->P = params[i];
+    s->mode = DCG_MODE_ADAPTIVE;
+    s->device = b->device;
+    s->sms = b->sms;
+    s->stream = b->stream;
+    s->own_stream = false;
+    s->batch_member = true;
+    s->ext_p = b->p_arena + b->arena_off[i];
+    s->ext_pt = b->pt_arena + b->arena_off[i];
+    b->m.push_back(s);
+    if ((rc = s->create_adaptive())) {
+      b->err = "member " + std::to_string(i) + ": " + s->err;
+      delete b;
+      return rc;
+    }
+    b->maxtop = std::max(b->maxtop, s->D.g.levels - 1);
+    cudaStream_t a = nullptr;
+    cudaEvent_t j = nullptr;
+    if (cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&j, cudaEventDisableTiming) != cudaSuccess) {
+      delete b;
+      return DCG_E_CUDA;
+    }
+    b->aux.push_back(a);
+    b->joins.push_back(j);
+  }
+  for (int k = 0; k < 4; k++) b->tune.tile[k] = 4;
+  b->tune.solve_cache = 4;
+  b->tune.solve_ctas_per_sm = 0;
+  b->tune.solve_barrier = 1;
+  if ((rc = b->set_solve_config())) {
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return DCG_OK;
+}
+
+int dcg_batch_destroy(dcg_batch *b) {
+  if (bad(b)) return DCG_E_INVALID;
+  delete b;
+  return DCG_OK;
+}
+int dcg_batch_reset(dcg_batch *b) { return bad(b) ? DCG_E_INVALID : b->reset(); }
+int dcg_batch_step(dcg_batch *b, int32_t n) {
+  if (bad(b) || n < 0) return DCG_E_INVALID;
+  return b->step(n);
+}
+int dcg_batch_sync(dcg_batch *b) { return bad(b) ? DCG_E_INVALID : b->sync(); }
+int dcg_batch_member(dcg_batch *b, int32_t i, dcg_sim **out) {
+  if (bad(b) || !out || i < 0 || i >= b->n()) return DCG_E_INVALID;
+  *out = b->m[i];
+  return DCG_OK;
+}
+int dcg_batch_set_stream(dcg_batch *b, void *cuda_stream) {
+  if (bad(b)) return DCG_E_INVALID;
+  cudaStreamSynchronize(b->stream);
+  if (b->own_stream) cudaStreamDestroy(b->stream);
+  b->own_stream = false;
+  b->stream = reinterpret_cast<cudaStream_t>(cuda_stream);
+  for (dcg_sim *s : b->m) s->stream = b->stream;
+  b->drop_graphs();
+  return DCG_OK;
+}
+int dcg_batch_autotune(dcg_batch *b, int32_t spinup_steps, int32_t reps, dcg_tuning *out) {
+  if (bad(b) || spinup_steps < 0 || reps <= 0) return DCG_E_INVALID;
+  return b->autotune(spinup_steps, reps, out);
+}
+int dcg_batch_get_tuning(const dcg_batch *b, dcg_tuning *out) {
+  if (bad(b) || !out) return DCG_E_INVALID;
+  *out = b->tune;
+  return DCG_OK;
+}
+int dcg_batch_set_tuning(dcg_batch *b, const dcg_tuning *t) {
+  if (bad(b) || !t) return DCG_E_INVALID;
+  const dcg_tuning before = b->tune;
+  b->tune = *t;
+  int rc = b->set_solve_config();
+  if (rc) {
+    b->tune = before;
+    b->set_solve_config();
+    return rc;
+  }
+  cudaStreamSynchronize(b->stream);
+  b->drop_graphs();
+  return DCG_OK;
+}
+int dcg_batch_get_info(const dcg_batch *b, int32_t *n, int64_t *device_bytes, int64_t *launches_per_step) {
+  if (bad(b)) return DCG_E_INVALID;
+  if (n) *n = b->n();
+  if (device_bytes) {
+    size_t t = b->bytes;
+    for (const dcg_sim *s : b->m) t += s->bytes;
+    *device_bytes = (int64_t)t;
+  }
+  if (launches_per_step) *launches_per_step = b->kernels_per_step;
+  return DCG_OK;
+}
+int dcg_batch_time_solve(dcg_batch *b, int32_t reps, float *avg_ms, double *bytes) {
+  if (bad(b) || reps <= 0 || !avg_ms) return DCG_E_INVALID;
+  return b->time_solve(reps, avg_ms, bytes);
+}
+const char *dcg_batch_last_error_string(const dcg_batch *b) { return b ? b->err.c_str() : "null handle"; }
+size_t dcg_sizeof_tuning(void) { return sizeof(dcg_tuning); }
+
+}  // extern "C"

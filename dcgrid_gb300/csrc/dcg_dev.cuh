@@ -100,12 +100,12 @@ struct Dev {
 // last there releases everyone through the generation word. Same bounded wait
 // and timeout rule as grid_barrier. Layout (u32, from bar + 64): [0]
 // generation, [32*(1+g)] group g counter, [32*17] top counter.
-__device__ inline void grid_barrier_tree(const Dev &D, unsigned nctas) {
+__device__ inline void grid_barrier_tree(uint32_t *bar, uint32_t *errw, unsigned nctas) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    unsigned *tb = D.bar + 64;
+    unsigned *tb = bar + 64;
     volatile unsigned *gen = tb;
-    volatile unsigned *err = D.err;
+    volatile unsigned *err = errw;
     if ((*err & 8u) == 0) {
       const unsigned g = *gen;
       const unsigned grp = blockIdx.x & 15u;
@@ -128,7 +128,7 @@ __device__ inline void grid_barrier_tree(const Dev &D, unsigned nctas) {
         while (*gen == g) {
           __nanosleep(32);
           if (++spins > (1u << 22) || (*err & 8u)) {
-            atomicOr(D.err, 8u);
+            atomicOr(errw, 8u);
             break;
           }
         }
@@ -138,29 +138,30 @@ __device__ inline void grid_barrier_tree(const Dev &D, unsigned nctas) {
   }
   __syncthreads();
 }
+__device__ inline void grid_barrier_tree(const Dev &D, unsigned nctas) { grid_barrier_tree(D.bar, D.err, nctas); }
 
 // Grid-wide barrier for cooperative launches (all CTAs co-resident). The wait
 // is bounded: after 2^22 polls the CTA records DCG_DEVERR_TIMEOUT (8) in the
 // error word and continues; once that bit is set every later barrier returns
 // at once, so a broken barrier costs one bounded wait and never hangs the GPU.
-__device__ inline void grid_barrier(const Dev &D, unsigned nctas) {
+__device__ inline void grid_barrier(uint32_t *bar, uint32_t *errw, unsigned nctas) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned *gen = D.bar + 1;
-    volatile unsigned *err = D.err;
+    volatile unsigned *gen = bar + 1;
+    volatile unsigned *err = errw;
     if ((*err & 8u) == 0) {
       const unsigned g = *gen;
       __threadfence();
-      if (atomicAdd(D.bar, 1u) == nctas - 1) {
-        atomicExch(D.bar, 0u);
+      if (atomicAdd(bar, 1u) == nctas - 1) {
+        atomicExch(bar, 0u);
         __threadfence();
-        atomicAdd(D.bar + 1, 1u);
+        atomicAdd(bar + 1, 1u);
       } else {
         unsigned spins = 0;
         while (*gen == g) {
           __nanosleep(32);
           if (++spins > (1u << 22) || (*err & 8u)) {
-            atomicOr(D.err, 8u);
+            atomicOr(errw, 8u);
             break;
           }
         }
@@ -170,6 +171,7 @@ __device__ inline void grid_barrier(const Dev &D, unsigned nctas) {
   }
   __syncthreads();
 }
+__device__ inline void grid_barrier(const Dev &D, unsigned nctas) { grid_barrier(D.bar, D.err, nctas); }
 
 // ---------------------------------------------------------------- index math
 __host__ __device__ inline int spread2(int d, int off) { return ((d & 1) | ((d << 2) & 8)) << off; }

@@ -38,6 +38,39 @@ void launch_apply_pressure(const Dev &D, cudaStream_t st);
 int level_solve_grid(int sms);
 void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int grid, int epoch_sync, cudaStream_t st);
 
+// ---- batched launches (many independent simulations per launch)
+// Member devices travel in the kernel parameters (__grid_constant__, read
+// through the constant cache); BMAX members fit the 32 KB parameter space.
+constexpr int BMAX = 16;
+// cell stages: 0 advect velocity, 1 advect scalars, 2 divergence, 3 apply pressure
+struct CellBatch {
+  int n, pad;
+  long long end[BMAX];  // cumulative CTA count of members 0..s
+  Dev d[BMAX];
+};
+struct RestrictBatch {
+  int n, level;
+  long long end[BMAX];
+  Dev d[BMAX];
+  FieldList fl[BMAX];
+};
+// Cascade round r solves level maxtop - r of every member that has it (finest
+// levels aligned); p and p~ of all members are slices of two arenas.
+struct SolveBatch {
+  int n, maxtop, prolong, pad;
+  float *p, *pt;
+  uint32_t *bar, *err;
+  unsigned long long arena[BMAX];  // first cell of member s in the arenas
+  Dev d[BMAX];
+};
+static_assert(sizeof(RestrictBatch) < 32000 && sizeof(SolveBatch) < 32000, "kernel parameter space");
+void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st);
+void launch_restrict_batch(RestrictBatch &P, cudaStream_t st);
+// CTAs of the batched solve for a cache depth (0, 4, 8) and CTAs per SM (0 = occupancy limit)
+int batch_solve_grid(int sms, int cache, int ctas_per_sm);
+void launch_level_solve_batch(const SolveBatch &P, int round, int sweeps, int grid, int cache, int tree,
+                              cudaStream_t st);
+
 // k_topology.cu
 void launch_init_blocks(const Dev &D, cudaStream_t st);
 void launch_activate_level(const Dev &D, int level, cudaStream_t st);

@@ -95,12 +95,10 @@ __device__ inline void back_trace(const Dev &D, int4 bp, int c, size_t cell, flo
 
 // k_dcgrid_advect_velocity (dcgrid_fluid.cu:112-127) + buoyancy extension:
 // v.y += dt * (-alpha * rho + beta * (T - T_amb)) on leaf cells.
-__global__ void __launch_bounds__(256) k_advect_velocity(Dev D) {
-  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+__device__ __forceinline__ void advect_velocity_cell(const Dev &D, long long b, int c) {
   if (b >= D.g.B) return;
   const int4 bp = D.pos[b];
   if (bp.w < 0) return;
-  const int c = threadIdx.x & 63;
   const size_t cell = (size_t)b * BV + c;
   float o0 = 0.f, o1 = 0.f, o2 = 0.f;
   if (D.child[cell >> 3] == NONE) {
@@ -135,12 +133,10 @@ __global__ void __launch_bounds__(256) k_advect_velocity(Dev D) {
 
 // k_dcgrid_advect_density (dcgrid_fluid.cu:129-144) for every scalar; sphere
 // sources (extension) overwrite leaf cells inside the source.
-__global__ void __launch_bounds__(256) k_advect_scalars(Dev D) {
-  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+__device__ __forceinline__ void advect_scalars_cell(const Dev &D, long long b, int c) {
   if (b >= D.g.B) return;
   const int4 bp = D.pos[b];
   if (bp.w < 0) return;
-  const int c = threadIdx.x & 63;
   const size_t cell = (size_t)b * BV + c;
   const int nq = D.g.nq;
   float o[3] = {0.f, 0.f, 0.f};
@@ -205,8 +201,7 @@ __global__ void __launch_bounds__(256) k_add_noise(Dev D, unsigned long long see
 
 // accumulate<T> (dcgrid_structure.cu:188-205): parent cell = mean of the 8
 // cells of the child subblock; one thread per subblock of one level.
-__global__ void __launch_bounds__(256) k_restrict(Dev D, int level, FieldList fl) {
-  const long long sl = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void restrict_subblock(const Dev &D, int level, const FieldList &fl, long long sl) {
   if (sl >= 8 * D.g.budget[level]) return;
   const long long b = D.g.off[level] + (sl >> 3);
   if (D.pos[b].w != level) return;
@@ -244,12 +239,10 @@ __global__ void __launch_bounds__(256) k_restrict(Dev D, int level, FieldList fl
 // k_dcgrid_calc_divergence (dcgrid_fluid.cu:174-230): zero p, p~, div on all
 // cells; div on leaf cells from fluidity-weighted central differences, apron
 // velocities through the boundary conditions.
-__global__ void __launch_bounds__(256) k_divergence(Dev D) {
-  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+__device__ __forceinline__ void divergence_cell(const Dev &D, long long b, int c) {
   if (b >= D.g.B) return;
   const int4 bp = D.pos[b];
   if (bp.w < 0) return;
-  const int c = threadIdx.x & 63;
   const size_t cell = (size_t)b * BV + c;
   D.p[cell] = 0.f;
   D.pt[cell] = 0.f;
@@ -520,12 +513,10 @@ __global__ void __launch_bounds__(256) k_level_solve(Dev D, int level, int prolo
 }
 
 // k_dcgrid_apply_pressure (dcgrid_fluid.cu:232-259) on leaf cells.
-__global__ void __launch_bounds__(256) k_apply_pressure(Dev D) {
-  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+__device__ __forceinline__ void apply_pressure_cell(const Dev &D, long long b, int c) {
   if (b >= D.g.B) return;
   const int4 bp = D.pos[b];
   if (bp.w < 0) return;
-  const int c = threadIdx.x & 63;
   const size_t cell = (size_t)b * BV + c;
   if (D.child[cell >> 3] != NONE) return;
   int lx, ly, lz;
@@ -544,6 +535,17 @@ __global__ void __launch_bounds__(256) k_apply_pressure(Dev D) {
   D.v[0][cell] = D.v[0][cell] - alpha * (W[R] * (P[R] - pc) + W[L] * (pc - P[L]));
   D.v[1][cell] = D.v[1][cell] - alpha * (W[U] * (P[U] - pc) + W[Dn] * (pc - P[Dn]));
   D.v[2][cell] = D.v[2][cell] - alpha * (W[F] * (P[F] - pc) + W[Bk] * (pc - P[Bk]));
+}
+
+// ------------------------------------------------------------ single-simulation kernels
+// 256-thread CTAs, 4 blocks of 64 cells per CTA.
+__device__ __forceinline__ long long cta_block4() { return (long long)blockIdx.x * 4 + (threadIdx.x >> 6); }
+__global__ void __launch_bounds__(256) k_advect_velocity(Dev D) { advect_velocity_cell(D, cta_block4(), threadIdx.x & 63); }
+__global__ void __launch_bounds__(256) k_advect_scalars(Dev D) { advect_scalars_cell(D, cta_block4(), threadIdx.x & 63); }
+__global__ void __launch_bounds__(256) k_divergence(Dev D) { divergence_cell(D, cta_block4(), threadIdx.x & 63); }
+__global__ void __launch_bounds__(256) k_apply_pressure(Dev D) { apply_pressure_cell(D, cta_block4(), threadIdx.x & 63); }
+__global__ void __launch_bounds__(256) k_restrict(Dev D, int level, FieldList fl) {
+  restrict_subblock(D, level, fl, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ------------------------------------------------------------------ launchers
@@ -601,6 +603,198 @@ void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int gr
   cfg.numAttrs = 1;
   if (cached) cudaLaunchKernelEx(&cfg, k_level_solve<LS_CACHE>, D, level, prolong, sweeps, epoch_sync);
   else cudaLaunchKernelEx(&cfg, k_level_solve<0>, D, level, prolong, sweeps, epoch_sync == 2 ? 2 : 0);
+}
+
+// ------------------------------------------------------------------ batched kernels
+// Many independent simulations per launch. CTA ranges are assigned to the
+// members in order (P.end is cumulative); a CTA finds its member with a short
+// scan of uniform parameter loads and runs the same cell body as the
+// single-simulation kernels, so a member's results are bit-identical to those
+// of a standalone simulation. TB = blocks of 64 cells per CTA (the tile).
+__device__ __forceinline__ int batch_member(const long long *end, int n, long long x) {
+  int s = 0;
+  while (s + 1 < n && x >= end[s]) s++;
+  return s;
+}
+
+template <int TB, int STAGE>
+__global__ void __launch_bounds__(64 * TB) k_cells_batch(const __grid_constant__ CellBatch P) {
+  const int s = batch_member(P.end, P.n, blockIdx.x);
+  const long long b = ((long long)blockIdx.x - (s ? P.end[s - 1] : 0)) * TB + (threadIdx.x >> 6);
+  const Dev &D = P.d[s];
+  const int c = threadIdx.x & 63;
+  if (STAGE == 0) advect_velocity_cell(D, b, c);
+  else if (STAGE == 1) advect_scalars_cell(D, b, c);
+  else if (STAGE == 2) divergence_cell(D, b, c);
+  else apply_pressure_cell(D, b, c);
+}
+
+__global__ void __launch_bounds__(256) k_restrict_batch(const __grid_constant__ RestrictBatch P) {
+  const int s = batch_member(P.end, P.n, blockIdx.x);
+  const Dev &D = P.d[s];
+  if (P.level >= D.g.levels - 1) return;
+  restrict_subblock(D, P.level, P.fl[s], ((long long)blockIdx.x - (s ? P.end[s - 1] : 0)) * 256 + threadIdx.x);
+}
+
+// One round of the batched cascade: level maxtop - round of every member that
+// has it, optional prolongation from the member's parent level, then `sweeps`
+// Jacobi sweeps over the concatenated cells of all members, separated by grid
+// barriers (tree != 0: two-level barrier). Member m's cells of the level
+// occupy [s_end[m-1], s_end[m]) of the concatenated index. With CACHE > 0 and
+// at most CACHE cells per thread, each thread keeps, per cell, the six
+// neighbour cells and its own cell as arena indices plus alpha*div in dynamic
+// shared memory ([CACHE][8][256] words); a sweep is then six loads and one
+// store per cell. Arithmetic is that of k_jacobi (identical results).
+template <int CACHE>
+__global__ void __launch_bounds__(256) k_level_solve_batch(const __grid_constant__ SolveBatch P, int round, int sweeps,
+                                                           int tree) {
+  __shared__ long long s_end[BMAX];
+  __shared__ int s_lev[BMAX];
+  extern __shared__ uint32_t s_cache[];
+  const int t = threadIdx.x;
+  if (t == 0) {
+    long long acc = 0;
+    const int lev = P.maxtop - round;
+    for (int m = 0; m < P.n; m++) {
+      const Dev &D = P.d[m];
+      if (lev >= 0 && lev < D.g.levels) acc += __ldcg(D.load + lev) * 64;
+      s_lev[m] = lev;
+      s_end[m] = acc;
+    }
+  }
+  __syncthreads();
+  const long long total = s_end[P.n - 1];
+  const unsigned nctas = gridDim.x;
+  const long long stride = (long long)nctas * 256;
+  const long long first = (long long)blockIdx.x * 256 + t;
+  auto cell_of = [&](long long gi, int &m) {
+    m = batch_member(s_end, P.n, gi);
+    return P.d[m].g.off[s_lev[m]] * 64 + (gi - (m ? s_end[m - 1] : 0));
+  };
+  if (P.prolong)
+    for (long long gi = first; gi < total; gi += stride) {
+      int m;
+      const long long cell = cell_of(gi, m);
+      if (s_lev[m] < P.d[m].g.levels - 1) prolong_cell(P.d[m], cell);
+    }
+  if (sweeps <= 0) return;
+  auto barrier = [&]() {
+    if (tree) grid_barrier_tree(P.bar, P.err, nctas);
+    else grid_barrier(P.bar, P.err, nctas);
+  };
+  barrier();
+  const int rounds = (int)((total + stride - 1) / stride);
+  if (CACHE > 0 && rounds <= CACHE) {
+    for (int r = 0; r < rounds; r++) {
+      const long long gi = first + r * stride;
+      if (gi < total) {
+        int m;
+        const long long cell = cell_of(gi, m);
+        const Dev &D = P.d[m];
+        const Nb6 n = jacobi_neighbours(D, cell);
+        const uint32_t a = (uint32_t)P.arena[m];
+        uint32_t *e = s_cache + r * 8 * 256 + t;
+        e[0] = a + n.i0; e[256] = a + n.i1; e[512] = a + n.i2;
+        e[768] = a + n.i3; e[1024] = a + n.i4; e[1280] = a + n.i5;
+        e[1536] = a + (uint32_t)cell;
+        const int sc = 1 << s_lev[m];
+        const float alpha = (float)(sc * sc) * D.ph.dx * D.ph.dx;
+        e[1792] = __float_as_uint(alpha * D.div[cell]);
+      }
+    }
+    for (int it = 0; it < sweeps; it++) {
+      const float *src = (it & 1) ? P.pt : P.p;
+      float *dst = (it & 1) ? P.p : P.pt;
+      for (int r = 0; r < rounds; r++) {
+        if (first + r * stride < total) {
+          const uint32_t *e = s_cache + r * 8 * 256 + t;
+          const Nb6 n = {e[0], e[256], e[512], e[768], e[1024], e[1280]};
+          dst[e[1536]] = jacobi_update(src, n, __uint_as_float(e[1792]));
+        }
+      }
+      if (it + 1 < sweeps) barrier();
+    }
+  } else {
+    for (int it = 0; it < sweeps; it++) {
+      const float *src = (it & 1) ? P.pt : P.p;
+      float *dst = (it & 1) ? P.p : P.pt;
+      for (long long gi = first; gi < total; gi += stride) {
+        int m;
+        const long long cell = cell_of(gi, m);
+        const Dev &D = P.d[m];
+        const uint32_t a = (uint32_t)P.arena[m];
+        Nb6 n = jacobi_neighbours(D, cell);
+        n.i0 += a; n.i1 += a; n.i2 += a; n.i3 += a; n.i4 += a; n.i5 += a;
+        const int sc = 1 << s_lev[m];
+        const float alpha = (float)(sc * sc) * D.ph.dx * D.ph.dx;
+        dst[a + (uint32_t)cell] = jacobi_update(src, n, alpha * D.div[cell]);
+      }
+      if (it + 1 < sweeps) barrier();
+    }
+  }
+}
+
+template <int TB>
+static void cells_batch_tb(int stage, const CellBatch &P, unsigned grid, cudaStream_t st) {
+  switch (stage) {
+    case 0: k_cells_batch<TB, 0><<<grid, 64 * TB, 0, st>>>(P); break;
+    case 1: k_cells_batch<TB, 1><<<grid, 64 * TB, 0, st>>>(P); break;
+    case 2: k_cells_batch<TB, 2><<<grid, 64 * TB, 0, st>>>(P); break;
+    default: k_cells_batch<TB, 3><<<grid, 64 * TB, 0, st>>>(P); break;
+  }
+}
+void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st) {
+  if (tile != 2 && tile != 8) tile = 4;
+  long long acc = 0;
+  for (int m = 0; m < P.n; m++) {
+    acc += (P.d[m].g.B + tile - 1) / tile;
+    P.end[m] = acc;
+  }
+  if (acc == 0) return;
+  if (tile == 2) cells_batch_tb<2>(stage, P, (unsigned)acc, st);
+  else if (tile == 8) cells_batch_tb<8>(stage, P, (unsigned)acc, st);
+  else cells_batch_tb<4>(stage, P, (unsigned)acc, st);
+}
+void launch_restrict_batch(RestrictBatch &P, cudaStream_t st) {
+  long long acc = 0;
+  for (int m = 0; m < P.n; m++) {
+    if (P.level < P.d[m].g.levels - 1) acc += (8 * P.d[m].g.budget[P.level] + 255) / 256;
+    P.end[m] = acc;
+  }
+  if (acc > 0) k_restrict_batch<<<(unsigned)acc, 256, 0, st>>>(P);
+}
+
+template <int C>
+static int solve_batch_occupancy() {
+  const int smem = C * 8 * 256 * 4;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_level_solve_batch<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    return 0;
+  int a = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_level_solve_batch<C>, 256, smem) != cudaSuccess) return 0;
+  return a;
+}
+int batch_solve_grid(int sms, int cache, int ctas_per_sm) {
+  const int occ = cache == 8 ? solve_batch_occupancy<8>() : cache == 4 ? solve_batch_occupancy<4>()
+                                                                        : solve_batch_occupancy<0>();
+  const int k = (ctas_per_sm > 0 && ctas_per_sm < occ) ? ctas_per_sm : occ;
+  return k * sms;
+}
+void launch_level_solve_batch(const SolveBatch &P, int round, int sweeps, int grid, int cache, int tree,
+                              cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = (size_t)(cache == 8 ? 8 : cache == 4 ? 4 : 0) * 8 * 256 * 4;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cache == 8) cudaLaunchKernelEx(&cfg, k_level_solve_batch<8>, P, round, sweeps, tree);
+  else if (cache == 4) cudaLaunchKernelEx(&cfg, k_level_solve_batch<4>, P, round, sweeps, tree);
+  else cudaLaunchKernelEx(&cfg, k_level_solve_batch<0>, P, round, sweeps, tree);
 }
 
 }  // namespace dcg

@@ -61,7 +61,20 @@ def lib():
                                       C.POINTER(C.c_double)]
         L.dcg_launches_per_step.argtypes = [vp, C.POINTER(C.c_int64)]
         L.dcg_set_emission.argtypes = [vp, vp, C.c_int32]
-        for name in ["dcg_sizeof_params", "dcg_sizeof_info", "dcg_sizeof_stats"]:
+        L.dcg_batch_create.argtypes = [C.c_int32, vp, C.POINTER(vp)]
+        for name in ["dcg_batch_destroy", "dcg_batch_reset", "dcg_batch_sync"]:
+            getattr(L, name).argtypes = [vp]
+        L.dcg_batch_step.argtypes = [vp, C.c_int32]
+        L.dcg_batch_member.argtypes = [vp, C.c_int32, C.POINTER(vp)]
+        L.dcg_batch_set_stream.argtypes = [vp, vp]
+        L.dcg_batch_autotune.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(capi.DcgTuning)]
+        L.dcg_batch_get_tuning.argtypes = [vp, C.POINTER(capi.DcgTuning)]
+        L.dcg_batch_set_tuning.argtypes = [vp, C.POINTER(capi.DcgTuning)]
+        L.dcg_batch_get_info.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.dcg_batch_time_solve.argtypes = [vp, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_double)]
+        L.dcg_batch_last_error_string.argtypes = [vp]
+        L.dcg_batch_last_error_string.restype = C.c_char_p
+        for name in ["dcg_sizeof_params", "dcg_sizeof_info", "dcg_sizeof_stats", "dcg_sizeof_tuning"]:
             getattr(L, name).restype = C.c_size_t
             getattr(L, name).argtypes = []
         _lib = L
@@ -317,3 +330,106 @@ class FluidSimulationUniform(Simulation):
 
     def debugStats(self):
         return self.stats().mass
+
+
+class _Member(Simulation):
+    """Borrowed handle of one batch member: field, stats, topology and
+    emission access; the batch steps and owns it."""
+
+    def __init__(self, batch, handle, params):
+        self.L = lib()
+        self.params = params
+        self.h = handle
+        self.mode = capi.MODE_ADAPTIVE
+        self._batch = batch  # keeps the owner alive
+        self.info = capi.DcgInfo()
+        self._chk(self.L.dcg_get_info(self.h, C.byref(self.info)), "get_info")
+
+    def close(self):
+        self.h = None
+
+
+class Batch:
+    """Many independent adaptive simulations stepped together (dcg_batch_*):
+    one launch per field stage over all members, one cooperative launch per
+    cascade round, member adaptations as parallel graph branches."""
+
+    def __init__(self, params_list):
+        self.L = lib()
+        self.params = list(params_list)
+        arr = (capi.DcgParams * len(self.params))(*self.params)
+        h = C.c_void_p()
+        rc = self.L.dcg_batch_create(len(self.params), C.cast(arr, C.c_void_p), C.byref(h))
+        if rc != capi.DCG_OK:
+            raise DcgError(rc, "dcg_batch_create failed")
+        self.h = h
+        self.members = []
+        for i, p in enumerate(self.params):
+            mh = C.c_void_p()
+            self._chk(self.L.dcg_batch_member(self.h, i, C.byref(mh)), "member")
+            self.members.append(_Member(self, mh, p))
+
+    def _chk(self, rc, what):
+        if rc != capi.DCG_OK:
+            msg = self.L.dcg_batch_last_error_string(self.h).decode() if self.h else ""
+            raise DcgError(rc, f"{what}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            for m in self.members:
+                m.close()
+            self.L.dcg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __len__(self):
+        return len(self.members)
+
+    def __getitem__(self, i):
+        return self.members[i]
+
+    def reset(self):
+        self._chk(self.L.dcg_batch_reset(self.h), "reset")
+
+    def step(self, n=1):
+        self._chk(self.L.dcg_batch_step(self.h, n), "step")
+
+    def sync(self):
+        self._chk(self.L.dcg_batch_sync(self.h), "sync")
+
+    def set_stream(self, stream_ptr):
+        self._chk(self.L.dcg_batch_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")
+
+    def autotune(self, spinup_steps=10, reps=3):
+        t = capi.DcgTuning()
+        self._chk(self.L.dcg_batch_autotune(self.h, spinup_steps, reps, C.byref(t)), "autotune")
+        return capi.tuning_to_dict(t)
+
+    def get_tuning(self):
+        t = capi.DcgTuning()
+        self._chk(self.L.dcg_batch_get_tuning(self.h, C.byref(t)), "get_tuning")
+        return t
+
+    def set_tuning(self, t):
+        self._chk(self.L.dcg_batch_set_tuning(self.h, C.byref(t)), "set_tuning")
+
+    def info(self):
+        n, nb, nl = C.c_int32(), C.c_int64(), C.c_int64()
+        self._chk(self.L.dcg_batch_get_info(self.h, C.byref(n), C.byref(nb), C.byref(nl)), "get_info")
+        return {"n": n.value, "device_bytes": nb.value, "launches_per_step": nl.value}
+
+    def time_solve(self, reps=5):
+        ms, b = C.c_float(), C.c_double()
+        self._chk(self.L.dcg_batch_time_solve(self.h, reps, C.byref(ms), C.byref(b)), "time_solve")
+        return ms.value, b.value

@@ -279,10 +279,60 @@ int dcg_time_kernel(dcg_sim *sim, int32_t which, int32_t level, int32_t reps,
 /* Number of kernel launches one dcg_step performs (kernel nodes of the
  * captured step graph; 0 before the first graph capture). */
 int dcg_launches_per_step(dcg_sim *sim, int64_t *n);
+/* ---- batches: many independent adaptive simulations stepped together -----
+ * No reference counterpart: the reference runs one simulation per process
+ * (one global __constant__ parameter set, src/utils/sim_utils.h:5-6). A batch
+ * owns n adaptive simulations with their own parameters, domains, level
+ * counts and budgets; every field stage of a batch step is one launch over
+ * all members (groups of 16 members per launch), each cascade round of the
+ * pressure solve is one cooperative launch over the members' cells, the
+ * members' adaptations run as parallel branches, and the whole step is one
+ * CUDA graph. A member's results equal those of a standalone simulation with
+ * the same parameters, bit for bit. All members must use the same
+ * jacobi_iters. */
+typedef struct dcg_batch dcg_batch;
+typedef struct {
+  int32_t tile[4];           /* blocks of 64 cells per CTA (2, 4 or 8) for advect velocity,
+                                advect scalars, divergence, apply pressure                 */
+  int32_t solve_cache;       /* cells per thread whose stencil the level solve keeps in
+                                shared memory: 0, 4 or 8                                    */
+  int32_t solve_ctas_per_sm; /* CTAs per SM of the cooperative solve (0 = occupancy limit) */
+  int32_t solve_barrier;     /* grid barrier between sweeps: 0 flat, 1 two-level            */
+  int32_t reserved[5];
+  float solve_ms;            /* autotune: measured time of the whole cascade (all rounds)  */
+  float cells_ms[4];         /* autotune: measured time of each cell stage at its tile     */
+} dcg_tuning;
+
+int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out);
+int dcg_batch_destroy(dcg_batch *batch);
+int dcg_batch_reset(dcg_batch *batch);     /* every member as after creation */
+int dcg_batch_step(dcg_batch *batch, int32_t n);
+int dcg_batch_sync(dcg_batch *batch);      /* stream sync + every member's device error word */
+/* Borrowed handle of member i for field, stats, topology and emission access
+ * (issued on the batch's stream). Stepping, stage calls, set_params,
+ * set_stream, set_mode and destroy are refused on member handles. */
+int dcg_batch_member(dcg_batch *batch, int32_t i, dcg_sim **out);
+int dcg_batch_set_stream(dcg_batch *batch, void *cuda_stream);
+/* Autotuner: resets the batch, runs spinup_steps steps, times every candidate
+ * tile and solve schedule `reps` times with CUDA events, keeps the fastest,
+ * and resets the batch again (the state is that of dcg_batch_reset after it;
+ * results do not depend on the tuning). */
+int dcg_batch_autotune(dcg_batch *batch, int32_t spinup_steps, int32_t reps, dcg_tuning *out);
+int dcg_batch_get_tuning(const dcg_batch *batch, dcg_tuning *out);
+int dcg_batch_set_tuning(dcg_batch *batch, const dcg_tuning *tuning);
+int dcg_batch_get_info(const dcg_batch *batch, int32_t *n, int64_t *device_bytes, int64_t *launches_per_step);
+/* Times the pressure cascade of the current state (all rounds, the members'
+ * jacobi_iters sweeps each) `reps` times; *bytes = algorithmic bytes of one
+ * cascade, 12 per cell-sweep (p read, div read, p~ write). Leaves p and p~ in
+ * an unspecified state until the next step's projection. */
+int dcg_batch_time_solve(dcg_batch *batch, int32_t reps, float *avg_ms, double *bytes);
+const char *dcg_batch_last_error_string(const dcg_batch *batch);
+
 /* sizeof of the ABI structs, for binding checks. */
 size_t dcg_sizeof_params(void);
 size_t dcg_sizeof_info(void);
 size_t dcg_sizeof_stats(void);
+size_t dcg_sizeof_tuning(void);
 
 #ifdef __cplusplus
 }

@@ -1,6 +1,8 @@
 """Scenario builders shared by the tests: small, seconds-scale versions of the
 reference's default scene and of the benchmark configurations, with the same
 physics switches."""
+import random
+
 from dcgrid_gb300 import capi
 
 
@@ -83,3 +85,32 @@ def sphere_obstacle(gx=32, gy=64, gz=32, blocks=600):
     p.solids = capi.SOLIDS_SPHERE
     p.sphere_radius_world = 2000.0
     return p
+
+
+def plume_batch(n=16, seed=0, sizes=(64, 96, 128, 192, 256), iters=100, precision=capi.PRECISION_FP32,
+                levels=(2, 3)):
+    """Independent plumes with uneven domains: edge drawn from `sizes`, 2 or 3
+    levels, a sphere source in the bottom quarter of radius U[4,10] (capped to
+    the domain) and temperature U[5,15], field-driven refinement. Budget: the
+    coarsest level in full plus a quarter of the finest level's blocks."""
+    rng = random.Random(seed)
+    out = []
+    for _ in range(n):
+        d = rng.choice(sizes)
+        lv = rng.choice(levels)
+        full = [(d >> (l + 2)) ** 3 for l in range(lv)]
+        p = plume(d, d, d, full[-1] + full[0] // 4, lv, iters)
+        r = min(rng.uniform(4.0, 10.0), d / 8.0)
+        p.src_radius = r
+        p.src_center[0] = rng.uniform(r, d - r)
+        p.src_center[1] = rng.uniform(r, max(r, d / 4.0))
+        p.src_center[2] = rng.uniform(r, d - r)
+        p.src_temperature = rng.uniform(5.0, 15.0)
+        p.refine_criterion = capi.REFINE_FIELDS
+        p.refine_threshold = 1.0
+        p.vort_threshold = 0.5
+        p.grad_threshold = 0.05
+        p.ref_compat = 0
+        p.precision = precision
+        out.append(p)
+    return out

@@ -1,0 +1,142 @@
+"""Batched simulations (dcg_batch_*): many independent adaptive simulations per
+launch must give every member exactly the results of a standalone simulation
+with the same parameters, whatever the tuning, group split or precision."""
+import numpy as np
+import pytest
+
+from dcgrid_gb300 import capi
+from tests import scenarios
+from tests.test_parity_gpu import compare, orc
+
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("cuda_ok", "dcg_lib")]
+
+
+def small_batch(n=5, seed=3, precision=capi.PRECISION_FP32, iters=20):
+    return scenarios.plume_batch(n, seed, sizes=(16, 32, 48, 64), iters=iters, precision=precision)
+
+
+def standalone(p, steps):
+    from dcgrid_gb300 import Simulation
+    s = Simulation(p)
+    s.add_velocity_noise(11, 0.05)
+    s.step(steps)
+    s.sync()
+    return s
+
+
+def batch_run(params, steps, tuning=None):
+    from dcgrid_gb300 import Batch
+    b = Batch(params)
+    if tuning is not None:
+        b.set_tuning(tuning)
+    for m in b:
+        m.add_velocity_noise(11, 0.05)
+    b.step(steps)
+    b.sync()
+    return b
+
+
+@pytest.mark.parametrize("prec", [capi.PRECISION_FP32, capi.PRECISION_MIXED_FP16, capi.PRECISION_MIXED],
+                         ids=["fp32", "fp16", "bf16"])
+def test_batch_members_equal_standalone(prec):
+    params = small_batch(5, 3, prec)
+    assert len({(p.gx, p.levels) for p in params}) > 1  # uneven members
+    b = batch_run(params, 6)
+    for i, p in enumerate(params):
+        compare(b[i], standalone(p, 6), p, f"member {i}")
+
+
+def test_batch_mixed_precisions_and_levels_in_one_batch():
+    params = small_batch(4, 5)
+    params[1].precision = capi.PRECISION_MIXED_FP16
+    params[2].precision = capi.PRECISION_MIXED
+    params[3].levels = 3 if params[3].levels == 2 else 2
+    b = batch_run(params, 4)
+    for i, p in enumerate(params):
+        compare(b[i], standalone(p, 4), p, f"member {i}")
+
+
+def test_batch_member_equals_oracle():
+    params = small_batch(3, 8)
+    b = batch_run(params, 3)
+    for i, p in enumerate(params):
+        o = orc(p)
+        o.add_velocity_noise(11, 0.05)
+        o.step(3)
+        compare(b[i], o, p, f"member {i} vs oracle")
+
+
+def tuning(tile, cache, ctas, barrier):
+    t = capi.DcgTuning()
+    for k in range(4):
+        t.tile[k] = tile
+    t.solve_cache, t.solve_ctas_per_sm, t.solve_barrier = cache, ctas, barrier
+    return t
+
+
+def test_results_do_not_depend_on_tuning():
+    params = small_batch(5, 13)
+    ref = batch_run(params, 5, tuning(4, 4, 0, 1))
+    for t in [tuning(2, 0, 1, 0), tuning(8, 8, 2, 1), tuning(2, 8, 1, 0), tuning(8, 0, 0, 1)]:
+        b = batch_run(params, 5, t)
+        for i, p in enumerate(params):
+            compare(b[i], ref[i], p, f"tiles {list(t.tile)} cache {t.solve_cache} member {i}")
+
+
+def test_groups_beyond_sixteen_members():
+    params = scenarios.plume_batch(18, 21, sizes=(16, 32), iters=10)
+    b = batch_run(params, 3)
+    for i in [0, 7, 15, 16, 17]:
+        compare(b[i], standalone(params[i], 3), params[i], f"member {i}")
+
+
+def test_autotune_resets_and_keeps_results():
+    from dcgrid_gb300 import Batch
+    params = small_batch(4, 17)
+    b = Batch(params)
+    t = b.autotune(spinup_steps=3, reps=2)
+    assert all(x in (2, 4, 8) for x in t["tile"])
+    assert t["solve_cache"] in (0, 4, 8) and t["solve_barrier"] in (0, 1)
+    assert t["solve_ms"] > 0
+    fresh = Batch(params)
+    for i, p in enumerate(params):
+        compare(b[i], fresh[i], p, f"after autotune member {i}")
+    for s in (b, fresh):
+        for m in s:
+            m.add_velocity_noise(11, 0.05)
+        s.step(4)
+        s.sync()
+    for i, p in enumerate(params):
+        compare(b[i], fresh[i], p, f"tuned vs default member {i}")
+    info = b.info()
+    assert info["n"] == 4 and info["launches_per_step"] > 0
+
+
+def test_member_handles_are_borrowed():
+    from dcgrid_gb300 import Batch, DcgError
+    b = Batch(small_batch(2, 1))
+    with pytest.raises(DcgError) as e:
+        b[0].step(1)
+    assert e.value.code == capi.DCG_E_INVALID
+    with pytest.raises(DcgError):
+        b[1].reset()
+    assert b.L.dcg_destroy(b[0].h) == capi.DCG_E_INVALID
+    b.step(1)
+    b.sync()
+    assert np.isfinite(b[0].get_field("density")).all()
+
+
+def test_batch_rejects_mixed_sweep_counts():
+    from dcgrid_gb300 import Batch, DcgError
+    params = small_batch(2, 1)
+    params[1].jacobi_iters = params[0].jacobi_iters + 2
+    with pytest.raises(DcgError) as e:
+        Batch(params)
+    assert e.value.code == capi.DCG_E_INVALID
+
+
+def test_time_solve_reports_bytes():
+    params = small_batch(3, 2)
+    b = batch_run(params, 2)
+    ms, nbytes = b.time_solve(3)
+    assert ms > 0 and nbytes > 0

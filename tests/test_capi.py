@@ -33,6 +33,8 @@ def test_struct_layouts(dcg_lib):
     assert dcg_lib.dcg_sizeof_params() == C.sizeof(capi.DcgParams)
     assert dcg_lib.dcg_sizeof_info() == C.sizeof(capi.DcgInfo)
     assert dcg_lib.dcg_sizeof_stats() == C.sizeof(capi.DcgStats)
+    dcg_lib.dcg_sizeof_tuning.restype = C.c_size_t
+    assert dcg_lib.dcg_sizeof_tuning() == C.sizeof(capi.DcgTuning)
 
 
 def test_python_defaults_match_c_defaults(dcg_lib):
@@ -46,6 +48,9 @@ def test_null_handles_are_rejected(dcg_lib):
     assert dcg_lib.dcg_step(None, 1) == capi.DCG_E_INVALID
     assert dcg_lib.dcg_destroy(None) == capi.DCG_E_INVALID
     assert dcg_lib.dcg_create(None, 0, None) == capi.DCG_E_INVALID
+    assert dcg_lib.dcg_batch_step(None, 1) == capi.DCG_E_INVALID
+    assert dcg_lib.dcg_batch_destroy(None) == capi.DCG_E_INVALID
+    assert dcg_lib.dcg_batch_create(0, None, None) == capi.DCG_E_INVALID
 
 
 def test_oracle_exports(oracle_lib):
