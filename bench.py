@@ -1,19 +1,35 @@
 """Benchmark of the adaptive-grid simulation step on GB300.
 
-Metric: active (leaf) cell-steps per second of the 3-level adaptive cloud scene
-(effective 256^3 domain, 40k-block budget, terrain SDF from 5-octave value
-noise, wind inflow of 1 cell/step, temperature/vapor/density, refinement by
-|curl v| > 0.5 or |grad rho| > 0.05), 100 Jacobi sweeps per level.
-Synthetic inputs: seeded terrain, a seeded warm moist source bubble, seeded
-velocity noise; the scene is spun up 60 untimed steps before warm-up so the
-refined topology is developed.
+Metric: active (leaf) cell-steps per second.
+
+Workloads (--workload):
+  batch (default) — 16 independent smoke plumes stepped as one batch: domain
+    edges drawn (seed 0) from {64, 96, 128, 192, 256}, 2 or 3 levels, uneven
+    block budgets, a sphere source in the bottom quarter of radius U[4,10] and
+    temperature U[5,15], buoyancy, field-driven refinement, 100 Jacobi sweeps
+    per level, and a seeded 16^3 emission map per member that the host uploads
+    every step. The timed path is the mixed-precision batch (FP16 scalar
+    storage, FP32 compute) with autotuned tiles and solve schedule, the whole
+    step one CUDA graph. On the same plumes the line also reports the plain
+    FP32 path (16 standalone simulations stepped one after another, each its
+    own step graph), the FP32 batch, and the density error of FP16 storage
+    against the FP64 oracle.
+  cloud — one 3-level cloud scene at effective 256^3, 40k-block budget,
+    terrain, wind inflow, temperature/vapor/density, field-driven
+    refinement, 100 sweeps per level, FP32.
+
+Synthetic inputs throughout (seeded sources, terrain, noise, emission maps);
+scenes are spun up untimed before warm-up so the refined topology has
+developed.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-Under torchrun with N > 1 every rank runs an independent replica of the scene
-(one simulation does not shard); value sums the ranks' cell-steps over the
+                       [--workload batch|cloud]
+Under torchrun with N > 1 every rank runs an independent replica of the
+workload (no data exchange); value sums the ranks' cell-steps over the
 slowest rank's time.
 """
 import argparse
+import ctypes as C
 import json
 import os
 import subprocess
@@ -23,66 +39,23 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-G = 256
-BLOCKS = 40000
-LEVELS = 3
 ITERS = 100
-SPINUP = 60
+CLOUD_SPINUP = 60
+BATCH_N = 16
+BATCH_SPINUP = 30
 EM_N = 16
+METRIC = "active cell-steps/s"
 
 
-def workload_params(precision="fp32"):
-    from dcgrid_gb300 import capi
-    p = capi.default_params(G, G, G, BLOCKS)
-    p.levels = LEVELS
-    p.dx = 1.0
-    p.dt = 1.0
-    p.inlet_enabled = 0
-    p.jacobi_iters = ITERS
-    p.n_scalars = 3
-    p.buoy_alpha = 0.1
-    p.buoy_beta = 0.3
-    p.t_ambient = 0.0
-    p.solids = capi.SOLIDS_TERRAIN
-    p.terrain_amplitude = 40.0
-    p.terrain_base_height = 8.0
-    p.terrain_frequency = 1.0 / 64.0
-    p.terrain_persistence = 0.5
-    p.terrain_octaves = 5
-    p.terrain_seed = 7
-    p.wind_enabled = 1
-    p.wind[0] = 1.0
-    p.refine_criterion = capi.REFINE_FIELDS
-    p.refine_threshold = 1.0
-    p.vort_threshold = 0.5
-    p.grad_threshold = 0.05
-    p.ref_compat = 0
-    p.src_enabled = 1
-    p.src_center[0] = 0.3 * G
-    p.src_center[1] = 0.25 * G
-    p.src_center[2] = 0.5 * G
-    p.src_radius = 16.0
-    p.src_density = 1.0
-    p.src_temperature = 5.0
-    p.src_vapor = 0.5
-    p.precision = capi.PRECISION_FP32 if precision == "fp32" else capi.PRECISION_MIXED
-    p.emission_n = EM_N
-    p.emission_band = 16.0
-    return p
+def batch_params(precision):
+    from dcgrid_gb300 import scenes
+    return scenes.plume_batch(BATCH_N, 0, sizes=(64, 96, 128, 192, 256), iters=ITERS, precision=precision,
+                              em_n=EM_N)
 
 
-def emission_field(seed=1):
-    """Seeded ground emission (density per time unit), EM_N^3 values in [0, 0.05)."""
-    import numpy as np
-    return (0.05 * np.random.default_rng(seed).random(EM_N ** 3)).astype(np.float32)
-
-
-CONFIG = {"workload": f"adaptive cloud scene, effective {G}^3, {LEVELS} levels, {BLOCKS} block budget, "
-                      f"{ITERS} Jacobi sweeps/level",
-          "domain": [G, G, G], "levels": LEVELS, "max_blocks": BLOCKS, "jacobi_iters": ITERS,
-          "block_edge": 4, "spinup_steps": SPINUP, "n_scalars": 3,
-          "emission": f"{16}^3 field over the bottom 16 cell layers",
-          "l2": "flushed between timed steps (256 MiB write)"}
+def member_emission(i):
+    from dcgrid_gb300 import scenes
+    return scenes.emission_field(EM_N, 100 + i)
 
 
 def peaks():
@@ -94,10 +67,10 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def traffic_per_launch():
-    """dram bytes of one Jacobi launch from the committed ncu summary, if any."""
+def committed_traffic(name):
+    """dram bytes per launch of a kernel from a committed ncu summary, if any."""
     try:
-        with open(os.path.join(ROOT, "profiles", "jacobi_traffic.json")) as f:
+        with open(os.path.join(ROOT, "profiles", name)) as f:
             return json.load(f)
     except Exception:
         return None
@@ -150,69 +123,391 @@ class Clocks:
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(gpu_sim=None, steps=1):
-    """The FP64 oracle on the host cores: `steps` steps of the same workload,
-    started from the GPU's spun-up state when given (topology and fields)."""
+class Ctx:
+    """Process / rank context: torch device, stream, optional process group."""
+
+    def __init__(self):
+        import torch
+        self.torch = torch
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(self.local)
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+            self.dist = dist
+        from dcgrid_gb300 import build
+        build.build()
+        self.stream = torch.cuda.Stream()
+        self.flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        d = os.path.join(ROOT, "gpurun_out")
+        self.clock_path = os.path.join(d, f"clocks_r{self.rank}.csv") if os.path.isdir(d) \
+            else f"/tmp/dcg_clocks_r{self.rank}.csv"
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+        self.torch.cuda.synchronize()
+
+    def max_sum(self, ms, cells):
+        """max of the time and sum of the cells over the ranks"""
+        if not self.dist:
+            return ms, cells
+        t = self.torch.tensor([ms, float(cells)], dtype=self.torch.float64, device="cuda")
+        a = t.clone()
+        self.dist.all_reduce(a[:1], op=self.dist.ReduceOp.MAX)
+        self.dist.all_reduce(a[1:], op=self.dist.ReduceOp.SUM)
+        return float(a[0].item()), float(a[1].item())
+
+    def timed(self, steps, step_fn, cells_fn, nvtx="timed"):
+        """device time of `steps` calls of step_fn (CUDA events on the sims'
+        stream, L2 flushed before each step) and the active cells they covered"""
+        torch = self.torch
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        cells = 0
+        self.barrier()
+        torch.cuda.nvtx.range_push(nvtx)  # lets ncu select the timed launches (--nvtx-include)
+        for k in range(steps):
+            with torch.cuda.stream(self.stream):
+                self.flush.fill_(float(k))
+            ev[k][0].record(self.stream)
+            step_fn()
+            ev[k][1].record(self.stream)
+            cells += cells_fn()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        return sum(a.elapsed_time(b) for a, b in ev), cells
+
+    def close(self):
+        if self.dist:
+            self.dist.barrier()
+            self.dist.destroy_process_group()
+
+
+def oracle_from_gpu(sim, p):
+    """An FP64 oracle simulation holding the GPU simulation's topology and fields."""
     from oracle import pyoracle
-    from dcgrid_gb300 import capi
+    o = pyoracle.OracleSim(p, precision="double")
+    if p.emission_n > 0:
+        o.set_emission(sim._em)
+    o.set_topology(sim.get_topology())
+    names = ["density", "vel_x", "vel_y", "vel_z", "fluidity"]
+    if p.n_scalars == 3:
+        names += ["temperature", "vapor"]
+    for f in names:
+        o.set_field(f, sim.get_field(f).astype("float64"))
+    return o
+
+
+def cpu_sample(sims, params, steps=1):
+    """The FP64 oracle on the host cores, started from the GPU states: `steps`
+    steps of every simulation, active cell-steps per second."""
+    from oracle import pyoracle
     threads = os.cpu_count() or 1
     pyoracle.set_threads(threads)
-    p = workload_params()
-    o = pyoracle.OracleSim(p, precision="double")
-    o.set_emission(emission_field())
-    if gpu_sim is not None:
-        topo = gpu_sim.get_topology()
-        o.set_topology(topo)
-        names = ["density", "temperature", "vapor", "vel_x", "vel_y", "vel_z", "fluidity"]
-        for f in names:
-            o.set_field(f, gpu_sim.get_field(f).astype("float64"))
-    else:
-        o.add_velocity_noise(0, 0.01)
-        o.step(SPINUP)
+    orcs = [oracle_from_gpu(s, p) for s, p in zip(sims, params)]
     cells = 0
     t0 = time.perf_counter()
-    for _ in range(steps):
-        o.step(1)
-        cells += o.stats().active_cells
+    for o in orcs:
+        for _ in range(steps):
+            o.step(1)
+            cells += o.stats().active_cells
     dt = time.perf_counter() - t0
-    return {"value": cells / dt, "unit": "active cell-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} step(s) of the same workload from the spun-up state, FP64 oracle, "
-                      f"{threads} OpenMP threads"}, o
+    return {"value": cells / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{steps} step(s) of each of the {len(sims)} simulation(s) from the GPU's spun-up state "
+                      f"(same topology and fields), FP64 oracle, {threads} OpenMP threads"}
 
 
+def density_error_fp16(params, steps=10):
+    """Relative L2 density error of FP16 scalar storage against the FP64
+    oracle after `steps` steps of the smallest plume (both driven with the
+    GPU's adaptation decisions so they share one topology)."""
+    from dcgrid_gb300 import Simulation, capi
+    from oracle import pyoracle
+    import numpy as np
+    i = min(range(len(params)), key=lambda k: params[k].max_blocks)
+    p = params[i]
+    q = capi.params_from_dict(capi.params_to_dict(p))
+    q.precision = capi.PRECISION_MIXED_FP16
+    g = Simulation(q)
+    o = pyoracle.OracleSim(p, precision="double")
+    em = member_emission(i)
+    g.set_emission(em)
+    o.set_emission(em)
+    for s in (g, o):
+        s.add_velocity_noise(0, 0.01)
+    for _ in range(steps):
+        g.advect_velocity()
+        o.advect_velocity()
+        g.adapt()
+        mv, rf = g.get_last_adapt()
+        o.adapt_replay(mv, rf)
+        g.project()
+        o.project()
+        g.advect_scalars()
+        o.advect_scalars()
+    g.sync()
+    alloc = np.repeat(o.get_topology()["pos"][:, 3] >= 0, 64)
+    out = {"member": i, "domain": p.gx, "levels": p.levels, "steps": steps}
+    for f in ["density", "temperature", "vel_y", "pressure"]:
+        a = g.get_field(f)[alloc].astype(np.float64)
+        b = o.get_field(f)[alloc]
+        out[f] = float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+    g.close()
+    return out
+
+
+# ------------------------------------------------------------------ batch
+def run_batch(args, ctx):
+    import numpy as np
+    from dcgrid_gb300 import Batch, Simulation, capi
+    torch = ctx.torch
+    ems = [member_emission(i) for i in range(BATCH_N)]
+
+    def make_batch(prec):
+        b = Batch(batch_params(prec))
+        b.set_stream(ctx.stream.cuda_stream)
+        tune = b.autotune(spinup_steps=5, reps=3)  # leaves the batch reset
+        for i, m in enumerate(b):
+            m.set_emission(ems[i])
+            m._em = ems[i]
+            m.add_velocity_noise(0, 0.01)
+        b.step(BATCH_SPINUP + max(args.warmup, 3))
+        b.sync()
+        return b, tune
+
+    def batch_cells(b):
+        return sum(m.stats().active_cells for m in b)
+
+    # mixed-precision batch: the headline
+    bm, tune_m = make_batch(capi.PRECISION_MIXED_FP16)
+    clocks = Clocks(ctx.clock_path)
+    clocks.start()
+    ms, cells = ctx.timed(args.steps, lambda: bm.step(1), lambda: batch_cells(bm))
+    clk = clocks.stop(ctx.local)
+    ms, cells = ctx.max_sum(ms, cells)
+    value = cells / (ms * 1e-3)
+    info = bm.info()
+
+    # FP32 batch (batching alone)
+    bf, tune_f = make_batch(capi.PRECISION_FP32)
+    ms_f, cells_f = ctx.timed(args.steps, lambda: bf.step(1), lambda: batch_cells(bf), "timed_fp32_batch")
+    ms_f, cells_f = ctx.max_sum(ms_f, cells_f)
+    batched_fp32 = cells_f / (ms_f * 1e-3)
+    bf.close()
+
+    # plain FP32 path: 16 standalone simulations, one after another on one stream
+    plain = []
+    for i, p in enumerate(batch_params(capi.PRECISION_FP32)):
+        s = Simulation(p)
+        s.set_stream(ctx.stream.cuda_stream)
+        s.set_emission(ems[i])
+        s.add_velocity_noise(0, 0.01)
+        s.step(BATCH_SPINUP + max(args.warmup, 3))
+        plain.append(s)
+    for s in plain:
+        s.sync()
+
+    def plain_step():
+        for s in plain:
+            s.step(1)
+
+    ms_p, cells_p = ctx.timed(args.steps, plain_step, lambda: sum(s.stats().active_cells for s in plain),
+                              "timed_plain_fp32")
+    ms_p, cells_p = ctx.max_sum(ms_p, cells_p)
+    plain_fp32 = cells_p / (ms_p * 1e-3)
+    plain_launches = sum(s.launches_per_step() for s in plain)
+    for s in plain:
+        s.close()
+
+    # end to end through the public API: per step the host uploads every
+    # member's emission map (pinned host -> device), steps the batch, and reads
+    # every member's statistics (mass, residual, active cells) back
+    host_em = [torch.from_numpy(e).pin_memory() for e in ems]
+    ctx.barrier()
+    t0 = time.perf_counter()
+    e2e_cells = 0
+    for k in range(args.steps):
+        for i, m in enumerate(bm):
+            m.set_emission(host_em[i])
+        bm.step(1)
+        e2e_cells += batch_cells(bm)
+    torch.cuda.synchronize()
+    e2e_ms, e2e_cells = ctx.max_sum((time.perf_counter() - t0) * 1e3, e2e_cells)
+    stats_bytes = C.sizeof(capi.DcgStats)
+    e2e = {"value": e2e_cells / (e2e_ms * 1e-3), "unit": METRIC,
+           "h2d_bytes_per_step": 4 * EM_N ** 3 * BATCH_N, "d2h_bytes_per_step": stats_bytes * BATCH_N,
+           "note": "per step: dcg_set_emission of each member from pinned host memory, dcg_batch_step, "
+                   "dcg_get_stats of each member; host clock"}
+
+    # roofline of the dominant kernel: the batched cooperative cascade
+    peak, peak_kind = peaks()
+    solve_ms, solve_bytes = bm.time_solve(5)
+    achieved = solve_bytes / (solve_ms * 1e-3) / 1e9
+    tr = committed_traffic("level_solve_batch_traffic.json")
+    traffic = None
+    if tr and tr.get("bytes_per_cell_sweep"):
+        traffic = tr["bytes_per_cell_sweep"] * solve_bytes / 12.0
+    roofline = {"bound": "hbm", "kernel": f"k_level_solve_batch (whole cascade: every round, {ITERS} sweeps each)",
+                "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_cascade": solve_bytes,
+                "cascade_ms": solve_ms,
+                "note": "algorithmic bytes: 12 per allocated cell per sweep (p read, div read, p~ write); "
+                        "traffic: ncu dram bytes per cell-sweep of a smaller capture scaled to these cells"}
+
+    members = [{"edge": p.gx, "levels": p.levels, "max_blocks": p.max_blocks} for p in batch_params(0)]
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ctx.world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (seeded plume sources, emission maps, velocity noise)",
+            "config": {"workload": f"batch of {BATCH_N} independent plumes, edges from {{64,96,128,192,256}} "
+                                   f"(seed 0), 2-3 levels, {ITERS} Jacobi sweeps/level, FP16 scalar storage / "
+                                   f"FP32 compute, autotuned, one CUDA graph per step",
+                       "members": members, "block_edge": 4, "spinup_steps": BATCH_SPINUP,
+                       "emission": f"{EM_N}^3 map per member over the bottom 16 cell layers",
+                       "tuning": tune_m, "l2": "flushed between timed steps (256 MiB write)",
+                       "parallelism": f"replicas x{ctx.world}" if ctx.world > 1 else "single",
+                       "active_cells_last_step": int(batch_cells(bm))},
+            "comparison": {"plain_fp32_standalone": plain_fp32, "plain_fp32_ms_per_step": ms_p / args.steps,
+                           "plain_fp32_launches_per_step": plain_launches,
+                           "batched_fp32": batched_fp32, "batched_fp32_tuning": tune_f,
+                           "speedup_vs_plain_fp32": value / plain_fp32,
+                           "speedup_batching_fp32": batched_fp32 / plain_fp32},
+            "gpu_launches": int(info["launches_per_step"] * args.steps),
+            "launches_per_step": info["launches_per_step"], "roofline": roofline, "e2e": e2e}
+    if clk:
+        line["clocks"] = clk
+    if ctx.rank == 0 and not args.no_cpu:
+        line["comparison"]["rel_err_fp16_vs_fp64"] = density_error_fp16(batch_params(capi.PRECISION_FP32))
+        line["cpu_baseline"] = cpu_sample(list(bm), batch_params(capi.PRECISION_FP32), 1)
+    bm.close()
+    return line
+
+
+# ------------------------------------------------------------------ cloud
+def run_cloud(args, ctx):
+    from dcgrid_gb300 import Simulation, capi, scenes
+    torch = ctx.torch
+    p = scenes.cloud256()
+    sim = Simulation(p)
+    sim.set_stream(ctx.stream.cuda_stream)
+    em = scenes.emission_field(EM_N, 1)
+    sim._em = em
+    sim.set_emission(em)
+    sim.add_velocity_noise(0, 0.01)
+    sim.step(CLOUD_SPINUP + max(args.warmup, 3))
+    sim.sync()
+    clocks = Clocks(ctx.clock_path)
+    clocks.start()
+    ms, cells = ctx.timed(args.steps, lambda: sim.step(1), lambda: sim.stats().active_cells)
+    clk = clocks.stop(ctx.local)
+    ms, cells = ctx.max_sum(ms, cells)
+    value = cells / (ms * 1e-3)
+    launches = sim.launches_per_step()
+
+    # end to end: per step upload the emission map (pinned host -> device) and
+    # read back the dense density volume (device -> pinned host)
+    g = p.gx
+    host_out = torch.empty(g * g * g, dtype=torch.float32).pin_memory()
+    host_em = torch.from_numpy(em).pin_memory()
+    ctx.barrier()
+    e2e_cells = 0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        sim.set_emission(host_em)
+        sim.step(1)
+        if sim.L.dcg_get_dense(sim.h, capi.FIELD_DENSITY, C.c_void_p(host_out.data_ptr()), capi.HOST):
+            raise RuntimeError("dcg_get_dense failed")
+        e2e_cells += sim.stats().active_cells
+    torch.cuda.synchronize()
+    e2e_ms, e2e_cells = ctx.max_sum((time.perf_counter() - t0) * 1e3, e2e_cells)
+    e2e = {"value": e2e_cells / (e2e_ms * 1e-3), "unit": METRIC,
+           "h2d_bytes_per_step": 4 * EM_N ** 3, "d2h_bytes_per_step": 4 * g * g * g,
+           "note": "per step: dcg_set_emission from pinned host memory, dcg_step, dcg_get_dense into pinned "
+                   "host memory, dcg_get_stats; host clock"}
+
+    peak, peak_kind = peaks()
+    jac_ms, jac_bytes = sim.time_kernel(4, 0, 5)
+    achieved = jac_bytes / (jac_ms * 1e-3) / 1e9
+    tr = committed_traffic("jacobi_traffic.json")
+    roofline = {"bound": "hbm", "kernel": f"k_level_solve (level 0, {ITERS} sweeps per launch)",
+                "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": (tr or {}).get("bytes_per_launch_scaled"),
+                "algorithmic_bytes_per_launch": jac_bytes, "launch_ms": jac_ms,
+                "note": "working set (p, p~, div of the level) is L2-resident across sweeps; frac > 1 "
+                        "would mean L2 reuse beyond the HBM roofline"}
+    st = sim.stats()
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ctx.world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (seeded terrain, source bubble, emission map, velocity noise)",
+            "config": {"workload": f"adaptive cloud scene, effective 256^3, 3 levels, 40000 block budget, "
+                                   f"{ITERS} Jacobi sweeps/level",
+                       "domain": [g, g, g], "levels": 3, "max_blocks": 40000, "jacobi_iters": ITERS,
+                       "block_edge": 4, "spinup_steps": CLOUD_SPINUP, "n_scalars": 3,
+                       "emission": f"{EM_N}^3 map over the bottom 16 cell layers",
+                       "l2": "flushed between timed steps (256 MiB write)",
+                       "parallelism": f"replicas x{ctx.world}" if ctx.world > 1 else "single",
+                       "active_cells_last_step": int(st.active_cells)},
+            "gpu_launches": int(launches * args.steps), "launches_per_step": launches,
+            "roofline": roofline, "e2e": e2e}
+    if clk:
+        line["clocks"] = clk
+    if ctx.rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample([sim], [p], 2)
+    sim.close()
+    return line
+
+
+# ------------------------------------------------------------------ reference arm
 def run_reference(args):
-    """--impl reference: the reference's own arithmetic on the host cores (the
-    reference has no CPU implementation and its GPU kernels are not the CPU arm;
-    the oracle port is timed), each step one oracle step of the same workload."""
+    """--impl reference: the reference's arithmetic on the host cores. The
+    reference has no CPU implementation, so its FP64 restatement (the oracle
+    port) is timed; each step is one oracle step of every simulation of the
+    workload, after a shorter spin-up than the GPU arm's."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     from oracle import pyoracle
+    from dcgrid_gb300 import capi, scenes
     threads = os.cpu_count() or 1
     pyoracle.set_threads(threads)
-    p = workload_params()
-    o = pyoracle.OracleSim(p, precision="double")
-    o.set_emission(emission_field())
-    o.add_velocity_noise(0, 0.01)
-    o.step(SPINUP)
-    for _ in range(args.warmup):
-        o.step(1)
+    if args.workload == "batch":
+        params = batch_params(capi.PRECISION_FP32)
+        ems = [member_emission(i) for i in range(BATCH_N)]
+        spin = 5
+        workload = f"batch of {BATCH_N} independent plumes (same members as the GPU arm), FP64"
+    else:
+        params = [scenes.cloud256()]
+        ems = [scenes.emission_field(EM_N, 1)]
+        spin = 10
+        workload = "adaptive cloud scene, effective 256^3, 3 levels, 40000 block budget, FP64"
+    orcs = []
+    for p, e in zip(params, ems):
+        o = pyoracle.OracleSim(p, precision="double")
+        o.set_emission(e)
+        o.add_velocity_noise(0, 0.01)
+        o.step(spin + args.warmup)
+        orcs.append(o)
     cells = 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        o.step(1)
-        cells += o.stats().active_cells
+        for o in orcs:
+            o.step(1)
+            cells += o.stats().active_cells
     dt = time.perf_counter() - t0
     val = cells / dt
-    line = {"metric": "active cell-steps/s", "value": val, "unit": "active cell-steps/s", "n_gpus": args.gpus,
+    line = {"metric": METRIC, "value": val, "unit": METRIC, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "impl": "reference", "config": CONFIG,
-            "cpu_baseline": {"value": val, "unit": "active cell-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} oracle steps after {SPINUP} spin-up and {args.warmup} "
-                                       f"warm-up steps, {threads} OpenMP threads"},
-            "e2e": {"value": val, "unit": "active cell-steps/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": workload, "spinup_steps": spin},
+            "cpu_baseline": {"value": val, "unit": METRIC, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} oracle steps of every simulation after {spin} spin-up and "
+                                       f"{args.warmup} warm-up steps, {threads} OpenMP threads"},
+            "e2e": {"value": val, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -223,135 +518,16 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--workload", default="batch", choices=["batch", "cloud"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and FP64 error legs")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
-
-    import numpy as np
-    import torch
-
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-
-    from dcgrid_gb300 import Simulation, build
-    build.build()
-    stream = torch.cuda.Stream()
-    p = workload_params()
-    sim = Simulation(p)
-    sim.set_stream(stream.cuda_stream)
-    em = emission_field()
-    sim.set_emission(em)
-    sim.add_velocity_noise(0, 0.01)
-    sim.step(SPINUP)
-    for _ in range(max(args.warmup, 3)):
-        sim.step(1)
-    sim.sync()
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-
-    # ---- device-resident timed region
-    clocks = Clocks(os.path.join(ROOT, "gpurun_out", f"clocks_r{rank}.csv")
-                    if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else f"/tmp/dcg_clocks_r{rank}.csv")
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    cells = 0
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(float(k))
-        ev[k][0].record(stream)
-        sim.step(1)
-        ev[k][1].record(stream)
-        cells += sim.stats().active_cells
-    torch.cuda.synchronize()
-    clk = clocks.stop(local)
-    ms = sum(a.elapsed_time(b) for a, b in ev)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        c = torch.tensor([float(cells)], device="cuda")
-        dist.all_reduce(c, op=dist.ReduceOp.SUM)
-        cells = float(c.item())
-    value = cells / (ms * 1e-3)
-    launches = sim.launches_per_step()
-
-    # ---- end to end through the public API: per step the host uploads the
-    # step's emission field (pinned host -> device, dcg_set_emission) and reads
-    # back the dense density volume the step produced (device -> pinned host).
-    n_dense = G * G * G
-    host_out = torch.empty(n_dense, dtype=torch.float32).pin_memory()
-    host_em = torch.from_numpy(em).pin_memory()
-    import ctypes as C
-    from dcgrid_gb300 import capi
-    e2e_ms = 0.0
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e2e_cells = 0
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        sim.set_emission(host_em)
-        sim.step(1)
-        rc = sim.L.dcg_get_dense(sim.h, capi.FIELD_DENSITY, C.c_void_p(host_out.data_ptr()), capi.HOST)
-        if rc:
-            raise RuntimeError("dcg_get_dense failed")
-        e2e_cells += sim.stats().active_cells
-    torch.cuda.synchronize()
-    e2e_ms = (time.perf_counter() - t0) * 1e3
-    if dist:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-        c = torch.tensor([float(e2e_cells)], device="cuda")
-        dist.all_reduce(c, op=dist.ReduceOp.SUM)
-        e2e_cells = float(c.item())
-    e2e = {"value": e2e_cells / (e2e_ms * 1e-3), "unit": "active cell-steps/s",
-           "h2d_bytes_per_step": 4 * EM_N ** 3, "d2h_bytes_per_step": 4 * n_dense,
-           "note": "per step: dcg_set_emission from pinned host memory, dcg_step, dcg_get_dense into pinned "
-                   "host memory, dcg_get_stats; host clock"}
-
-    # ---- roofline of the dominant kernel: the cooperative solve of the finest
-    # level (one launch = all ITERS sweeps; 12 B per allocated cell per sweep)
-    peak, peak_kind = peaks()
-    jac_ms, jac_bytes = sim.time_kernel(4, 0, 5)
-    achieved = jac_bytes / (jac_ms * 1e-3) / 1e9
-    tr = traffic_per_launch()
-    roofline = {"bound": "hbm", "kernel": f"k_level_solve (level 0, {ITERS} sweeps per launch)",
-                "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": (tr or {}).get("bytes_per_launch_scaled"),
-                "algorithmic_bytes_per_launch": jac_bytes, "launch_ms": jac_ms,
-                "note": "working set (p, p~, div of the level) is L2-resident across sweeps; frac > 1 "
-                        "would mean L2 reuse beyond the HBM roofline"}
-
-    st = sim.stats()
-    line = {"metric": "active cell-steps/s", "value": value, "unit": "active cell-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-            "data": "synthetic (seeded terrain, source bubble, velocity noise)",
-            "config": dict(CONFIG, parallelism=f"replicas x{world}" if world > 1 else "single",
-                           active_cells_last_step=int(st.active_cells)),
-            "gpu_launches": int(launches * args.steps), "launches_per_step": launches,
-            "roofline": roofline, "e2e": e2e}
-    if clk:
-        line["clocks"] = clk
-    if rank == 0 and not args.no_cpu:
-        cb, _ = cpu_baseline(sim, steps=2)
-        line["cpu_baseline"] = cb
-    if rank == 0:
+    ctx = Ctx()
+    line = run_batch(args, ctx) if args.workload == "batch" else run_cloud(args, ctx)
+    if ctx.rank == 0:
         print(json.dumps(line), flush=True)
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
-    sim.close()
+    ctx.close()
     return 0
 
 

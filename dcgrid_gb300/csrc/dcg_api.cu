@@ -452,7 +452,10 @@ int dcg_time_kernel(dcg_sim *s, int32_t which, int32_t level, int32_t reps, floa
         break;
       case 1: launch_advect_velocity(s->D, s->stream); break;
       case 2: launch_advect_scalars(s->D, s->stream); break;
-      case 4: launch_level_solve(s->D, level, 0, s->P.jacobi_iters, s->ls_grid, s->ls_epoch, s->stream); break;
+      case 4:
+        if (s->ls_epoch == 3) s->solve_staged(level, 0, s->P.jacobi_iters);
+        else launch_level_solve(s->D, level, 0, s->P.jacobi_iters, s->ls_grid, s->ls_epoch, s->stream);
+        break;
       default: launch_divergence(s->D, s->stream); break;
     }
   };

@@ -7,8 +7,8 @@
 // over all members: the members' device descriptors travel in the kernel
 // parameters, and a CTA picks its member from the cumulative CTA counts.
 // The pressure cascade is one cooperative launch per round over the members'
-// concatenated cells of one level; p and p~ of all members are slices of two
-// batch arenas so the solve addresses them with one base pointer. Member
+// concatenated cells of one level; p, p~ and div of all members are slices of
+// three batch arenas so the solve addresses them with one base pointer. Member
 // adaptations (sorts and selections of one simulation's blocks) run as
 // parallel branches of the captured step graph. Per-member arithmetic is the
 // single simulation's, so results are bit-identical to standalone runs.
@@ -27,7 +27,7 @@ struct dcg_batch {
   std::string err;
   std::vector<void *> allocs;
   size_t bytes = 0;
-  float *p_arena = nullptr, *pt_arena = nullptr;
+  float *p_arena = nullptr, *pt_arena = nullptr, *div_arena = nullptr;
   uint32_t *bar = nullptr, *errw = nullptr;
   std::vector<unsigned long long> arena_off;
   int maxtop = 0, iters = 0;
@@ -132,6 +132,7 @@ struct dcg_batch {
         P.prolong = 1;
         P.p = p_arena;
         P.pt = pt_arena;
+        P.div = div_arena;
         P.bar = bar;
         P.err = errw;
         for (int i = 0; i < P.n; i++) {
@@ -366,6 +367,7 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
   }
   int rc;
   if ((rc = b->alloc(&b->p_arena, cells)) || (rc = b->alloc(&b->pt_arena, cells)) ||
+      (rc = b->alloc(&b->div_arena, cells)) ||
       (rc = b->alloc(&b->bar, 64 + 32 * 18)) || (rc = b->alloc(&b->errw, 4))) {
     delete b;
     return rc;
@@ -383,6 +385,7 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
     s->batch_member = true;
     s->ext_p = b->p_arena + b->arena_off[i];
     s->ext_pt = b->pt_arena + b->arena_off[i];
+    s->ext_div = b->div_arena + b->arena_off[i];
     b->m.push_back(s);
     if ((rc = s->create_adaptive())) {
       b->err = "member " + std::to_string(i) + ": " + s->err;

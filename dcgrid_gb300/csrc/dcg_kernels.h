@@ -59,6 +59,7 @@ struct RestrictBatch {
 struct SolveBatch {
   int n, maxtop, prolong, pad;
   float *p, *pt;
+  const float *div;  // divergence arena (same layout as p)
   uint32_t *bar, *err;
   unsigned long long arena[BMAX];  // first cell of member s in the arenas
   Dev d[BMAX];

@@ -58,10 +58,14 @@ struct dcg_sim {
   bool use_graphs = true;
   long long kernels_per_step = 0;
   int ls_grid = 0;  // CTAs of the cooperative level solve (0 = per-sweep launches)
-  int ls_epoch = 2; // sweep ordering: 0 flat grid barrier, 1 neighbour epochs, 2 two-level barrier
+  // level solve kernel and sweep ordering: 3 = the staged solve shared with
+  // batches (two-level barrier); the per-level kernel with 0 flat grid
+  // barrier, 1 neighbour epochs, 2 two-level barrier
+  int ls_epoch = 3;
+  int ls_grid_staged = 0;  // CTAs of the staged solve
   // batch members: p and p~ are slices of the batch's arenas, and the batch
   // steps the member (its own step and stage entry points are refused)
-  float *ext_p = nullptr, *ext_pt = nullptr;
+  float *ext_p = nullptr, *ext_pt = nullptr, *ext_div = nullptr;
   bool batch_member = false;
 
   int fail(int code, const std::string &msg) {
@@ -237,7 +241,8 @@ struct dcg_sim {
       if ((rc = alloc(&D.p, nc))) return rc;
       if ((rc = alloc(&D.pt, nc))) return rc;
     }
-    if ((rc = alloc(&D.div, nc))) return rc;
+    if (ext_div) D.div = ext_div;
+    else if ((rc = alloc(&D.div, nc))) return rc;
     if ((rc = alloc(&D.ss, 8 * B + 1))) return rc;
     if ((rc = alloc(&D.bs, B))) return rc;
     if ((rc = alloc(&D.moves, 2 * 2 * B))) return rc;
@@ -250,7 +255,10 @@ struct dcg_sim {
     if ((rc = alloc(&D.epoch, B))) return rc;
     ls_grid = level_solve_grid(sms);
     if (const char *m = std::getenv("DCG_SOLVE_SYNC"))
-      ls_epoch = std::strcmp(m, "epoch") == 0 ? 1 : (std::strcmp(m, "barrier") == 0 ? 0 : 2);
+      ls_epoch = std::strcmp(m, "epoch") == 0 ? 1 : std::strcmp(m, "barrier") == 0 ? 0
+                 : std::strcmp(m, "tree") == 0 ? 2 : 3;
+    ls_grid_staged = batch_solve_grid(sms, 4, 0);
+    if (ls_grid_staged <= 0 && ls_epoch == 3) ls_epoch = 2;
     if (P.emission_n > 0) {
       const size_t ne = (size_t)P.emission_n * P.emission_n * P.emission_n;
       if ((rc = alloc(&emis, ne))) return rc;
@@ -349,7 +357,12 @@ struct dcg_sim {
       // one cooperative launch per level: prolongation (not for the coarsest
       // level, nor in projectLocal) and all of the level's sweeps
       const int sweeps = local ? 2 * P.jacobi_iters : P.jacobi_iters;
-      for (int l = top; l >= 0; l--) launch_level_solve(D, l, (!local && l < top) ? 1 : 0, sweeps, ls_grid, ls_epoch, stream);
+      if (ls_epoch == 3) {
+        for (int l = top; l >= 0; l--) solve_staged(l, local ? 0 : 1, sweeps);
+      } else {
+        for (int l = top; l >= 0; l--)
+          launch_level_solve(D, l, (!local && l < top) ? 1 : 0, sweeps, ls_grid, ls_epoch, stream);
+      }
     } else if (local) {
       const int pairs = P.jacobi_iters;
       for (int l = top; l >= 0; l--)
@@ -373,6 +386,22 @@ struct dcg_sim {
     }
     launch_apply_pressure(D, stream);
     restrict_v();
+  }
+  // one level of the cascade through the staged solve, as a batch of one
+  // (prolongation only below the coarsest level)
+  void solve_staged(int level, int prolong, int sweeps) {
+    SolveBatch SB{};
+    SB.n = 1;
+    SB.maxtop = D.g.levels - 1;
+    SB.prolong = prolong;
+    SB.p = D.p;
+    SB.pt = D.pt;
+    SB.div = D.div;
+    SB.bar = D.bar;
+    SB.err = D.err;
+    SB.arena[0] = 0;
+    SB.d[0] = D;
+    launch_level_solve_batch(SB, SB.maxtop - level, sweeps, ls_grid_staged, 4, 1, stream);
   }
   void a_advect_scalars() {
     launch_advect_scalars(D, stream);

@@ -636,6 +636,45 @@ __global__ void __launch_bounds__(256) k_restrict_batch(const __grid_constant__ 
   restrict_subblock(D, P.level, P.fl[s], ((long long)blockIdx.x - (s ? P.end[s - 1] : 0)) * 256 + threadIdx.x);
 }
 
+// Description of one block for the staged sweep, BI_WORDS words: [0] arena
+// index of its first cell, [1] alpha (bits), [2..4] level-local position,
+// [5..10] arena index of the first cell of the block that holds the halo of
+// face f (-x, +x, -y, +y, -z, +z; the block itself when the face is outside),
+// [11..12] one byte per face: levels by which that block is coarser, 16 for
+// outside, 17 for outside under the compat quirk of apron_cell. Lanes 0-5
+// resolve one face each, lane 6 the rest.
+constexpr int BI_WORDS = 13;
+__device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long long *s_end, const int *s_lev,
+                                                long long gb, uint32_t *bi, int lane) {
+  const int m = batch_member(s_end, P.n, gb << 6);
+  const Dev &D = P.d[m];
+  const int lev = s_lev[m];
+  const uint32_t b = (uint32_t)(D.g.off[lev] + (gb - (m ? (s_end[m - 1] >> 6) : 0)));
+  const uint32_t a = (uint32_t)P.arena[m];
+  if (lane < 6) {
+    const int dir = lane == 0 ? 4 : lane == 1 ? 22 : lane == 2 ? 10 : lane == 3 ? 16 : lane == 4 ? 12 : 14;
+    const uint32_t e = D.nbr[27u * b + dir];
+    uint32_t base, code;
+    if (e == OUT) {
+      base = a + b * BV;
+      code = (D.g.ref_compat && lev < D.g.sparse) ? 17u : 16u;
+    } else {
+      base = a + (e & NBR_MASK) * BV;
+      code = e >> 28;
+    }
+    bi[5 + lane] = base;
+    reinterpret_cast<uint8_t *>(bi + 11)[lane] = (uint8_t)code;
+  } else if (lane == 6) {
+    const int4 bp = D.pos[b];
+    bi[0] = a + b * BV;
+    const int sc = 1 << lev;
+    bi[1] = __float_as_uint((float)(sc * sc) * D.ph.dx * D.ph.dx);
+    bi[2] = (uint32_t)bp.x;
+    bi[3] = (uint32_t)bp.y;
+    bi[4] = (uint32_t)bp.z;
+  }
+}
+
 // One round of the batched cascade: level maxtop - round of every member that
 // has it, optional prolongation from the member's parent level, then `sweeps`
 // Jacobi sweeps over the concatenated cells of all members, separated by grid
@@ -644,9 +683,11 @@ __global__ void __launch_bounds__(256) k_restrict_batch(const __grid_constant__ 
 // at most CACHE cells per thread, each thread keeps, per cell, the six
 // neighbour cells and its own cell as arena indices plus alpha*div in dynamic
 // shared memory ([CACHE][8][256] words); a sweep is then six loads and one
-// store per cell. Arithmetic is that of k_jacobi (identical results).
+// store per cell. Larger levels are swept one block per warp through a 6^3
+// shared-memory tile holding the block and its face halo. Arithmetic is that
+// of k_jacobi (identical results).
 template <int CACHE>
-__global__ void __launch_bounds__(256) k_level_solve_batch(const __grid_constant__ SolveBatch P, int round, int sweeps,
+__global__ void __launch_bounds__(256, 5) k_level_solve_batch(const __grid_constant__ SolveBatch P, int round, int sweeps,
                                                            int tree) {
   __shared__ long long s_end[BMAX];
   __shared__ int s_lev[BMAX];
@@ -715,19 +756,91 @@ __global__ void __launch_bounds__(256) k_level_solve_batch(const __grid_constant
       if (it + 1 < sweeps) barrier();
     }
   } else {
+    // staged sweeps, one warp per block: per round each of the CTA's 8 warps
+    // takes one block; its 64 cells and 96 face-halo cells go into a 6^3 tile
+    // in shared memory, then every cell reads its six neighbours from the
+    // tile. The block's description (see fill_block_info) is built once per
+    // launch into the dynamic shared memory when it fits, else per sweep.
+    constexpr int W = 8;
+    __shared__ float s_tile[W][AW * AW * AW];
+    __shared__ uint32_t s_scratch[W][BI_WORDS];
+    const int w = t >> 5, lane = t & 31;
+    int o0, o1;
+    {
+      int x, y, z;
+      local_xyz(lane, x, y, z);
+      o0 = (x + 1) * 36 + (y + 1) * 6 + (z + 1);
+      local_xyz(lane + 32, x, y, z);
+      o1 = (x + 1) * 36 + (y + 1) * 6 + (z + 1);
+    }
+    // halo slots h = lane + 32q: tile position, cell in a same-level
+    // neighbour, clamped own cell, compat-quirk own cell; apron coords + face
+    uint32_t hpk[3], hax[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const int h = lane + 32 * q;
+      const int f = h >> 4, i = 1 + ((h >> 2) & 3), j = 1 + (h & 3);
+      const int side = (f & 1) ? AW - 1 : 0;
+      const int ax = f < 2 ? side : i, ay = f < 2 ? i : (f < 4 ? side : j), az = f < 4 ? j : side;
+      const int same = local_of((ax - 1) & 3, (ay - 1) & 3, (az - 1) & 3);
+      const int self = local_of(clampi(ax, 1, BW) - 1, clampi(ay, 1, BW) - 1, clampi(az, 1, BW) - 1);
+      const int quirk = local_of(clampi(ax, 1, BW) & 3, clampi(ay, 1, BW) & 3, clampi(az, 1, BW) & 3);
+      hpk[q] = (uint32_t)(ax * 36 + ay * 6 + az) | ((uint32_t)same << 8) | ((uint32_t)self << 14) |
+               ((uint32_t)quirk << 20);
+      hax[q] = (uint32_t)ax | ((uint32_t)ay << 4) | ((uint32_t)az << 8) | ((uint32_t)f << 12);
+    }
+    const long long nblocks = total >> 6;
+    const int rounds_b = (int)((nblocks + (long long)W * nctas - 1) / ((long long)W * nctas));
+    const bool cached = rounds_b <= CACHE * 2048 / (W * BI_WORDS);
+    if (cached) {
+      for (int r = 0; r < rounds_b; r++) {
+        const long long gb = ((long long)r * nctas + blockIdx.x) * W + w;
+        if (gb < nblocks) fill_block_info(P, s_end, s_lev, gb, s_cache + (r * W + w) * BI_WORDS, lane);
+      }
+      __syncwarp();
+    }
     for (int it = 0; it < sweeps; it++) {
       const float *src = (it & 1) ? P.pt : P.p;
       float *dst = (it & 1) ? P.p : P.pt;
-      for (long long gi = first; gi < total; gi += stride) {
-        int m;
-        const long long cell = cell_of(gi, m);
-        const Dev &D = P.d[m];
-        const uint32_t a = (uint32_t)P.arena[m];
-        Nb6 n = jacobi_neighbours(D, cell);
-        n.i0 += a; n.i1 += a; n.i2 += a; n.i3 += a; n.i4 += a; n.i5 += a;
-        const int sc = 1 << s_lev[m];
-        const float alpha = (float)(sc * sc) * D.ph.dx * D.ph.dx;
-        dst[a + (uint32_t)cell] = jacobi_update(src, n, alpha * D.div[cell]);
+      for (int r = 0; r < rounds_b; r++) {
+        const long long gb = ((long long)r * nctas + blockIdx.x) * W + w;
+        if (gb >= nblocks) continue;  // warp-uniform
+        const uint32_t *bi = cached ? s_cache + (r * W + w) * BI_WORDS : s_scratch[w];
+        if (!cached) {
+          fill_block_info(P, s_end, s_lev, gb, s_scratch[w], lane);
+          __syncwarp();
+        }
+        const uint32_t own = bi[0];
+        float *T = s_tile[w];
+        T[o0] = __ldcg(src + own + lane);
+        T[o1] = __ldcg(src + own + lane + 32);
+        const uint8_t *codes = reinterpret_cast<const uint8_t *>(bi + 11);
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const uint32_t pk = hpk[q], ga = hax[q];
+          const int f = (int)(ga >> 12);
+          const int code = codes[f];
+          uint32_t li;
+          if (code == 0) {
+            li = (pk >> 8) & 63;
+          } else if (code == 16) {
+            li = (pk >> 14) & 63;
+          } else if (code == 17) {
+            li = (pk >> 20) & 63;
+          } else {  // coarser by `code` levels: injection
+            const int cx = (int)bi[2] + (int)(ga & 15) - 1, cy = (int)bi[3] + (int)((ga >> 4) & 15) - 1,
+                      cz = (int)bi[4] + (int)((ga >> 8) & 15) - 1;
+            li = (uint32_t)local_of((cx >> code) & 3, (cy >> code) & 3, (cz >> code) & 3);
+          }
+          T[pk & 255] = __ldcg(src + bi[5 + f] + li);
+        }
+        __syncwarp();
+        const float alpha = __uint_as_float(bi[1]);
+        const float ad0 = alpha * P.div[own + lane], ad1 = alpha * P.div[own + lane + 32];
+        dst[own + lane] = (T[o0 - 36] + T[o0 + 36] + T[o0 - 6] + T[o0 + 6] + T[o0 - 1] + T[o0 + 1] - ad0) / 6.f;
+        dst[own + lane + 32] =
+            (T[o1 - 36] + T[o1 + 36] + T[o1 - 6] + T[o1 + 6] + T[o1 - 1] + T[o1 + 1] - ad1) / 6.f;
+        __syncwarp();
       }
       if (it + 1 < sweeps) barrier();
     }
