@@ -675,6 +675,19 @@ __device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long 
   }
 }
 
+// Staged-sweep schedule: blocks per warp pass, software pipelining of the
+// next pass's loads, and the minimum resident CTAs per SM the register
+// allocation targets.
+#ifndef DCG_SOLVE_U
+#define DCG_SOLVE_U 2
+#endif
+#ifndef DCG_SOLVE_PIPE
+#define DCG_SOLVE_PIPE 0
+#endif
+#ifndef DCG_SOLVE_MINB
+#define DCG_SOLVE_MINB 4
+#endif
+
 // One round of the batched cascade: level maxtop - round of every member that
 // has it, optional prolongation from the member's parent level, then `sweeps`
 // Jacobi sweeps over the concatenated cells of all members, separated by grid
@@ -687,7 +700,7 @@ __device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long 
 // shared-memory tile holding the block and its face halo. Arithmetic is that
 // of k_jacobi (identical results).
 template <int CACHE>
-__global__ void __launch_bounds__(256, 5) k_level_solve_batch(const __grid_constant__ SolveBatch P, int round, int sweeps,
+__global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const __grid_constant__ SolveBatch P, int round, int sweeps,
                                                            int tree) {
   __shared__ long long s_end[BMAX];
   __shared__ int s_lev[BMAX];
@@ -761,9 +774,9 @@ __global__ void __launch_bounds__(256, 5) k_level_solve_batch(const __grid_const
     // in shared memory, then every cell reads its six neighbours from the
     // tile. The block's description (see fill_block_info) is built once per
     // launch into the dynamic shared memory when it fits, else per sweep.
-    constexpr int W = 8;
-    __shared__ float s_tile[W][AW * AW * AW];
-    __shared__ uint32_t s_scratch[W][BI_WORDS];
+    constexpr int W = 8, U = DCG_SOLVE_U;
+    __shared__ float s_tile[W][U][AW * AW * AW];
+    __shared__ uint32_t s_scratch[W][U][BI_WORDS];
     const int w = t >> 5, lane = t & 31;
     int o0, o1;
     {
@@ -799,48 +812,91 @@ __global__ void __launch_bounds__(256, 5) k_level_solve_batch(const __grid_const
       }
       __syncwarp();
     }
-    for (int it = 0; it < sweeps; it++) {
-      const float *src = (it & 1) ? P.pt : P.p;
-      float *dst = (it & 1) ? P.p : P.pt;
-      for (int r = 0; r < rounds_b; r++) {
+    // Passes of U rounds: every lane issues the loads of U blocks before the
+    // warp computes any of them; with DCG_SOLVE_PIPE the loads of the next
+    // pass are issued before the current pass is computed from its tiles.
+    struct Pass {
+      float v[U][5], dv[U][2], alpha[U];
+      uint32_t own[U];
+      bool act[U];
+    };
+    const float *src = P.p;
+    auto load_pass = [&](int r0, Pass &ps) {
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int r = r0 + u;
         const long long gb = ((long long)r * nctas + blockIdx.x) * W + w;
-        if (gb >= nblocks) continue;  // warp-uniform
-        const uint32_t *bi = cached ? s_cache + (r * W + w) * BI_WORDS : s_scratch[w];
+        ps.act[u] = r < rounds_b && gb < nblocks;  // warp-uniform
+        if (!ps.act[u]) continue;
+        const uint32_t *bi = cached ? s_cache + (r * W + w) * BI_WORDS : s_scratch[w][u];
         if (!cached) {
-          fill_block_info(P, s_end, s_lev, gb, s_scratch[w], lane);
+          fill_block_info(P, s_end, s_lev, gb, s_scratch[w][u], lane);
           __syncwarp();
         }
         const uint32_t own = bi[0];
-        float *T = s_tile[w];
-        T[o0] = __ldcg(src + own + lane);
-        T[o1] = __ldcg(src + own + lane + 32);
-        const uint8_t *codes = reinterpret_cast<const uint8_t *>(bi + 11);
+        uint32_t addr[3];
+        if (bi[11] == 0u && (bi[12] & 0xFFFFu) == 0u) {
+          // all six faces border same-level blocks (warp-uniform fast path)
 #pragma unroll
-        for (int q = 0; q < 3; q++) {
-          const uint32_t pk = hpk[q], ga = hax[q];
-          const int f = (int)(ga >> 12);
-          const int code = codes[f];
-          uint32_t li;
-          if (code == 0) {
-            li = (pk >> 8) & 63;
-          } else if (code == 16) {
-            li = (pk >> 14) & 63;
-          } else if (code == 17) {
-            li = (pk >> 20) & 63;
-          } else {  // coarser by `code` levels: injection
-            const int cx = (int)bi[2] + (int)(ga & 15) - 1, cy = (int)bi[3] + (int)((ga >> 4) & 15) - 1,
-                      cz = (int)bi[4] + (int)((ga >> 8) & 15) - 1;
-            li = (uint32_t)local_of((cx >> code) & 3, (cy >> code) & 3, (cz >> code) & 3);
+          for (int q = 0; q < 3; q++) addr[q] = bi[5 + (hax[q] >> 12)] + ((hpk[q] >> 8) & 63);
+        } else {
+          const uint8_t *codes = reinterpret_cast<const uint8_t *>(bi + 11);
+#pragma unroll
+          for (int q = 0; q < 3; q++) {
+            const uint32_t pk = hpk[q], ga = hax[q];
+            const int f = (int)(ga >> 12);
+            const int code = codes[f];
+            uint32_t li = code == 0 ? (pk >> 8) & 63 : code == 16 ? (pk >> 14) & 63 : (pk >> 20) & 63;
+            if (code > 0 && code < 16) {  // coarser by `code` levels: injection
+              const int cx = (int)bi[2] + (int)(ga & 15) - 1, cy = (int)bi[3] + (int)((ga >> 4) & 15) - 1,
+                        cz = (int)bi[4] + (int)((ga >> 8) & 15) - 1;
+              li = (uint32_t)local_of((cx >> code) & 3, (cy >> code) & 3, (cz >> code) & 3);
+            }
+            addr[q] = bi[5 + f] + li;
           }
-          T[pk & 255] = __ldcg(src + bi[5 + f] + li);
+        }
+        ps.own[u] = own;
+        ps.alpha[u] = __uint_as_float(bi[1]);
+        ps.v[u][0] = __ldcg(src + own + lane);
+        ps.v[u][1] = __ldcg(src + own + lane + 32);
+        ps.v[u][2] = __ldcg(src + addr[0]);
+        ps.v[u][3] = __ldcg(src + addr[1]);
+        ps.v[u][4] = __ldcg(src + addr[2]);
+        ps.dv[u][0] = P.div[own + lane];
+        ps.dv[u][1] = P.div[own + lane + 32];
+      }
+    };
+    for (int it = 0; it < sweeps; it++) {
+      src = (it & 1) ? P.pt : P.p;
+      float *dst = (it & 1) ? P.p : P.pt;
+      Pass cur, nxt;
+      if (DCG_SOLVE_PIPE) load_pass(0, cur);
+      for (int r0 = 0; r0 < rounds_b; r0 += U) {
+        if (!DCG_SOLVE_PIPE) load_pass(r0, cur);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          if (!cur.act[u]) continue;
+          float *T = s_tile[w][u];
+          T[o0] = cur.v[u][0];
+          T[o1] = cur.v[u][1];
+          T[hpk[0] & 255] = cur.v[u][2];
+          T[hpk[1] & 255] = cur.v[u][3];
+          T[hpk[2] & 255] = cur.v[u][4];
         }
         __syncwarp();
-        const float alpha = __uint_as_float(bi[1]);
-        const float ad0 = alpha * P.div[own + lane], ad1 = alpha * P.div[own + lane + 32];
-        dst[own + lane] = (T[o0 - 36] + T[o0 + 36] + T[o0 - 6] + T[o0 + 6] + T[o0 - 1] + T[o0 + 1] - ad0) / 6.f;
-        dst[own + lane + 32] =
-            (T[o1 - 36] + T[o1 + 36] + T[o1 - 6] + T[o1 + 6] + T[o1 - 1] + T[o1 + 1] - ad1) / 6.f;
+        if (DCG_SOLVE_PIPE) load_pass(r0 + U, nxt);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          if (!cur.act[u]) continue;
+          const float *T = s_tile[w][u];
+          const float ad0 = cur.alpha[u] * cur.dv[u][0], ad1 = cur.alpha[u] * cur.dv[u][1];
+          dst[cur.own[u] + lane] =
+              (T[o0 - 36] + T[o0 + 36] + T[o0 - 6] + T[o0 + 6] + T[o0 - 1] + T[o0 + 1] - ad0) / 6.f;
+          dst[cur.own[u] + lane + 32] =
+              (T[o1 - 36] + T[o1 + 36] + T[o1 - 6] + T[o1 + 6] + T[o1 - 1] + T[o1 + 1] - ad1) / 6.f;
+        }
         __syncwarp();
+        if (DCG_SOLVE_PIPE) cur = nxt;
       }
       if (it + 1 < sweeps) barrier();
     }
@@ -879,8 +935,9 @@ void launch_restrict_batch(RestrictBatch &P, cudaStream_t st) {
 
 template <int C>
 static int solve_batch_occupancy() {
+  // static + dynamic shared memory above 48 KB needs the opt-in
   const int smem = C * 8 * 256 * 4;
-  if (smem > 48 * 1024 &&
+  if (smem > 0 &&
       cudaFuncSetAttribute(k_level_solve_batch<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
     return 0;
   int a = 0;
