@@ -74,8 +74,8 @@ struct dcg_batch {
   int groups() const { return (n() + BMAX - 1) / BMAX; }
 
   int set_solve_config() {
-    if (tune.solve_cache != 0 && tune.solve_cache != 4 && tune.solve_cache != 8)
-      return fail(DCG_E_INVALID, "solve_cache must be 0, 4 or 8");
+    if (tune.solve_cache != 0 && tune.solve_cache != 3 && tune.solve_cache != 4 && tune.solve_cache != 8)
+      return fail(DCG_E_INVALID, "solve_cache must be 0, 3, 4 or 8");
     for (int k = 0; k < 4; k++)
       if (tune.tile[k] != 2 && tune.tile[k] != 4 && tune.tile[k] != 8)
         return fail(DCG_E_INVALID, "tiles must be 2, 4 or 8 blocks");
@@ -290,7 +290,7 @@ struct dcg_batch {
     }
     // level solve: cache depth x CTAs per SM x barrier kind
     float best_solve = 1e30f;
-    for (int cache : {0, 4, 8}) {
+    for (int cache : {0, 3, 4, 8}) {
       const int occ = batch_solve_grid(sms, cache, 0) / std::max(1, sms);
       for (int k = 1; k <= occ; k++)
         for (int tree = 0; tree < 2; tree++) {

@@ -687,6 +687,14 @@ __device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long 
 #ifndef DCG_SOLVE_MINB
 #define DCG_SOLVE_MINB 4
 #endif
+// block+halo tile strides: 52 (x) and 8 (y) put the 32 cells of either half
+// of a block, and each of their six neighbour sets, in 32 distinct banks
+#ifndef DCG_TILE_SX
+#define DCG_TILE_SX 52
+#endif
+#ifndef DCG_TILE_SY
+#define DCG_TILE_SY 8
+#endif
 
 // One round of the batched cascade: level maxtop - round of every member that
 // has it, optional prolongation from the member's parent level, then `sweeps`
@@ -774,17 +782,18 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
     // in shared memory, then every cell reads its six neighbours from the
     // tile. The block's description (see fill_block_info) is built once per
     // launch into the dynamic shared memory when it fits, else per sweep.
-    constexpr int W = 8, U = DCG_SOLVE_U;
-    __shared__ float s_tile[W][U][AW * AW * AW];
+    // tile strides SX (x), SY (y), 1 (z)
+    constexpr int W = 8, U = DCG_SOLVE_U, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 6;
+    __shared__ float s_tile[W][U][TILE];
     __shared__ uint32_t s_scratch[W][U][BI_WORDS];
     const int w = t >> 5, lane = t & 31;
     int o0, o1;
     {
       int x, y, z;
       local_xyz(lane, x, y, z);
-      o0 = (x + 1) * 36 + (y + 1) * 6 + (z + 1);
+      o0 = (x + 1) * SX + (y + 1) * SY + (z + 1);
       local_xyz(lane + 32, x, y, z);
-      o1 = (x + 1) * 36 + (y + 1) * 6 + (z + 1);
+      o1 = (x + 1) * SX + (y + 1) * SY + (z + 1);
     }
     // halo slots h = lane + 32q: tile position, cell in a same-level
     // neighbour, clamped own cell, compat-quirk own cell; apron coords + face
@@ -798,8 +807,8 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
       const int same = local_of((ax - 1) & 3, (ay - 1) & 3, (az - 1) & 3);
       const int self = local_of(clampi(ax, 1, BW) - 1, clampi(ay, 1, BW) - 1, clampi(az, 1, BW) - 1);
       const int quirk = local_of(clampi(ax, 1, BW) & 3, clampi(ay, 1, BW) & 3, clampi(az, 1, BW) & 3);
-      hpk[q] = (uint32_t)(ax * 36 + ay * 6 + az) | ((uint32_t)same << 8) | ((uint32_t)self << 14) |
-               ((uint32_t)quirk << 20);
+      hpk[q] = (uint32_t)(ax * SX + ay * SY + az) | ((uint32_t)same << 9) | ((uint32_t)self << 15) |
+               ((uint32_t)quirk << 21);
       hax[q] = (uint32_t)ax | ((uint32_t)ay << 4) | ((uint32_t)az << 8) | ((uint32_t)f << 12);
     }
     const long long nblocks = total >> 6;
@@ -838,7 +847,7 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
         if (bi[11] == 0u && (bi[12] & 0xFFFFu) == 0u) {
           // all six faces border same-level blocks (warp-uniform fast path)
 #pragma unroll
-          for (int q = 0; q < 3; q++) addr[q] = bi[5 + (hax[q] >> 12)] + ((hpk[q] >> 8) & 63);
+          for (int q = 0; q < 3; q++) addr[q] = bi[5 + (hax[q] >> 12)] + ((hpk[q] >> 9) & 63);
         } else {
           const uint8_t *codes = reinterpret_cast<const uint8_t *>(bi + 11);
 #pragma unroll
@@ -846,7 +855,7 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
             const uint32_t pk = hpk[q], ga = hax[q];
             const int f = (int)(ga >> 12);
             const int code = codes[f];
-            uint32_t li = code == 0 ? (pk >> 8) & 63 : code == 16 ? (pk >> 14) & 63 : (pk >> 20) & 63;
+            uint32_t li = code == 0 ? (pk >> 9) & 63 : code == 16 ? (pk >> 15) & 63 : (pk >> 21) & 63;
             if (code > 0 && code < 16) {  // coarser by `code` levels: injection
               const int cx = (int)bi[2] + (int)(ga & 15) - 1, cy = (int)bi[3] + (int)((ga >> 4) & 15) - 1,
                         cz = (int)bi[4] + (int)((ga >> 8) & 15) - 1;
@@ -879,9 +888,9 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
           float *T = s_tile[w][u];
           T[o0] = cur.v[u][0];
           T[o1] = cur.v[u][1];
-          T[hpk[0] & 255] = cur.v[u][2];
-          T[hpk[1] & 255] = cur.v[u][3];
-          T[hpk[2] & 255] = cur.v[u][4];
+          T[hpk[0] & 511] = cur.v[u][2];
+          T[hpk[1] & 511] = cur.v[u][3];
+          T[hpk[2] & 511] = cur.v[u][4];
         }
         __syncwarp();
         if (DCG_SOLVE_PIPE) load_pass(r0 + U, nxt);
@@ -891,9 +900,9 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
           const float *T = s_tile[w][u];
           const float ad0 = cur.alpha[u] * cur.dv[u][0], ad1 = cur.alpha[u] * cur.dv[u][1];
           dst[cur.own[u] + lane] =
-              (T[o0 - 36] + T[o0 + 36] + T[o0 - 6] + T[o0 + 6] + T[o0 - 1] + T[o0 + 1] - ad0) / 6.f;
+              (T[o0 - SX] + T[o0 + SX] + T[o0 - SY] + T[o0 + SY] + T[o0 - 1] + T[o0 + 1] - ad0) / 6.f;
           dst[cur.own[u] + lane + 32] =
-              (T[o1 - 36] + T[o1 + 36] + T[o1 - 6] + T[o1 + 6] + T[o1 - 1] + T[o1 + 1] - ad1) / 6.f;
+              (T[o1 - SX] + T[o1 + SX] + T[o1 - SY] + T[o1 + SY] + T[o1 - 1] + T[o1 + 1] - ad1) / 6.f;
         }
         __syncwarp();
         if (DCG_SOLVE_PIPE) cur = nxt;
@@ -946,7 +955,7 @@ static int solve_batch_occupancy() {
 }
 int batch_solve_grid(int sms, int cache, int ctas_per_sm) {
   const int occ = cache == 8 ? solve_batch_occupancy<8>() : cache == 4 ? solve_batch_occupancy<4>()
-                                                                        : solve_batch_occupancy<0>();
+                  : cache == 3 ? solve_batch_occupancy<3>() : solve_batch_occupancy<0>();
   const int k = (ctas_per_sm > 0 && ctas_per_sm < occ) ? ctas_per_sm : occ;
   return k * sms;
 }
@@ -955,7 +964,8 @@ void launch_level_solve_batch(const SolveBatch &P, int round, int sweeps, int gr
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = (size_t)(cache == 8 ? 8 : cache == 4 ? 4 : 0) * 8 * 256 * 4;
+  if (cache != 8 && cache != 4 && cache != 3) cache = 0;
+  cfg.dynamicSmemBytes = (size_t)cache * 8 * 256 * 4;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -964,6 +974,7 @@ void launch_level_solve_batch(const SolveBatch &P, int round, int sweeps, int gr
   cfg.numAttrs = 1;
   if (cache == 8) cudaLaunchKernelEx(&cfg, k_level_solve_batch<8>, P, round, sweeps, tree);
   else if (cache == 4) cudaLaunchKernelEx(&cfg, k_level_solve_batch<4>, P, round, sweeps, tree);
+  else if (cache == 3) cudaLaunchKernelEx(&cfg, k_level_solve_batch<3>, P, round, sweeps, tree);
   else cudaLaunchKernelEx(&cfg, k_level_solve_batch<0>, P, round, sweeps, tree);
 }
 

@@ -295,7 +295,7 @@ typedef struct {
   int32_t tile[4];           /* blocks of 64 cells per CTA (2, 4 or 8) for advect velocity,
                                 advect scalars, divergence, apply pressure                 */
   int32_t solve_cache;       /* cells per thread whose stencil the level solve keeps in
-                                shared memory: 0, 4 or 8                                    */
+                                shared memory: 0, 3, 4 or 8 (8 KB of shared memory each)    */
   int32_t solve_ctas_per_sm; /* CTAs per SM of the cooperative solve (0 = occupancy limit) */
   int32_t solve_barrier;     /* grid barrier between sweeps: 0 flat, 1 two-level            */
   int32_t reserved[5];
