@@ -431,10 +431,13 @@ def run_cloud(args, ctx):
     peak, peak_kind = peaks()
     jac_ms, jac_bytes = sim.time_kernel(4, 0, 5)
     achieved = jac_bytes / (jac_ms * 1e-3) / 1e9
-    tr = committed_traffic("jacobi_traffic.json")
-    roofline = {"bound": "hbm", "kernel": f"k_level_solve (level 0, {ITERS} sweeps per launch)",
+    tr = committed_traffic("level_solve_cloud256_traffic.json")
+    traffic = None
+    if tr and tr.get("bytes_per_cell_sweep"):
+        traffic = tr["bytes_per_cell_sweep"] * jac_bytes / 12.0
+    roofline = {"bound": "hbm", "kernel": f"k_level_solve_batch (one member, level 0, {ITERS} sweeps per launch)",
                 "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": (tr or {}).get("bytes_per_launch_scaled"),
+                "frac": achieved / peak, "traffic": traffic,
                 "algorithmic_bytes_per_launch": jac_bytes, "launch_ms": jac_ms,
                 "note": "working set (p, p~, div of the level) is L2-resident across sweeps; frac > 1 "
                         "would mean L2 reuse beyond the HBM roofline"}
