@@ -495,6 +495,98 @@ size_t dcg_sizeof_params(void) { return sizeof(dcg_params); }
 size_t dcg_sizeof_info(void) { return sizeof(dcg_info); }
 size_t dcg_sizeof_stats(void) { return sizeof(dcg_stats); }
 
+// ---- state I/O -------------------------------------------------------------
+namespace {
+struct StateHeader {
+  char magic[8];
+  int32_t version, gx, gy, gz, levels, n_scalars, precision, pad;
+  int64_t max_blocks, bytes, reserved;
+};
+static_assert(sizeof(StateHeader) == 64, "state header is 64 bytes");
+const char kStateMagic[8] = {'D', 'C', 'G', 'S', 'T', 'A', 'T', 'E'};
+}  // namespace
+
+int dcg_state_bytes(dcg_sim *s, int64_t *bytes) {
+  if (bad(s) || !bytes || s->mode != DCG_MODE_ADAPTIVE) return DCG_E_INVALID;
+  size_t n = sizeof(StateHeader);
+  for (auto &sec : s->state_sections()) n += sec.second;
+  *bytes = (int64_t)n;
+  return DCG_OK;
+}
+int dcg_save_state(dcg_sim *s, void *dst, int32_t where) {
+  if (bad(s) || !dst || s->mode != DCG_MODE_ADAPTIVE) return DCG_E_INVALID;
+  int64_t total = 0;
+  dcg_state_bytes(s, &total);
+  StateHeader h{};
+  std::memcpy(h.magic, kStateMagic, 8);
+  h.version = 1;
+  h.gx = s->P.gx; h.gy = s->P.gy; h.gz = s->P.gz;
+  h.levels = s->D.g.levels;
+  h.n_scalars = s->P.n_scalars;
+  h.precision = s->P.precision;
+  h.max_blocks = s->D.g.B;
+  h.bytes = total;
+  const cudaMemcpyKind kind = where == DCG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  char *out = static_cast<char *>(dst);
+  int rc;
+  if (where == DCG_DEVICE) {
+    if ((rc = s->cuda(cudaMemcpyAsync(out, &h, sizeof h, cudaMemcpyHostToDevice, s->stream), "save_state")))
+      return rc;
+  } else {
+    std::memcpy(out, &h, sizeof h);
+  }
+  size_t off = sizeof h;
+  for (auto &sec : s->state_sections()) {
+    if ((rc = s->cuda(cudaMemcpyAsync(out + off, sec.first, sec.second, kind, s->stream), "save_state"))) return rc;
+    off += sec.second;
+  }
+  return s->sync("save_state");
+}
+int dcg_load_state(dcg_sim *s, const void *src, int32_t where) {
+  if (bad(s) || !src || s->mode != DCG_MODE_ADAPTIVE) return DCG_E_INVALID;
+  StateHeader h{};
+  const char *in = static_cast<const char *>(src);
+  int rc;
+  if (where == DCG_DEVICE) {
+    if ((rc = s->cuda(cudaMemcpy(&h, in, sizeof h, cudaMemcpyDeviceToHost), "load_state"))) return rc;
+  } else {
+    std::memcpy(&h, in, sizeof h);
+  }
+  int64_t total = 0;
+  dcg_state_bytes(s, &total);
+  if (std::memcmp(h.magic, kStateMagic, 8) != 0 || h.version != 1 || h.gx != s->P.gx || h.gy != s->P.gy ||
+      h.gz != s->P.gz || h.levels != s->D.g.levels || h.n_scalars != s->P.n_scalars ||
+      h.precision != s->P.precision || h.max_blocks != s->D.g.B || h.bytes != total)
+    return s->fail(DCG_E_INVALID, "state does not match this simulation's geometry, budget or formats");
+  const cudaMemcpyKind kind = where == DCG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  size_t off = sizeof h;
+  for (auto &sec : s->state_sections()) {
+    if ((rc = s->cuda(cudaMemcpyAsync(sec.first, in + off, sec.second, kind, s->stream), "load_state"))) return rc;
+    off += sec.second;
+  }
+  cudaMemsetAsync(s->D.ctr, 0, sizeof(long long) * C_COUNT, s->stream);
+  cudaMemsetAsync(s->D.err, 0, 4, s->stream);
+  return s->sync("load_state");
+}
+
+// ---- adjoint of the density path ------------------------------------------
+int dcg_adjoint_step(dcg_sim *s, const float *lam_in, float *lam_out, float *lam_emission) {
+  if (bad(s) || !lam_in || !lam_out || s->mode != DCG_MODE_ADAPTIVE) return DCG_E_INVALID;
+  if (s->D.g.mixed) return s->fail(DCG_E_INVALID, "the adjoint is implemented for FP32 scalar storage");
+  const size_t nc = (size_t)s->D.g.B * BV;
+  int rc;
+  if (!s->adj_tmp && (rc = s->alloc(&s->adj_tmp, nc))) return rc;
+  if ((rc = s->cuda(cudaMemcpyAsync(s->adj_tmp, lam_in, nc * 4, cudaMemcpyDeviceToDevice, s->stream), "adjoint")))
+    return rc;
+  launch_adjoint_step(s->D, s->adj_tmp, lam_out, s->P.emission_n > 0 ? lam_emission : nullptr, s->sms, s->stream);
+  return s->check_launch("adjoint_step");
+}
+int dcg_adjoint_dense(dcg_sim *s, const float *lam_dense, float *lam_cells) {
+  if (bad(s) || !lam_dense || !lam_cells || s->mode != DCG_MODE_ADAPTIVE) return DCG_E_INVALID;
+  launch_adjoint_dense(s->D, lam_dense, lam_cells, s->stream);
+  return s->check_launch("adjoint_dense");
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

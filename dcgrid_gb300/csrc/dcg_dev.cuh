@@ -423,4 +423,90 @@ __device__ inline void tq_st(const Dev &D, int k, size_t i, float v) {
   else D.tq[k][i] = v;
 }
 
+// ---------------------------------------------------------------- sampling
+// Shared by the advection kernels and their adjoint, so both compute the same
+// sample indices and weights.
+struct Smp {
+  unsigned long long idx[8];
+  float wt[8];
+  float wAcc;
+  int x0, y0, z0, x1, y1, z1, scale;
+};
+
+// INIT_SAMPLE (src/dcgrid/dcgrid_fluid.cu:7-72): locate the finest block that
+// holds the back-traced point, then trilinear weights x fluidity, renormalised.
+// The block is found from the advected cell's own block through its neighbour
+// table and child pointers (no hash probes); points more than one block away
+// fall back to a descent from the finest dense level.
+__device__ inline void sample_at(const Dev &D, uint32_t b0, int4 bp0, float pxw, float pyw, float pzw,
+                                 Smp &s) {
+  const int ix = clampi((int)floorf(pxw), 0, D.g.gx - 1);
+  const int iy = clampi((int)floorf(pyw), 0, D.g.gy - 1);
+  const int iz = clampi((int)floorf(pzw), 0, D.g.gz - 1);
+  const int L0 = bp0.w;
+  const int ddx = ((ix >> L0) >> 2) - (bp0.x >> 2);
+  const int ddy = ((iy >> L0) >> 2) - (bp0.y >> 2);
+  const int ddz = ((iz >> L0) >> 2) - (bp0.z >> 2);
+  uint32_t b = NONE;
+  int lev = L0;
+  if (ddx >= -1 && ddx <= 1 && ddy >= -1 && ddy <= 1 && ddz >= -1 && ddz <= 1) {
+    if ((ddx | ddy | ddz) == 0) {
+      b = b0;
+    } else {
+      const uint32_t e = D.nbr[27u * b0 + (ddx + 1) * 9 + (ddy + 1) * 3 + (ddz + 1)];
+      if (e != OUT) {
+        b = e & NBR_MASK;
+        lev = L0 + (int)(e >> 28);
+      }
+    }
+    if (b != NONE && lev == L0) b = descend(D, b, lev, ix, iy, iz);
+  }
+  if (b == NONE) b = locate(D, ix, iy, iz, 0, lev);
+  const int4 bp = (b == b0) ? bp0 : D.pos[b];
+  s.scale = 1 << lev;
+  const float scaleInv = 1.f / (float)s.scale;
+  const float x = pxw * scaleInv - 0.5f, y = pyw * scaleInv - 0.5f, z = pzw * scaleInv - 0.5f;
+  const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+  const float dx = x - xf, dy = y - yf, dz = z - zf;
+  s.x0 = (int)xf; s.y0 = (int)yf; s.z0 = (int)zf;
+  s.x1 = s.x0 + 1; s.y1 = s.y0 + 1; s.z1 = s.z0 + 1;
+  const int i = clampi(s.x1 - bp.x, 0, AW - 2);
+  const int j = clampi(s.y1 - bp.y, 0, AW - 2);
+  const int k = clampi(s.z1 - bp.z, 0, AW - 2);
+#pragma unroll
+  for (int c = 0; c < 8; c++)
+    s.idx[c] = apron_cell(D, b, bp, i + ((c >> 2) & 1), j + ((c >> 1) & 1), k + (c & 1));
+  const float Dx = 1.f - dx, Dy = 1.f - dy, Dz = 1.f - dz;
+  s.wt[0] = D.w[s.idx[0]] * Dx * Dy * Dz;
+  s.wt[1] = D.w[s.idx[1]] * Dx * Dy * dz;
+  s.wt[2] = D.w[s.idx[2]] * Dx * dy * Dz;
+  s.wt[3] = D.w[s.idx[3]] * Dx * dy * dz;
+  s.wt[4] = D.w[s.idx[4]] * dx * Dy * Dz;
+  s.wt[5] = D.w[s.idx[5]] * dx * Dy * dz;
+  s.wt[6] = D.w[s.idx[6]] * dx * dy * Dz;
+  s.wt[7] = D.w[s.idx[7]] * dx * dy * dz;
+  s.wAcc = s.wt[0] + s.wt[1] + s.wt[2] + s.wt[3] + s.wt[4] + s.wt[5] + s.wt[6] + s.wt[7];
+  const float wInv = 1.f / s.wAcc;
+#pragma unroll
+  for (int c = 0; c < 8; c++) s.wt[c] = s.wt[c] * wInv;
+}
+
+__device__ inline void corner_of(const Smp &s, int c, int &x, int &y, int &z) {
+  x = (c & 4) ? s.x1 : s.x0;
+  y = (c & 2) ? s.y1 : s.y0;
+  z = (c & 1) ? s.z1 : s.z0;
+}
+
+// Back-trace (dcgrid_fluid.cu:115-122): (pos + .5) * scale - v * dt * rdx.
+__device__ inline void back_trace(const Dev &D, int4 bp, int c, size_t cell, float &px, float &py,
+                                  float &pz) {
+  int lx, ly, lz;
+  local_xyz(c, lx, ly, lz);
+  const float scale = (float)(1 << bp.w);
+  const float alpha = D.ph.dt * D.ph.rdx;
+  px = ((float)(bp.x + lx) + 0.5f) * scale - D.v[0][cell] * alpha;
+  py = ((float)(bp.y + ly) + 0.5f) * scale - D.v[1][cell] * alpha;
+  pz = ((float)(bp.z + lz) + 0.5f) * scale - D.v[2][cell] * alpha;
+}
+
 }  // namespace dcg

@@ -84,6 +84,11 @@ void launch_h16_to_f32(const uint16_t *src, float *dst, long long n, int mode, c
 void launch_f32_to_h16(const float *src, uint16_t *dst, long long n, int mode, cudaStream_t st);
 void launch_apron_table(const Dev &D, long long *dst, cudaStream_t st);
 
+// k_adjoint.cu — transpose of one step's density map (flow and topology fixed)
+void launch_adjoint_step(const Dev &D, float *lam_in_scratch, float *lam_out, float *lam_em, int sms,
+                         cudaStream_t st);
+void launch_adjoint_dense(const Dev &D, const float *lam_dense, float *lam, cudaStream_t st);
+
 // k_uniform.cu — uniform (dense, mip-mapped) grid
 struct UDev {
   int gx, gy, gz, levels, nq, ref_compat, pad0, pad1;

@@ -47,6 +47,7 @@ struct dcg_sim {
   float *vbuf[2][3] = {}, *qbuf[2][3] = {};
   uint16_t *qhbuf[2][3] = {};  // 16-bit scalar storage (mixed precision)
   float *conv_tmp = nullptr;   // FP32 staging for access to 16-bit fields
+  float *adj_tmp = nullptr;    // adjoint scratch (allocated on first use)
   int vpar = 0, qpar = 0;
 
   // uniform
@@ -387,6 +388,30 @@ struct dcg_sim {
     launch_apply_pressure(D, stream);
     restrict_v();
   }
+  // ---------------------------------------------------------------- state I/O
+  // The state a step depends on, as (device pointer, bytes) sections in a
+  // fixed order: block table, neighbour table, counters, then the fields of
+  // the current buffer parity.
+  std::vector<std::pair<void *, size_t>> state_sections() {
+    std::vector<std::pair<void *, size_t>> s;
+    const size_t B = (size_t)D.g.B, nc = B * BV;
+    s.push_back({D.pos, B * sizeof(int4)});
+    s.push_back({D.parent, B * 4});
+    s.push_back({D.child, 8 * B * 4});
+    s.push_back({D.nbr, 27 * B * 4});
+    s.push_back({D.flags, B});
+    s.push_back({D.load, MAXL * 8});
+    s.push_back({D.move_limit, MAXL * 8});
+    for (int d = 0; d < 3; d++) s.push_back({D.v[d], nc * 4});
+    s.push_back({D.w, nc * 4});
+    s.push_back({D.p, nc * 4});
+    s.push_back({D.pt, nc * 4});
+    s.push_back({D.div, nc * 4});
+    for (int k = 0; k < P.n_scalars; k++)
+      s.push_back({D.g.mixed ? static_cast<void *>(D.qh[k]) : static_cast<void *>(D.q[k]), nc * (D.g.mixed ? 2 : 4)});
+    return s;
+  }
+
   // one level of the cascade through the staged solve, as a batch of one
   // (prolongation only below the coarsest level)
   void solve_staged(int level, int prolong, int sweeps) {

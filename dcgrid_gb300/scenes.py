@@ -149,3 +149,25 @@ def cloud256(precision=capi.PRECISION_FP32, blocks=40000, levels=3, iters=100, e
 def emission_field(n=16, seed=1, scale=0.05):
     """Seeded emission map (density per time unit), n^3 values in [0, scale)."""
     return (scale * np.random.default_rng(seed).random(n ** 3)).astype(np.float32)
+
+
+def differentiable(g=128, levels=2, iters=20, em_n=16, noise=0.5):
+    """Differentiable scene: passive density transport in a seeded noise flow
+    (no buoyancy, no source, closed walls), the density injected by an
+    em_n^3 emission map over the bottom 16 cell layers, and the reference's
+    position-based refinement score, so the block topology does not depend on
+    the density. Budget: the coarsest level in full plus a quarter of the
+    finest level. `noise` is the amplitude of the seeded initial velocity."""
+    full = [(g >> (l + 2)) ** 3 for l in range(levels)]
+    p = capi.default_params(g, g, g, full[-1] + full[0] // 4)
+    p.levels = levels
+    p.dx = 1.0
+    p.dt = 1.0
+    p.inlet_enabled = 0
+    p.jacobi_iters = iters
+    p.n_scalars = 1
+    p.refine_criterion = capi.REFINE_GEOMETRIC
+    p.ref_compat = 0
+    p.emission_n = em_n
+    p.emission_band = 16.0
+    return p

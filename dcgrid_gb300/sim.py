@@ -61,6 +61,11 @@ def lib():
                                       C.POINTER(C.c_double)]
         L.dcg_launches_per_step.argtypes = [vp, C.POINTER(C.c_int64)]
         L.dcg_set_emission.argtypes = [vp, vp, C.c_int32]
+        L.dcg_state_bytes.argtypes = [vp, C.POINTER(C.c_int64)]
+        L.dcg_save_state.argtypes = [vp, vp, C.c_int32]
+        L.dcg_load_state.argtypes = [vp, vp, C.c_int32]
+        L.dcg_adjoint_step.argtypes = [vp, vp, vp, vp]
+        L.dcg_adjoint_dense.argtypes = [vp, vp, vp]
         L.dcg_batch_create.argtypes = [C.c_int32, vp, C.POINTER(vp)]
         for name in ["dcg_batch_destroy", "dcg_batch_reset", "dcg_batch_sync"]:
             getattr(L, name).argtypes = [vp]
@@ -269,6 +274,51 @@ class Simulation:
         n = C.c_int64()
         self._chk(self.L.dcg_launches_per_step(self.h, C.byref(n)), "launches_per_step")
         return int(n.value)
+
+    # -- state I/O (checkpoint / resume) ------------------------------------
+    def state_bytes(self):
+        n = C.c_int64()
+        self._chk(self.L.dcg_state_bytes(self.h, C.byref(n)), "state_bytes")
+        return n.value
+
+    def save_state(self, out=None):
+        """The state a step depends on, into a uint8 buffer: a numpy array (host)
+        or a CUDA torch tensor (device); a new host array when out is None."""
+        if out is None:
+            out = np.empty(self.state_bytes(), np.uint8)
+        if hasattr(out, "data_ptr"):
+            where = capi.DEVICE if out.is_cuda else capi.HOST
+            self._chk(self.L.dcg_save_state(self.h, C.c_void_p(out.data_ptr()), where), "save_state")
+        else:
+            self._chk(self.L.dcg_save_state(self.h, _ptr(out), capi.HOST), "save_state")
+        return out
+
+    def load_state(self, buf):
+        if hasattr(buf, "data_ptr"):
+            where = capi.DEVICE if buf.is_cuda else capi.HOST
+            self._chk(self.L.dcg_load_state(self.h, C.c_void_p(buf.data_ptr()), where), "load_state")
+        else:
+            a = np.ascontiguousarray(buf, np.uint8)
+            self._chk(self.L.dcg_load_state(self.h, _ptr(a), capi.HOST), "load_state")
+
+    def save(self, path):
+        """Writes the state to a file (checkpoint)."""
+        self.save_state().tofile(path)
+
+    def load(self, path):
+        self.load_state(np.fromfile(path, np.uint8))
+
+    # -- adjoint of the density path (CUDA torch tensors) --------------------
+    def adjoint_step(self, lam_in, lam_out, lam_emission=None):
+        """lam_out <- transpose of the last step's density map applied to
+        lam_in; lam_emission (emission_n^3) accumulates the emission adjoint."""
+        em = C.c_void_p(lam_emission.data_ptr()) if lam_emission is not None else None
+        self._chk(self.L.dcg_adjoint_step(self.h, C.c_void_p(lam_in.data_ptr()), C.c_void_p(lam_out.data_ptr()), em),
+                  "adjoint_step")
+
+    def adjoint_dense(self, lam_dense, lam_cells):
+        self._chk(self.L.dcg_adjoint_dense(self.h, C.c_void_p(lam_dense.data_ptr()),
+                                           C.c_void_p(lam_cells.data_ptr())), "adjoint_dense")
 
     def stats(self):
         st = capi.DcgStats()

@@ -328,6 +328,33 @@ int dcg_batch_get_info(const dcg_batch *batch, int32_t *n, int64_t *device_bytes
 int dcg_batch_time_solve(dcg_batch *batch, int32_t reps, float *avg_ms, double *bytes);
 const char *dcg_batch_last_error_string(const dcg_batch *batch);
 
+/* ---- state I/O (checkpoint / resume) -------------------------------------
+ * No reference counterpart (the reference keeps no on-disk format). The state
+ * is everything a step depends on: the block table, neighbour table, level
+ * loads and move limits, and the velocity, fluidity, pressure, divergence
+ * and scalar fields, after a 64-byte header naming the geometry, budget and
+ * storage formats. `where` = DCG_HOST or DCG_DEVICE for the buffer; loading
+ * a state into a simulation with a different geometry, budget or format is
+ * refused (DCG_E_INVALID). Parameters and the emission map are not part of
+ * the state. */
+int dcg_state_bytes(dcg_sim *sim, int64_t *bytes);
+int dcg_save_state(dcg_sim *sim, void *dst, int32_t where);
+int dcg_load_state(dcg_sim *sim, const void *src, int32_t where);
+
+/* ---- adjoint of the density path (spec extension; no reference
+ * counterpart) ----------------------------------------------------------------
+ * With the flow and the topology of the last step held fixed, one step maps
+ * the density linearly. dcg_adjoint_step applies the transpose of that map
+ * for the step that produced the current state: lam_in (device, 64*max_blocks
+ * cells, block-major) is the adjoint of the density after the step;
+ * lam_out (device, same size) receives the adjoint of the density before the
+ * step; lam_emission (device, emission_n^3, may be NULL) accumulates the
+ * adjoint of the emission map. dcg_adjoint_dense adds the transpose of the
+ * dense resampling (dcg_get_dense): lam_dense (device, gx*gy*gz) to
+ * lam_cells (device, block-major, accumulated). FP32 scalar storage only. */
+int dcg_adjoint_step(dcg_sim *sim, const float *lam_in, float *lam_out, float *lam_emission);
+int dcg_adjoint_dense(dcg_sim *sim, const float *lam_dense, float *lam_cells);
+
 /* sizeof of the ABI structs, for binding checks. */
 size_t dcg_sizeof_params(void);
 size_t dcg_sizeof_info(void);

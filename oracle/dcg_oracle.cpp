@@ -271,6 +271,36 @@ template <typename R> struct Physics {
     const R e11 = lerp(at(i0, j1, k1), at(i1, j1, k1), fu);
     return lerp(lerp(e00, e10, fv), lerp(e01, e11, fv), fw);
   }
+  // q_bc passes the scalar through (identity) at this corner
+  bool q_passes(int x, int y, int z, int scale) const {
+    if (in_inlet(x, y, z, scale)) return false;
+    if (P->wind_enabled && yz_inside(y, z, scale)) {
+      if (x < 0) return false;
+      if (x * scale >= gx) return true;
+    }
+    return !outside(x, y, z, scale);
+  }
+  // transpose of emission_at: lam_em[i] += g * d(emission)/d(E[i])
+  void emission_adjoint(int x, int y, int z, int scale, double g, double *lam_em) const {
+    const int n = P->emission_n;
+    const R s = (R)scale;
+    const R yw = ((R)y + (R)0.5f) * s;
+    if (!(yw < (R)P->emission_band)) return;
+    const R xw = ((R)x + (R)0.5f) * s, zw = ((R)z + (R)0.5f) * s;
+    const R top = (R)(n - 1);
+    const R u = clampr(xw * ((R)n / (R)gx) - (R)0.5f, (R)0, top);
+    const R v = clampr(yw * ((R)n / (R)P->emission_band) - (R)0.5f, (R)0, top);
+    const R w = clampr(zw * ((R)n / (R)gz) - (R)0.5f, (R)0, top);
+    const int i0 = (int)std::floor(u), j0 = (int)std::floor(v), k0 = (int)std::floor(w);
+    const int I[2] = {i0, i0 + 1 < n ? i0 + 1 : n - 1}, J[2] = {j0, j0 + 1 < n ? j0 + 1 : n - 1},
+              K[2] = {k0, k0 + 1 < n ? k0 + 1 : n - 1};
+    const double fu = (double)(u - (R)i0), fv = (double)(v - (R)j0), fw = (double)(w - (R)k0);
+    const double WU[2] = {1 - fu, fu}, WV[2] = {1 - fv, fv}, WW[2] = {1 - fw, fw};
+    for (int c = 0; c < 8; c++) {
+      const int a = (c >> 2) & 1, bb = (c >> 1) & 1, cc = c & 1;
+      lam_em[((size_t)K[cc] * n + J[bb]) * n + I[a]] += g * WU[a] * WV[bb] * WW[cc];
+    }
+  }
   R src_value(int k) const {
     return k == 0 ? (R)P->src_density : (k == 1 ? (R)P->src_temperature : (R)P->src_vapor);
   }
@@ -1237,6 +1267,93 @@ template <typename R> struct DC : Base {
         }
     return DCG_OK;
   }
+  // ---------------- adjoint of the density path ----------------
+  // Transpose of the step that produced the current state, with its flow and
+  // topology held fixed: restriction^T, (advection + emission)^T with source
+  // cells cut, then the transpose of the propagation into touched blocks.
+  // Serial loops: the scatters need no atomics.
+  void adjoint_step(const double *lam_in, double *lam_out, double *lam_em) {
+    const size_t nc = (size_t)B * BV;
+    std::vector<double> lam(lam_in, lam_in + nc);
+    for (int level = levels - 2; level >= 0; level--)
+      for (int64_t b = off[level]; b < off[level] + maxL[level]; b++) {
+        if (lvl[b] != level || parent[b] == NF) continue;
+        for (int s = 0; s < 8; s++) {
+          const size_t pc = (size_t)parent[b] * 8 + s;
+          const double lp = lam[pc] * 0.125;
+          for (int i = 0; i < 8; i++) lam[(size_t)b * BV + 8 * s + i] += lp;
+          lam[pc] = 0;
+        }
+      }
+    std::fill(lam_out, lam_out + nc, 0.0);
+    for (int64_t b = 0; b < B; b++) {
+      if (lvl[b] == FREE) continue;
+      for (int c = 0; c < BV; c++) {
+        const size_t cell = (size_t)b * BV + c;
+        if (!leaf(cell) || lam[cell] == 0) continue;
+        int x, y, z;
+        local_xyz(c, x, y, z);
+        const int scale = 1 << lvl[b];
+        if (ph.in_source(bx[b] + x, by[b] + y, bz[b] + z, scale)) continue;
+        if (P.emission_n > 0 && lam_em)
+          ph.emission_adjoint(bx[b] + x, by[b] + y, bz[b] + z, scale, (double)ph.dt * lam[cell], lam_em);
+        R pos[3];
+        back_trace(b, c, pos);
+        Sample s;
+        sample(pos[0], pos[1], pos[2], s);
+        if (s.wAcc < (R)1e-6f) continue;
+        for (int k = 0; k < 8; k++) {
+          int cx, cy, cz;
+          corner(s, k, cx, cy, cz);
+          if (ph.q_passes(cx, cy, cz, s.scale)) lam_out[s.idx[k]] += lam[cell] * (double)s.wt[k];
+        }
+      }
+    }
+    for (int level = 0; level <= levels - 2; level++)
+      for (size_t t = 0; t < touched.size(); t++) {
+        const int64_t b = touched[t];
+        if (b == NF || lvl[b] != level || parent[b] == NF) continue;
+        const int64_t pb = parent[b] / 8;
+        const int64_t *a = &apron[(size_t)pb * AV];
+        for (int c = 0; c < BV; c++) {
+          int lx, ly, lz;
+          local_xyz(c, lx, ly, lz);
+          const int x = bx[b] + lx, y = by[b] + ly, z = bz[b] + lz;
+          const int px = (x / 2) % BW, py = (y / 2) % BW, pz = (z / 2) % BW;
+          const int idx = AA * (1 + px) + AW * (1 + py) + (1 + pz);
+          const int i = x % 2 ? AA : -AA, j = y % 2 ? AW : -AW, k = z % 2 ? 1 : -1;
+          const size_t cell = (size_t)b * BV + c;
+          const double l = lam_out[cell];
+          lam_out[cell] = 0;
+          lam_out[a[idx]] += 27.0 / 64.0 * l;
+          lam_out[a[idx + k]] += 9.0 / 64.0 * l;
+          lam_out[a[idx + j]] += 9.0 / 64.0 * l;
+          lam_out[a[idx + i]] += 9.0 / 64.0 * l;
+          lam_out[a[idx + j + k]] += 3.0 / 64.0 * l;
+          lam_out[a[idx + i + k]] += 3.0 / 64.0 * l;
+          lam_out[a[idx + i + j]] += 3.0 / 64.0 * l;
+          lam_out[a[idx + i + j + k]] += 1.0 / 64.0 * l;
+        }
+      }
+  }
+  // transpose of get_dense: lam_cells[leaf covering (x,y,z)] += lam_dense[x,y,z]
+  void adjoint_dense(const double *lam_dense, double *lam_cells) const {
+    for (int z = 0; z < gz; z++)
+      for (int y = 0; y < gy; y++)
+        for (int x = 0; x < gx; x++) {
+          int level = 0;
+          const int64_t b = deep(x, y, z, level);
+          const int lx = (x >> level) - bx[b], ly = (y >> level) - by[b], lz = (z >> level) - bz[b];
+          lam_cells[(size_t)b * BV + local_of(lx, ly, lz)] += lam_dense[((size_t)z * gy + y) * gx + x];
+        }
+  }
+  // this simulation takes another one's whole state (same parameters)
+  void copy_state_from(const DC &o) {
+    *this = o;
+    ph.P = &P;
+    ph.em = &emis;
+  }
+
   void info(dcg_info *i) const override {
     std::memset(i, 0, sizeof(*i));
     i->mode = DCG_MODE_ADAPTIVE;
@@ -1886,5 +2003,26 @@ int dcgo_set_emission(dcgo_sim *s, const double *src) {
   return s && src ? s->impl->set_emission(src) : DCG_E_INVALID;
 }
 int dcgo_get_stats(dcgo_sim *s, dcg_stats *st) { return s && st ? s->impl->stats(st) : DCG_E_INVALID; }
+int dcgo_adjoint_step(dcgo_sim *s, const double *lam_in, double *lam_out, double *lam_em) {
+  if (!lam_in || !lam_out) return DCG_E_INVALID;
+  return with_dc(s, [&](auto &d) {
+    d.adjoint_step(lam_in, lam_out, lam_em);
+    return DCG_OK;
+  });
+}
+int dcgo_adjoint_dense(dcgo_sim *s, const double *lam_dense, double *lam_cells) {
+  if (!lam_dense || !lam_cells) return DCG_E_INVALID;
+  return with_dc(s, [&](auto &d) {
+    d.adjoint_dense(lam_dense, lam_cells);
+    return DCG_OK;
+  });
+}
+int dcgo_copy_state(dcgo_sim *dst, const dcgo_sim *src) {
+  if (!dst || !src) return DCG_E_INVALID;
+  if (dst->dcd && src->dcd) dst->dcd->copy_state_from(*src->dcd);
+  else if (dst->dcf && src->dcf) dst->dcf->copy_state_from(*src->dcf);
+  else return DCG_E_INVALID;
+  return DCG_OK;
+}
 
 }  // extern "C"

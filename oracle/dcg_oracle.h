@@ -72,6 +72,15 @@ int dcgo_adapt_replay(dcgo_sim *s, const int64_t *moves, int64_t n_moves,
 int dcgo_get_scores(dcgo_sim *s, float *subblock, float *block);
 int dcgo_get_stats(dcgo_sim *s, dcg_stats *st);
 int dcgo_set_emission(dcgo_sim *s, const double *src);
+/* FP64 host adjoint of the density path: transpose of the step that produced
+ * the current state (flow and topology fixed); lam_em (emission_n^3) is
+ * accumulated and may be NULL. */
+int dcgo_adjoint_step(dcgo_sim *s, const double *lam_in, double *lam_out, double *lam_em);
+/* transpose of dcgo_get_dense, accumulated into lam_cells */
+int dcgo_adjoint_dense(dcgo_sim *s, const double *lam_dense, double *lam_cells);
+/* dst takes src's whole state; both created with the same parameters and
+ * precision (checkpoints of the host adjoint). */
+int dcgo_copy_state(dcgo_sim *dst, const dcgo_sim *src);
 
 #ifdef __cplusplus
 }

@@ -54,6 +54,9 @@ def lib():
         L.dcgo_get_scores.argtypes = [vp, vp, vp]
         L.dcgo_get_stats.argtypes = [vp, C.POINTER(capi.DcgStats)]
         L.dcgo_set_emission.argtypes = [vp, vp]
+        L.dcgo_adjoint_step.argtypes = [vp, vp, vp, vp]
+        L.dcgo_adjoint_dense.argtypes = [vp, vp, vp]
+        L.dcgo_copy_state.argtypes = [vp, vp]
         _lib = L
     return _lib
 
@@ -200,6 +203,21 @@ class OracleSim:
         st = capi.DcgStats()
         self._chk(self.L.dcgo_get_stats(self.h, C.byref(st)), "stats")
         return st
+
+    def adjoint_step(self, lam_in, lam_em=None):
+        """FP64 transpose of the step that produced the current state; returns
+        the adjoint of the density before it; lam_em is accumulated in place."""
+        a = np.ascontiguousarray(lam_in, np.float64)
+        out = np.empty_like(a)
+        self._chk(self.L.dcgo_adjoint_step(self.h, _ptr(a), _ptr(out), _ptr(lam_em)), "adjoint_step")
+        return out
+
+    def adjoint_dense(self, lam_dense, lam_cells):
+        a = np.ascontiguousarray(lam_dense, np.float64).reshape(-1)
+        self._chk(self.L.dcgo_adjoint_dense(self.h, _ptr(a), _ptr(lam_cells)), "adjoint_dense")
+
+    def copy_state_from(self, other):
+        self._chk(self.L.dcgo_copy_state(self.h, other.h), "copy_state")
 
 
 def set_threads(n):

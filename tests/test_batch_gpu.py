@@ -96,7 +96,7 @@ def test_autotune_resets_and_keeps_results():
     b = Batch(params)
     t = b.autotune(spinup_steps=3, reps=2)
     assert all(x in (2, 4, 8) for x in t["tile"])
-    assert t["solve_cache"] in (0, 4, 8) and t["solve_barrier"] in (0, 1)
+    assert t["solve_cache"] in (0, 3, 4, 8) and t["solve_barrier"] in (0, 1)
     assert t["solve_ms"] > 0
     fresh = Batch(params)
     for i, p in enumerate(params):
