@@ -699,18 +699,19 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
     // in shared memory, then every cell reads its six neighbours from the
     // tile. The block's description (see fill_block_info) is built once per
     // launch into the dynamic shared memory when it fits, else per sweep.
-    // tile strides SX (x), SY (y), 1 (z)
-    constexpr int W = 8, U = DCG_SOLVE_U, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 6;
-    __shared__ float s_tile[W][U][TILE];
+    // tile strides SX (x), SY (y), 1 (z), interior cell (lx,ly,lz) at
+    // (lx+1)*SX + (ly+1)*SY + lz + 2; each lane owns the z-adjacent cell pair
+    // c = 2*lane, 2*lane+1, so its own values, divergences and results move
+    // as float2 and four of its twelve neighbour reads are float2 tile loads
+    constexpr int W = 8, U = DCG_SOLVE_U, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 8;
+    __shared__ __align__(16) float s_tile[W][U][TILE];
     __shared__ uint32_t s_scratch[W][U][BI_WORDS];
     const int w = t >> 5, lane = t & 31;
-    int o0, o1;
+    int oA;
     {
       int x, y, z;
-      local_xyz(lane, x, y, z);
-      o0 = (x + 1) * SX + (y + 1) * SY + (z + 1);
-      local_xyz(lane + 32, x, y, z);
-      o1 = (x + 1) * SX + (y + 1) * SY + (z + 1);
+      local_xyz(2 * lane, x, y, z);
+      oA = (x + 1) * SX + (y + 1) * SY + (z + 1) + 1;
     }
     // halo slots h = lane + 32q: tile position, cell in a same-level
     // neighbour, clamped own cell, compat-quirk own cell; apron coords + face
@@ -724,7 +725,7 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
       const int same = local_of((ax - 1) & 3, (ay - 1) & 3, (az - 1) & 3);
       const int self = local_of(clampi(ax, 1, BW) - 1, clampi(ay, 1, BW) - 1, clampi(az, 1, BW) - 1);
       const int quirk = local_of(clampi(ax, 1, BW) & 3, clampi(ay, 1, BW) & 3, clampi(az, 1, BW) & 3);
-      hpk[q] = (uint32_t)(ax * SX + ay * SY + az) | ((uint32_t)same << 9) | ((uint32_t)self << 15) |
+      hpk[q] = (uint32_t)(ax * SX + ay * SY + az + 1) | ((uint32_t)same << 9) | ((uint32_t)self << 15) |
                ((uint32_t)quirk << 21);
       hax[q] = (uint32_t)ax | ((uint32_t)ay << 4) | ((uint32_t)az << 8) | ((uint32_t)f << 12);
     }
@@ -742,7 +743,8 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
     // warp computes any of them; with DCG_SOLVE_PIPE the loads of the next
     // pass are issued before the current pass is computed from its tiles.
     struct Pass {
-      float v[U][5], dv[U][2], alpha[U];
+      float2 own_v[U], dv[U];
+      float halo[U][3], alpha[U];
       uint32_t own[U];
       bool act[U];
     };
@@ -783,13 +785,11 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
         }
         ps.own[u] = own;
         ps.alpha[u] = __uint_as_float(bi[1]);
-        ps.v[u][0] = __ldcg(src + own + lane);
-        ps.v[u][1] = __ldcg(src + own + lane + 32);
-        ps.v[u][2] = __ldcg(src + addr[0]);
-        ps.v[u][3] = __ldcg(src + addr[1]);
-        ps.v[u][4] = __ldcg(src + addr[2]);
-        ps.dv[u][0] = P.div[own + lane];
-        ps.dv[u][1] = P.div[own + lane + 32];
+        ps.own_v[u] = __ldcg(reinterpret_cast<const float2 *>(src + own) + lane);
+        ps.halo[u][0] = __ldcg(src + addr[0]);
+        ps.halo[u][1] = __ldcg(src + addr[1]);
+        ps.halo[u][2] = __ldcg(src + addr[2]);
+        ps.dv[u] = reinterpret_cast<const float2 *>(P.div + own)[lane];
       }
     };
     for (int it = 0; it < sweeps; it++) {
@@ -803,11 +803,10 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
         for (int u = 0; u < U; u++) {
           if (!cur.act[u]) continue;
           float *T = s_tile[w][u];
-          T[o0] = cur.v[u][0];
-          T[o1] = cur.v[u][1];
-          T[hpk[0] & 511] = cur.v[u][2];
-          T[hpk[1] & 511] = cur.v[u][3];
-          T[hpk[2] & 511] = cur.v[u][4];
+          *reinterpret_cast<float2 *>(T + oA) = cur.own_v[u];
+          T[hpk[0] & 511] = cur.halo[u][0];
+          T[hpk[1] & 511] = cur.halo[u][1];
+          T[hpk[2] & 511] = cur.halo[u][2];
         }
         __syncwarp();
         if (DCG_SOLVE_PIPE) load_pass(r0 + U, nxt);
@@ -815,11 +814,17 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
         for (int u = 0; u < U; u++) {
           if (!cur.act[u]) continue;
           const float *T = s_tile[w][u];
-          const float ad0 = cur.alpha[u] * cur.dv[u][0], ad1 = cur.alpha[u] * cur.dv[u][1];
-          dst[cur.own[u] + lane] =
-              (T[o0 - SX] + T[o0 + SX] + T[o0 - SY] + T[o0 + SY] + T[o0 - 1] + T[o0 + 1] - ad0) / 6.f;
-          dst[cur.own[u] + lane + 32] =
-              (T[o1 - SX] + T[o1 + SX] + T[o1 - SY] + T[o1 + SY] + T[o1 - 1] + T[o1 + 1] - ad1) / 6.f;
+          const float2 L = *reinterpret_cast<const float2 *>(T + oA - SX);
+          const float2 R = *reinterpret_cast<const float2 *>(T + oA + SX);
+          const float2 Dn = *reinterpret_cast<const float2 *>(T + oA - SY);
+          const float2 Up = *reinterpret_cast<const float2 *>(T + oA + SY);
+          const float Bk = T[oA - 1], Fw = T[oA + 2];
+          const float a = cur.own_v[u].x, b = cur.own_v[u].y;
+          const float adA = cur.alpha[u] * cur.dv[u].x, adB = cur.alpha[u] * cur.dv[u].y;
+          float2 res;
+          res.x = (L.x + R.x + Dn.x + Up.x + Bk + b - adA) / 6.f;
+          res.y = (L.y + R.y + Dn.y + Up.y + a + Fw - adB) / 6.f;
+          reinterpret_cast<float2 *>(dst + cur.own[u])[lane] = res;
         }
         __syncwarp();
         if (DCG_SOLVE_PIPE) cur = nxt;
