@@ -17,6 +17,9 @@ Workloads (--workload):
   cloud — one 3-level cloud scene at effective 256^3, 40k-block budget,
     terrain, wind inflow, temperature/vapor/density, field-driven
     refinement, 100 sweeps per level, FP32.
+  large — the 512^3 4-level fire plume with a 100 GB block budget: FP16
+    storage, FP32, and the uniform grid at the largest cube that fits 100 GB
+    (no CPU baseline or end-to-end leg at this size).
 
 Synthetic inputs throughout (seeded sources, terrain, noise, emission maps);
 scenes are spun up untimed before warm-up so the refined topology has
@@ -464,6 +467,70 @@ def run_cloud(args, ctx):
     return line
 
 
+# ------------------------------------------------------------------ large
+LARGE_SPINUP = 10
+LARGE_BUDGET = 100 * 10 ** 9
+
+
+def run_large(args, ctx):
+    """BASELINE config 5: the 512^3 4-level fire plume with a 100 GB block
+    budget (which exceeds the full block count of every level, so every level
+    is allocated in full), FP16 storage against FP32, and the uniform grid at
+    the largest cube that fits the same 100 GB."""
+    from dcgrid_gb300 import Simulation, capi, memory, scenes
+    out = {}
+    sims = [("fp16", capi.PRECISION_MIXED_FP16, capi.MODE_ADAPTIVE), ("fp32", capi.PRECISION_FP32, capi.MODE_ADAPTIVE),
+            ("uniform_fp32", capi.PRECISION_FP32, capi.MODE_UNIFORM)]
+    clk, launches, roof = None, 0, None
+    for name, prec, mode in sims:
+        p = scenes.fire(precision=prec, budget_bytes=LARGE_BUDGET)
+        if mode == capi.MODE_UNIFORM:
+            p.levels = 0
+            edge = memory.uniform_edge_for_budget(p, LARGE_BUDGET)
+            p.gx = p.gy = p.gz = edge
+            p.src_center[0] = p.src_center[2] = edge / 2.0
+        s = Simulation(p, mode)
+        s.set_stream(ctx.stream.cuda_stream)
+        s.add_velocity_noise(0, 0.01)
+        s.step(LARGE_SPINUP + max(args.warmup, 3))
+        s.sync()
+        if name == "fp16":
+            clocks = Clocks(ctx.clock_path)
+            clocks.start()
+        ms, cells = ctx.timed(args.steps, lambda: s.step(1), lambda: s.stats().active_cells, "timed_" + name)
+        if name == "fp16":
+            clk = clocks.stop(ctx.local)
+            launches = s.launches_per_step()
+            peak, peak_kind = peaks()
+            jms, jbytes = s.time_kernel(4, 0, 3)
+            ach = jbytes / (jms * 1e-3) / 1e9
+            roof = {"bound": "hbm", "kernel": f"k_level_solve_batch (one member, level 0, {ITERS} sweeps)",
+                    "achieved": ach, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
+                    "traffic": None, "algorithmic_bytes_per_launch": jbytes, "launch_ms": jms}
+        ms, cells = ctx.max_sum(ms, cells)
+        out[name] = {"value": cells / (ms * 1e-3), "ms_per_step": ms / args.steps, "domain": p.gx,
+                     "max_blocks": p.max_blocks if mode == capi.MODE_ADAPTIVE else None,
+                     "device_bytes": s.info.device_bytes, "active_cells_per_step": cells / args.steps}
+        s.close()
+    v = out["fp16"]
+    line = {"metric": METRIC, "value": v["value"], "unit": METRIC, "n_gpus": ctx.world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": v["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (seeded terrain, jittered heat source, velocity noise)",
+            "config": {"workload": "fire plume, effective 512^3, 4 levels, block budget sized to 100 GB "
+                                   f"(= the full {v['max_blocks']} blocks), crosswind 2 cells/step, "
+                                   f"{ITERS} Jacobi sweeps/level, FP16 scalar storage",
+                       "spinup_steps": LARGE_SPINUP, "l2": "inputs larger than L2; flushed between steps",
+                       "parallelism": f"replicas x{ctx.world}" if ctx.world > 1 else "single"},
+            "comparison": out, "gpu_launches": int(launches * args.steps), "launches_per_step": launches,
+            "roofline": roof,
+            "cpu_baseline": None,
+            "e2e": None}
+    if clk:
+        line["clocks"] = clk
+    return line
+
+
 # ------------------------------------------------------------------ reference arm
 def run_reference(args):
     """--impl reference: the reference's arithmetic on the host cores. The
@@ -521,13 +588,13 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "cloud"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "cloud", "large"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and FP64 error legs")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     ctx = Ctx()
-    line = run_batch(args, ctx) if args.workload == "batch" else run_cloud(args, ctx)
+    line = {"batch": run_batch, "cloud": run_cloud, "large": run_large}[args.workload](args, ctx)
     if ctx.rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -97,7 +97,8 @@ class DcgParams(C.Structure):
         ("precision", C.c_int32),
         ("emission_n", C.c_int32),
         ("emission_band", C.c_float),
-        ("reserved", C.c_int32 * 6),
+        ("src_jitter", C.c_float), ("src_jitter_seed", C.c_uint32),
+        ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -187,10 +188,17 @@ def params_to_dict(p):
 
 
 def params_from_dict(d):
+    """Inverse of params_to_dict. Dicts written before src_jitter and
+    src_jitter_seed took two of the six reserved words carry six zero
+    reserved entries; the extra zeros are dropped."""
     p = DcgParams()
     for k, v in d.items():
         if isinstance(v, (list, tuple)):
             arr = getattr(p, k)
+            if k == "reserved" and len(v) > len(arr):
+                if any(v[len(arr):]):
+                    raise ValueError("reserved parameter words must be zero")
+                v = v[:len(arr)]
             for i, x in enumerate(v):
                 arr[i] = x
         else:

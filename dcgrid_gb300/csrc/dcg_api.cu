@@ -495,6 +495,64 @@ size_t dcg_sizeof_params(void) { return sizeof(dcg_params); }
 size_t dcg_sizeof_info(void) { return sizeof(dcg_info); }
 size_t dcg_sizeof_stats(void) { return sizeof(dcg_stats); }
 
+// ---- memory-budget calculator -----------------------------------------------
+int dcg_plan_bytes(const dcg_params *params, int32_t mode, int64_t *bytes) {
+  if (!params || !bytes || (mode != DCG_MODE_ADAPTIVE && mode != DCG_MODE_UNIFORM)) return DCG_E_INVALID;
+  dcg_sim s;
+  s.P = *params;
+  s.mode = mode;
+  s.plan_only = true;
+  const int rc = mode == DCG_MODE_ADAPTIVE ? s.create_adaptive() : s.create_uniform();
+  if (rc) return rc;
+  *bytes = (int64_t)s.bytes;
+  return DCG_OK;
+}
+int dcg_blocks_for_budget(const dcg_params *params, int64_t budget_bytes, int64_t *max_blocks) {
+  if (!params || !max_blocks || budget_bytes <= 0) return DCG_E_INVALID;
+  dcg_params p = *params;
+  auto fits = [&](int64_t b, int *rc) {
+    p.max_blocks = b;
+    int64_t n = 0;
+    *rc = dcg_plan_bytes(&p, DCG_MODE_ADAPTIVE, &n);
+    return *rc == DCG_OK && n <= budget_bytes;
+  };
+  // the smallest valid budget fills the coarsest level; budgets beyond the
+  // full block count of every level leave blocks no level can use
+  dcg_params q = *params;
+  q.max_blocks = (1ll << 28) - 1;
+  dcg_sim probe;
+  probe.P = q;
+  probe.plan_only = true;
+  int rc = probe.create_adaptive();
+  if (rc) return rc;
+  long long lo = probe.D.g.full[probe.D.g.levels - 1], hi = 0;
+  for (int l = 0; l < probe.D.g.levels; l++) hi += probe.D.g.full[l];
+  // smallest budget the level split accepts (every level gets a block)
+  for (long long a = lo, b = hi; ; ) {
+    if (a >= b) {
+      lo = a;
+      break;
+    }
+    const long long mid = a + (b - a) / 2;
+    int64_t n = 0;
+    p.max_blocks = mid;
+    if (dcg_plan_bytes(&p, DCG_MODE_ADAPTIVE, &n) == DCG_OK) b = mid;
+    else a = mid + 1;
+  }
+  if (!fits(lo, &rc)) return rc ? rc : DCG_E_BUDGET;
+  if (fits(hi, &rc)) {
+    *max_blocks = hi;
+    return DCG_OK;
+  }
+  while (hi - lo > 1) {
+    const long long mid = lo + (hi - lo) / 2;
+    if (fits(mid, &rc)) lo = mid;
+    else hi = mid;
+  }
+  *max_blocks = lo;
+  return DCG_OK;
+}
+
 // ---- state I/O -------------------------------------------------------------
 namespace {
 struct StateHeader {

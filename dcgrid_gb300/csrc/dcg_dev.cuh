@@ -72,6 +72,8 @@ struct Phys {
   int em_n;
   float em_band;
   const float *em;  // em_n^3 emission field (device), or null
+  float src_jit;    // source temperature jitter amplitude
+  unsigned src_seed;
 };
 
 struct Dev {
@@ -371,6 +373,13 @@ __device__ inline bool in_source(const Phys &P, int x, int y, int z, int scale) 
   const float cy = ((float)y + 0.5f) * s - P.src_c[1];
   const float cz = ((float)z + 0.5f) * s - P.src_c[2];
   return cx * cx + cy * cy + cz * cz < P.src_r * P.src_r;
+}
+
+// Value a source cell takes for scalar k: the temperature (k = 1) with the
+// seeded per-cell jitter of the cell's level-local position.
+__device__ inline float src_value_at(const Phys &P, int k, int x, int y, int z, int level) {
+  if (k != 1 || P.src_jit == 0.f) return P.src_val[k];
+  return P.src_val[1] + P.src_jit * noise_unit(P.src_seed, x, y, z, level, 7);
 }
 
 // Emission field (extension): trilinear sample of the em_n^3 field over

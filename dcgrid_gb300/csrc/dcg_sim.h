@@ -79,9 +79,17 @@ struct dcg_sim {
     failed = true;
     return DCG_E_CUDA;
   }
+  // plan_only: creation only adds up the device bytes it would allocate
+  // (no CUDA calls), for the memory-budget calculator
+  bool plan_only = false;
   template <typename T> int alloc(T **p, size_t count) {
     void *q = nullptr;
     const size_t nbytes = std::max<size_t>(count * sizeof(T), 256);
+    if (plan_only) {
+      bytes += nbytes;
+      *p = nullptr;
+      return DCG_OK;
+    }
     cudaError_t e = cudaMalloc(&q, nbytes);
     if (e != cudaSuccess) return cuda(e, "cudaMalloc");
     allocs.push_back(q);
@@ -144,6 +152,8 @@ struct dcg_sim {
     ph.src_val[0] = P.src_density;
     ph.src_val[1] = P.src_temperature;
     ph.src_val[2] = P.src_vapor;
+    ph.src_jit = P.src_jitter;
+    ph.src_seed = P.src_jitter_seed;
     ph.wind = P.wind_enabled;
     ph.ter_amp = P.terrain_amplitude;
     ph.ter_base = P.terrain_base_height;
@@ -254,6 +264,7 @@ struct dcg_sim {
     if ((rc = alloc(&D.red, 32))) return rc;
     if ((rc = alloc(&D.bar, 64 + 32 * 18))) return rc;
     if ((rc = alloc(&D.epoch, B))) return rc;
+    if (plan_only) return plan_tail_adaptive(B);
     ls_grid = level_solve_grid(sms);
     if (const char *m = std::getenv("DCG_SOLVE_SYNC"))
       ls_epoch = std::strcmp(m, "epoch") == 0 ? 1 : std::strcmp(m, "barrier") == 0 ? 0
@@ -281,6 +292,18 @@ struct dcg_sim {
     S.max_n = nsort;
     bind_parity();
     return reset_adaptive();
+  }
+
+  // the allocations create_adaptive makes after the block table and fields
+  int plan_tail_adaptive(long long B) {
+    void *v;
+    if (P.emission_n > 0) alloc(reinterpret_cast<float **>(&v), (size_t)P.emission_n * P.emission_n * P.emission_n);
+    const long long nsort = 8 * B, nt = sort_tiles(nsort);
+    for (int i = 0; i < 6; i++) alloc(reinterpret_cast<uint32_t **>(&v), nsort);
+    alloc(reinterpret_cast<uint32_t **>(&v), 256 * nt);
+    alloc(reinterpret_cast<uint32_t **>(&v), 256);
+    alloc(reinterpret_cast<uint32_t **>(&v), nt + 1);
+    return DCG_OK;
   }
 
   // FluidSimulationDCGrid::reset + init (fluid_simulation_dcgrid.cu:190-261)
@@ -480,10 +503,12 @@ struct dcg_sim {
     if (P.emission_n > 0) {
       const size_t ne = (size_t)P.emission_n * P.emission_n * P.emission_n;
       if ((rc = alloc(&emis, ne))) return rc;
+      if (plan_only) return DCG_OK;
       if ((rc = cuda(cudaMemset(emis, 0, ne * 4), "emission"))) return rc;
       fill_phys(D.ph);
       fill_phys(U.ph);
     }
+    if (plan_only) return DCG_OK;
     bind_parity();
     return reset_uniform();
   }

@@ -81,7 +81,7 @@ __device__ __forceinline__ void advect_scalars_cell(const Dev &D, long long b, i
       o[0] = o[0] + D.ph.dt * emission_at(D.g, D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w);
     if (D.ph.src) {
       if (in_source(D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w))
-        for (int kq = 0; kq < nq; kq++) o[kq] = D.ph.src_val[kq];
+        for (int kq = 0; kq < nq; kq++) o[kq] = src_value_at(D.ph, kq, bp.x + lx, bp.y + ly, bp.z + lz, bp.w);
     }
   }
   for (int kq = 0; kq < nq; kq++) tq_st(D, kq, cell, o[kq]);
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(256) k_sources(Dev D) {
   int lx, ly, lz;
   local_xyz(c, lx, ly, lz);
   if (in_source(D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w))
-    for (int kq = 0; kq < D.g.nq; kq++) q_st(D, kq, cell, D.ph.src_val[kq]);
+    for (int kq = 0; kq < D.g.nq; kq++) q_st(D, kq, cell, src_value_at(D.ph, kq, bp.x + lx, bp.y + ly, bp.z + lz, bp.w));
 }
 
 // Seeded velocity noise on every allocated cell.

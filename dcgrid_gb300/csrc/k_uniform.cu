@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(256) k_u_sources(UDev U) {
   if (i >= U.nc) return;
   const int x = (int)(i % U.gx), y = (int)((i / U.gx) % U.gy), z = (int)(i / ((long long)U.gx * U.gy));
   if (in_source(U.ph, x, y, z, 1))
-    for (int k = 0; k < U.nq; k++) U.q[k][i] = U.ph.src_val[k];
+    for (int k = 0; k < U.nq; k++) U.q[k][i] = src_value_at(U.ph, k, x, y, z, 0);
 }
 
 struct USmp {
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(256) k_u_advect_scalars(UDev U) {
       }
     }
     if (k == 0 && U.ph.em_n > 0) acc = acc + U.ph.dt * emission_at(U.g, U.ph, x, y, z, 1);
-    U.tq[k][i] = src ? U.ph.src_val[k] : acc;
+    U.tq[k][i] = src ? src_value_at(U.ph, k, x, y, z, 0) : acc;
   }
 }
 

@@ -171,3 +171,30 @@ def differentiable(g=128, levels=2, iters=20, em_n=16, noise=0.5):
     p.emission_n = em_n
     p.emission_band = 16.0
     return p
+
+
+def fire(g=512, levels=4, precision=capi.PRECISION_FP32, budget_bytes=100 * 10 ** 9, iters=100):
+    """Large fire plume: effective g^3, `levels` levels, block budget sized to
+    `budget_bytes` of device memory (dcg_blocks_for_budget; capped at the full
+    block count, which 100 GB exceeds at 512^3), terrain from seeded value
+    noise (amplitude 40 cells), a ground heat source 64 cells wide at the
+    domain centre (temperature 30 with seeded per-cell jitter of +-3, density
+    1), buoyancy, crosswind of 2 cells/step, field-driven refinement."""
+    from . import memory
+    p = cloud(g, 1, levels, iters, 0)
+    p.terrain_amplitude = 40.0
+    p.terrain_base_height = 4.0
+    p.terrain_seed = 13
+    p.wind[0] = 2.0
+    p.src_center[0] = g / 2.0
+    p.src_center[1] = 4.0
+    p.src_center[2] = g / 2.0
+    p.src_radius = 32.0
+    p.src_density = 1.0
+    p.src_temperature = 30.0
+    p.src_vapor = 0.0
+    p.src_jitter = 3.0
+    p.src_jitter_seed = 11
+    p.precision = precision
+    p.max_blocks = memory.blocks_for_budget(p, budget_bytes)
+    return p

@@ -124,7 +124,11 @@ typedef struct dcg_params {
    * leaf cells there gain dt * E(trilinear) of density every step. */
   int32_t emission_n;        /* 0 = no emission field                        */
   float emission_band;       /* finest cells                                 */
-  int32_t reserved[6];
+  /* extension: seeded per-cell jitter of the source temperature, src_temperature
+   * + src_jitter * u with u in [-1, 1) from the cell's level-local position */
+  float src_jitter;
+  uint32_t src_jitter_seed;
+  int32_t reserved[4];
 } dcg_params;
 
 /* Fills *p with the reference's defaults (src/data/sim_params.cpp:4-34) for a
@@ -327,6 +331,17 @@ int dcg_batch_get_info(const dcg_batch *batch, int32_t *n, int64_t *device_bytes
  * an unspecified state until the next step's projection. */
 int dcg_batch_time_solve(dcg_batch *batch, int32_t reps, float *avg_ms, double *bytes);
 const char *dcg_batch_last_error_string(const dcg_batch *batch);
+
+/* ---- memory-budget calculator (the reference's scripts/calcMemory*.js,
+ * restated for this layout; no GPU needed) ---------------------------------
+ * dcg_plan_bytes: device bytes dcg_create(params, mode) allocates (buffers that
+ * read-out calls allocate on first use are not included). dcg_blocks_for_budget:
+ * the largest max_blocks (params->max_blocks ignored) whose adaptive
+ * allocation fits budget_bytes, capped at the full block count of every level
+ * (blocks beyond it are never used by any level); DCG_E_BUDGET when not even
+ * the coarsest level fits. */
+int dcg_plan_bytes(const dcg_params *params, int32_t mode, int64_t *bytes);
+int dcg_blocks_for_budget(const dcg_params *params, int64_t budget_bytes, int64_t *max_blocks);
 
 /* ---- state I/O (checkpoint / resume) -------------------------------------
  * No reference counterpart (the reference keeps no on-disk format). The state

@@ -301,6 +301,12 @@ template <typename R> struct Physics {
       lam_em[((size_t)K[cc] * n + J[bb]) * n + I[a]] += g * WU[a] * WV[bb] * WW[cc];
     }
   }
+  // a source cell's value for scalar k: the temperature with the seeded
+  // per-cell jitter of the cell's level-local position (extension)
+  R src_value_at(int k, int x, int y, int z, int level) const {
+    if (k != 1 || P->src_jitter == 0.f) return src_value(k);
+    return (R)(P->src_temperature + P->src_jitter * noise_unit(P->src_jitter_seed, x, y, z, level, 7));
+  }
   R src_value(int k) const {
     return k == 0 ? (R)P->src_density : (k == 1 ? (R)P->src_temperature : (R)P->src_vapor);
   }
@@ -697,7 +703,8 @@ template <typename R> struct DC : Base {
         int x, y, z;
         local_xyz(c, x, y, z);
         if (ph.in_source(bx[b] + x, by[b] + y, bz[b] + z, 1 << lvl[b]))
-          for (int k = 0; k < nq; k++) q[k][cell] = store_q(ph.src_value(k), P.precision);
+          for (int k = 0; k < nq; k++)
+            q[k][cell] = store_q(ph.src_value_at(k, bx[b] + x, by[b] + y, bz[b] + z, lvl[b]), P.precision);
       }
     }
   }
@@ -722,7 +729,7 @@ template <typename R> struct DC : Base {
           if (P.emission_n > 0)
             tq[0][cell] = tq[0][cell] + ph.dt * ph.emission_at(bx[b] + x, by[b] + y, bz[b] + z, 1 << lvl[b]);
           if (ph.in_source(bx[b] + x, by[b] + y, bz[b] + z, 1 << lvl[b]))
-            for (int k = 0; k < nq; k++) tq[k][cell] = ph.src_value(k);
+            for (int k = 0; k < nq; k++) tq[k][cell] = ph.src_value_at(k, bx[b] + x, by[b] + y, bz[b] + z, lvl[b]);
           for (int k = 0; k < nq; k++) tq[k][cell] = store_q(tq[k][cell], P.precision);
         } else {
           for (int k = 0; k < nq; k++) tq[k][cell] = 0;
@@ -1521,7 +1528,7 @@ template <typename R> struct UG : Base {
       for (int y = 0; y < gy; y++)
         for (int x = 0; x < gx; x++)
           if (ph.in_source(x, y, z, 1))
-            for (int k = 0; k < nq; k++) q[k][idx3(x, y, z)] = ph.src_value(k);
+            for (int k = 0; k < nq; k++) q[k][idx3(x, y, z)] = ph.src_value_at(k, x, y, z, 0);
   }
   struct Sample {
     size_t idx[8];
@@ -1622,7 +1629,7 @@ template <typename R> struct UG : Base {
             tq[k][i] = out;
           }
           if (ph.in_source(x, y, z, 1))
-            for (int k = 0; k < nq; k++) tq[k][i] = ph.src_value(k);
+            for (int k = 0; k < nq; k++) tq[k][i] = ph.src_value_at(k, x, y, z, 0);
         }
     for (int k = 0; k < nq; k++) q[k].swap(tq[k]);
     return DCG_OK;

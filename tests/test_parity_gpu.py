@@ -78,6 +78,8 @@ SCENARIOS = {
     "ref_sphere": lambda: scenarios.sphere_obstacle(64, 128, 64, 3000),
     "ref_nocompat": lambda: (lambda p: (setattr(p, "ref_compat", 0), p)[1])(scenarios.ref_default(64, 128, 64, 3000)),
     "plume": lambda: scenarios.plume(32, 64, 32, None, 2, 20),
+    "plume_jitter": lambda: (lambda p: (setattr(p, "src_jitter", 3.0), setattr(p, "src_jitter_seed", 5), p)[2])(
+        scenarios.plume(32, 64, 32, None, 2, 20)),
     "cloud": lambda: scenarios.cloud(64, 1500, 3, 10, 0),
     "cloud_compat": lambda: scenarios.cloud(64, 1500, 3, 10, 1),
 }
@@ -162,6 +164,7 @@ def test_fp32_vs_fp64_oracle(name):
 def test_uniform_mode_bitexact():
     p = scenarios.plume(32, 64, 32, None, 0, 10)
     p.levels = 0
+    p.src_jitter, p.src_jitter_seed = 2.0, 3
     g, o = gpu(p, capi.MODE_UNIFORM), orc(p, "float", capi.MODE_UNIFORM)
     for s in (g, o):
         s.add_velocity_noise(9, 0.1)
