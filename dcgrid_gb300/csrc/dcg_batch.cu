@@ -28,6 +28,7 @@ struct dcg_batch {
   std::vector<void *> allocs;
   size_t bytes = 0;
   float *p_arena = nullptr, *pt_arena = nullptr, *div_arena = nullptr;
+  uint32_t *binfo = nullptr;  // block descriptions of a cascade round, 13 words per block
   uint32_t *bar = nullptr, *errw = nullptr;
   std::vector<unsigned long long> arena_off;
   int maxtop = 0, iters = 0;
@@ -133,6 +134,7 @@ struct dcg_batch {
         P.p = p_arena;
         P.pt = pt_arena;
         P.div = div_arena;
+        P.binfo = binfo;
         P.bar = bar;
         P.err = errw;
         for (int i = 0; i < P.n; i++) {
@@ -367,7 +369,7 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
   }
   int rc;
   if ((rc = b->alloc(&b->p_arena, cells)) || (rc = b->alloc(&b->pt_arena, cells)) ||
-      (rc = b->alloc(&b->div_arena, cells)) ||
+      (rc = b->alloc(&b->div_arena, cells)) || (rc = b->alloc(&b->binfo, 13 * (cells / BV))) ||
       (rc = b->alloc(&b->bar, 64 + 32 * 18)) || (rc = b->alloc(&b->errw, 4))) {
     delete b;
     return rc;

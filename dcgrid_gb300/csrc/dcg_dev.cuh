@@ -95,6 +95,7 @@ struct Dev {
   double *red;             // reductions (stats)
   uint32_t *bar;           // grid barrier {arrivals, generation}
   uint32_t *epoch;         // per block: sweeps completed in the running level solve
+  uint32_t *binfo;         // level solve: block descriptions of the running level (13 words per block)
 };
 
 // Two-level grid barrier: CTAs arrive on one of 16 group counters (separate

@@ -264,6 +264,7 @@ struct dcg_sim {
     if ((rc = alloc(&D.red, 32))) return rc;
     if ((rc = alloc(&D.bar, 64 + 32 * 18))) return rc;
     if ((rc = alloc(&D.epoch, B))) return rc;
+    if ((rc = alloc(&D.binfo, 13 * B))) return rc;
     if (plan_only) return plan_tail_adaptive(B);
     ls_grid = level_solve_grid(sms);
     if (const char *m = std::getenv("DCG_SOLVE_SYNC"))
@@ -445,6 +446,7 @@ struct dcg_sim {
     SB.p = D.p;
     SB.pt = D.pt;
     SB.div = D.div;
+    SB.binfo = D.binfo;
     SB.bar = D.bar;
     SB.err = D.err;
     SB.arena[0] = 0;

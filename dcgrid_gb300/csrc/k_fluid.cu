@@ -731,14 +731,23 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
     }
     const long long nblocks = total >> 6;
     const int rounds_b = (int)((nblocks + (long long)W * nctas - 1) / ((long long)W * nctas));
+    // block descriptions: in shared memory when they fit, else built once
+    // into the global table P.binfo (indexed by level block) and copied to
+    // the warp's scratch when the block comes up
     const bool cached = rounds_b <= CACHE * 2048 / (W * BI_WORDS);
-    if (cached) {
-      for (int r = 0; r < rounds_b; r++) {
-        const long long gb = ((long long)r * nctas + blockIdx.x) * W + w;
-        if (gb < nblocks) fill_block_info(P, s_end, s_lev, gb, s_cache + (r * W + w) * BI_WORDS, lane);
+    for (int r = 0; r < rounds_b; r++) {
+      const long long gb = ((long long)r * nctas + blockIdx.x) * W + w;
+      if (gb >= nblocks) continue;
+      if (cached) {
+        fill_block_info(P, s_end, s_lev, gb, s_cache + (r * W + w) * BI_WORDS, lane);
+      } else {
+        fill_block_info(P, s_end, s_lev, gb, s_scratch[w][0], lane);
+        __syncwarp();
+        if (lane < BI_WORDS) P.binfo[gb * BI_WORDS + lane] = s_scratch[w][0][lane];
+        __syncwarp();
       }
-      __syncwarp();
     }
+    __syncwarp();
     // Passes of U rounds: every lane issues the loads of U blocks before the
     // warp computes any of them; with DCG_SOLVE_PIPE the loads of the next
     // pass are issued before the current pass is computed from its tiles.
@@ -758,7 +767,7 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
         if (!ps.act[u]) continue;
         const uint32_t *bi = cached ? s_cache + (r * W + w) * BI_WORDS : s_scratch[w][u];
         if (!cached) {
-          fill_block_info(P, s_end, s_lev, gb, s_scratch[w][u], lane);
+          if (lane < BI_WORDS) s_scratch[w][u][lane] = P.binfo[gb * BI_WORDS + lane];
           __syncwarp();
         }
         const uint32_t own = bi[0];
