@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdcgrid_gb300.so")
-SOURCES = ["dcg_api.cu", "dcg_batch.cu", "k_adjoint.cu", "k_fluid.cu", "k_topology.cu", "k_sort.cu", "k_uniform.cu"]
+SOURCES = ["dcg_api.cu", "dcg_batch.cu", "k_adjoint.cu", "k_fluid.cu", "k_render.cu", "k_topology.cu", "k_sort.cu", "k_uniform.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fno-strict-aliasing"]

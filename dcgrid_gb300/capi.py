@@ -130,6 +130,19 @@ class DcgTuning(C.Structure):
     ]
 
 
+RENDER_FLUID, RENDER_DENSITY, RENDER_VELOCITY, RENDER_FLUIDITY, RENDER_RESOLUTION = range(5)
+
+
+class DcgRenderParams(C.Structure):
+    _fields_ = [
+        ("width", C.c_int32), ("height", C.c_int32), ("eye", C.c_float * 3), ("eye_dir", C.c_float * 3),
+        ("fov", C.c_float), ("sun_dir", C.c_float * 3), ("aa_samples", C.c_int32), ("channel", C.c_int32),
+        ("shadows", C.c_int32), ("solids", C.c_int32), ("precise", C.c_int32), ("ambient", C.c_float),
+        ("smoke_color", C.c_float * 3), ("scene_color", C.c_float * 3), ("floor_color", C.c_float * 3),
+        ("reserved", C.c_int32 * 4),
+    ]
+
+
 def tuning_to_dict(t):
     return {"tile": list(t.tile), "solve_cache": t.solve_cache, "solve_ctas_per_sm": t.solve_ctas_per_sm,
             "solve_barrier": t.solve_barrier, "solve_ms": t.solve_ms, "cells_ms": list(t.cells_ms)}

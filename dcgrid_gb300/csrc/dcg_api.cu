@@ -495,6 +495,65 @@ size_t dcg_sizeof_params(void) { return sizeof(dcg_params); }
 size_t dcg_sizeof_info(void) { return sizeof(dcg_info); }
 size_t dcg_sizeof_stats(void) { return sizeof(dcg_stats); }
 
+// ---- headless renderer -------------------------------------------------------
+void dcg_default_render_params(dcg_render_params *rp, int32_t width, int32_t height) {
+  std::memset(rp, 0, sizeof(*rp));
+  rp->width = width;
+  rp->height = height;
+  rp->eye_dir[2] = 1.f;  // along +z
+  rp->fov = 1.f;
+  const float sx = .5f, sy = 1.f, sz = .3f, sn = std::sqrt(sx * sx + sy * sy + sz * sz);
+  rp->sun_dir[0] = sx / sn; rp->sun_dir[1] = sy / sn; rp->sun_dir[2] = sz / sn;
+  rp->aa_samples = 1;              // src/data/sim_params.cpp:24
+  rp->channel = DCG_RENDER_FLUID;
+  rp->shadows = 1;                 // cpp:21
+  rp->solids = 1;                  // cpp:20
+  rp->precise = 1;                 // cpp:22
+  rp->ambient = .3f;               // cpp:27
+  for (int i = 0; i < 3; i++) rp->smoke_color[i] = .9f;  // cpp:30
+  const float scene[3] = {107.f, 163.f, 204.f}, floor_[3] = {178.f, 158.f, 135.f};  // cpp:29,31
+  for (int i = 0; i < 3; i++) {
+    rp->scene_color[i] = scene[i] / 255.f;
+    rp->floor_color[i] = floor_[i] / 255.f;
+  }
+}
+int dcg_render(dcg_sim *s, const dcg_render_params *rp, float *rgba, int32_t where) {
+  if (bad(s) || !rp || !rgba || rp->width <= 0 || rp->height <= 0 || rp->aa_samples < 1 || rp->channel < 0 ||
+      rp->channel > DCG_RENDER_RESOLUTION)
+    return DCG_E_INVALID;
+  if (s->mode == DCG_MODE_UNIFORM && s->P.precision != DCG_PRECISION_FP32) return DCG_E_INVALID;
+  RenderP R{};
+  R.width = rp->width; R.height = rp->height; R.aa = rp->aa_samples; R.channel = rp->channel;
+  R.shadows = rp->shadows; R.solids = rp->solids; R.precise = rp->precise;
+  for (int i = 0; i < 3; i++) {
+    R.eye[i] = rp->eye[i]; R.eye_dir[i] = rp->eye_dir[i]; R.sun[i] = rp->sun_dir[i];
+    R.smoke[i] = rp->smoke_color[i]; R.scene[i] = rp->scene_color[i]; R.floor_[i] = rp->floor_color[i];
+  }
+  R.fov = rp->fov;
+  R.ambient = rp->ambient;
+  const size_t n = (size_t)rp->width * rp->height;
+  float4 *out = reinterpret_cast<float4 *>(rgba);
+  int rc;
+  if (where != DCG_DEVICE) {
+    if (s->render_cap < n) {
+      if (s->render_tmp) cudaFree(s->render_tmp);
+      s->render_tmp = nullptr;
+      s->render_cap = 0;
+      if ((rc = s->cuda(cudaMalloc(&s->render_tmp, n * 16), "render"))) return rc;
+      s->render_cap = n;
+    }
+    out = reinterpret_cast<float4 *>(s->render_tmp);
+  }
+  if (s->mode == DCG_MODE_ADAPTIVE) launch_render_adaptive(s->D, R, out, s->stream);
+  else launch_render_uniform(s->U, R, out, s->stream);
+  if ((rc = s->check_launch("render"))) return rc;
+  if (where != DCG_DEVICE &&
+      (rc = s->cuda(cudaMemcpyAsync(rgba, out, n * 16, cudaMemcpyDeviceToHost, s->stream), "render")))
+    return rc;
+  return s->sync("render");
+}
+size_t dcg_sizeof_render_params(void) { return sizeof(dcg_render_params); }
+
 // ---- memory-budget calculator -----------------------------------------------
 int dcg_plan_bytes(const dcg_params *params, int32_t mode, int64_t *bytes) {
   if (!params || !bytes || (mode != DCG_MODE_ADAPTIVE && mode != DCG_MODE_UNIFORM)) return DCG_E_INVALID;

@@ -90,6 +90,12 @@ void launch_adjoint_step(const Dev &D, float *lam_in_scratch, float *lam_out, fl
                          cudaStream_t st);
 void launch_adjoint_dense(const Dev &D, const float *lam_dense, float *lam, cudaStream_t st);
 
+// k_render.cu — headless ray marcher (parameters mirror dcg_render_params)
+struct RenderP {
+  int width, height, aa, channel, shadows, solids, precise, pad;
+  float eye[3], eye_dir[3], fov, sun[3], ambient, smoke[3], scene[3], floor_[3];
+};
+
 // k_uniform.cu — uniform (dense, mip-mapped) grid
 struct UDev {
   int gx, gy, gz, levels, nq, ref_compat, pad0, pad1;
@@ -108,5 +114,7 @@ void launch_u_advect_scalars(const UDev &U, cudaStream_t st);
 void launch_u_project(const UDev &U, int top_pairs, int pairs, bool local, cudaStream_t st);
 void launch_u_add_noise(const UDev &U, unsigned long long seed, float amp, cudaStream_t st);
 void launch_u_stats(const UDev &U, cudaStream_t st);
+void launch_render_adaptive(const Dev &D, const RenderP &R, float4 *out, cudaStream_t st);
+void launch_render_uniform(const UDev &U, const RenderP &R, float4 *out, cudaStream_t st);
 
 }  // namespace dcg

@@ -48,6 +48,8 @@ struct dcg_sim {
   uint16_t *qhbuf[2][3] = {};  // 16-bit scalar storage (mixed precision)
   float *conv_tmp = nullptr;   // FP32 staging for access to 16-bit fields
   float *adj_tmp = nullptr;    // adjoint scratch (allocated on first use)
+  float *render_tmp = nullptr; // renderer output staging for host buffers
+  size_t render_cap = 0;
   int vpar = 0, qpar = 0;
 
   // uniform
@@ -105,6 +107,7 @@ struct dcg_sim {
     bytes = 0;
   }
   ~dcg_sim() {
+    if (render_tmp) cudaFree(render_tmp);
     free_all();
     if (own_stream && stream) cudaStreamDestroy(stream);
   }

@@ -61,6 +61,9 @@ def lib():
                                       C.POINTER(C.c_double)]
         L.dcg_launches_per_step.argtypes = [vp, C.POINTER(C.c_int64)]
         L.dcg_set_emission.argtypes = [vp, vp, C.c_int32]
+        L.dcg_default_render_params.argtypes = [C.POINTER(capi.DcgRenderParams), C.c_int32, C.c_int32]
+        L.dcg_default_render_params.restype = None
+        L.dcg_render.argtypes = [vp, C.POINTER(capi.DcgRenderParams), vp, C.c_int32]
         L.dcg_state_bytes.argtypes = [vp, C.POINTER(C.c_int64)]
         L.dcg_save_state.argtypes = [vp, vp, C.c_int32]
         L.dcg_load_state.argtypes = [vp, vp, C.c_int32]
@@ -79,7 +82,8 @@ def lib():
         L.dcg_batch_time_solve.argtypes = [vp, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_double)]
         L.dcg_batch_last_error_string.argtypes = [vp]
         L.dcg_batch_last_error_string.restype = C.c_char_p
-        for name in ["dcg_sizeof_params", "dcg_sizeof_info", "dcg_sizeof_stats", "dcg_sizeof_tuning"]:
+        for name in ["dcg_sizeof_params", "dcg_sizeof_info", "dcg_sizeof_stats", "dcg_sizeof_tuning",
+                     "dcg_sizeof_render_params"]:
             getattr(L, name).restype = C.c_size_t
             getattr(L, name).argtypes = []
         _lib = L
@@ -90,6 +94,17 @@ def default_params(gx, gy, gz, max_blocks):
     p = capi.DcgParams()
     lib().dcg_default_params(C.byref(p), gx, gy, gz, max_blocks)
     return p
+
+
+def default_render_params(width, height, params=None):
+    """The reference's render defaults; with `params`, the eye is placed in
+    front of the domain (-z side) looking along +z at its centre."""
+    rp = capi.DcgRenderParams()
+    lib().dcg_default_render_params(C.byref(rp), width, height)
+    if params is not None:
+        dx = params.dx
+        rp.eye[0], rp.eye[1], rp.eye[2] = 0.5 * params.gx * dx, 0.5 * params.gy * dx, -1.2 * params.gz * dx
+    return rp
 
 
 def _ptr(a):
@@ -274,6 +289,19 @@ class Simulation:
         n = C.c_int64()
         self._chk(self.L.dcg_launches_per_step(self.h, C.byref(n)), "launches_per_step")
         return int(n.value)
+
+    # -- headless renderer ---------------------------------------------------
+    def render(self, rp, out=None):
+        """RGBA image (height, width, 4) float32: numpy (host) or a CUDA torch
+        tensor given as `out`."""
+        if out is None:
+            out = np.empty((rp.height, rp.width, 4), np.float32)
+        if hasattr(out, "data_ptr"):
+            where = capi.DEVICE if out.is_cuda else capi.HOST
+            self._chk(self.L.dcg_render(self.h, C.byref(rp), C.c_void_p(out.data_ptr()), where), "render")
+        else:
+            self._chk(self.L.dcg_render(self.h, C.byref(rp), _ptr(out), capi.HOST), "render")
+        return out
 
     # -- state I/O (checkpoint / resume) ------------------------------------
     def state_bytes(self):

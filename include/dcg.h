@@ -332,6 +332,37 @@ int dcg_batch_get_info(const dcg_batch *batch, int32_t *n, int64_t *device_bytes
 int dcg_batch_time_solve(dcg_batch *batch, int32_t reps, float *avg_ms, double *bytes);
 const char *dcg_batch_last_error_string(const dcg_batch *batch);
 
+/* ---- headless renderer (the reference's render(): src/raymarching.cuh,
+ * src/dcgrid/dcgrid_rendering.cu, src/uniformgrid/uniformgrid_rendering.cu)
+ * ------------------------------------------------------------------------
+ * Ray-marches the density into width*height RGBA float4 pixels (row-major,
+ * x fastest) in a caller buffer instead of a GL surface. Camera, colours and
+ * switches follow the reference's SimParams render fields. */
+enum {
+  DCG_RENDER_FLUID = 0,      /* density volume, optional sun shadows  */
+  DCG_RENDER_DENSITY = 1,    /* debug slice z = gz/2                  */
+  DCG_RENDER_VELOCITY = 2,
+  DCG_RENDER_FLUIDITY = 3,
+  DCG_RENDER_RESOLUTION = 4  /* checker of the sampled cell positions */
+};
+typedef struct {
+  int32_t width, height;
+  float eye[3];       /* world units                                       */
+  float eye_dir[3];   /* y and z pitch the view about the x axis           */
+  float fov;
+  float sun_dir[3];   /* unit vector toward the sun                        */
+  int32_t aa_samples; /* per axis                                          */
+  int32_t channel;    /* DCG_RENDER_*                                      */
+  int32_t shadows, solids, precise;
+  float ambient;
+  float smoke_color[3], scene_color[3], floor_color[3];
+  int32_t reserved[4];
+} dcg_render_params;
+/* the reference's defaults (src/data/sim_params.cpp:16-31) for a width*height
+ * image, eye outside the domain looking along +z */
+void dcg_default_render_params(dcg_render_params *rp, int32_t width, int32_t height);
+int dcg_render(dcg_sim *sim, const dcg_render_params *rp, float *rgba, int32_t where);
+
 /* ---- memory-budget calculator (the reference's scripts/calcMemory*.js,
  * restated for this layout; no GPU needed) ---------------------------------
  * dcg_plan_bytes: device bytes dcg_create(params, mode) allocates (buffers that
@@ -375,6 +406,7 @@ size_t dcg_sizeof_params(void);
 size_t dcg_sizeof_info(void);
 size_t dcg_sizeof_stats(void);
 size_t dcg_sizeof_tuning(void);
+size_t dcg_sizeof_render_params(void);
 
 #ifdef __cplusplus
 }

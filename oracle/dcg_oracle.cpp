@@ -131,6 +131,7 @@ struct Base {
   virtual int get_dense(int f, double *dst) = 0;
   virtual int stats(dcg_stats *st) = 0;
   virtual int set_emission(const double *src) = 0;
+  virtual int render(const dcg_render_params &rp, double *out) const = 0;
   int fail(int code, const char *msg) {
     err = msg;
     return code;
@@ -309,6 +310,220 @@ template <typename R> struct Physics {
   }
   R src_value(int k) const {
     return k == 0 ? (R)P->src_density : (k == 1 ? (R)P->src_temperature : (R)P->src_vapor);
+  }
+};
+
+// ======================================================================
+//  Ray marcher (src/raymarching.cuh:17-275, camera of k_dcgrid_render,
+//  src/dcgrid/dcgrid_rendering.cu:58-92), templated on the grid's sampler
+// ======================================================================
+template <typename R> struct V3 {
+  R x, y, z;
+  V3 operator+(V3 o) const { return {x + o.x, y + o.y, z + o.z}; }
+  V3 operator-(V3 o) const { return {x - o.x, y - o.y, z - o.z}; }
+  V3 operator*(R s) const { return {x * s, y * s, z * s}; }
+  V3 operator/(R s) const { return {x / s, y / s, z / s}; }
+};
+template <typename R> inline R dot3(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <typename R> inline R len3(V3<R> a) { return std::sqrt(dot3(a, a)); }
+template <typename R> inline V3<R> normalize3(V3<R> a) { return a * ((R)1 / len3(a)); }
+template <typename R> struct March {
+  int ix, iy, iz;
+  R fx, fy, fz;
+  size_t idx[8];
+  R density;
+};
+// MarchAux::interpolate (raymarching.cuh:27-42)
+template <typename R, class F> inline R interp(const March<R> &a, F f) {
+  const R dxInv = (R)1 - a.fx;
+  const R c00 = f(a.idx[0]) * dxInv + f(a.idx[4]) * a.fx;
+  const R c01 = f(a.idx[1]) * dxInv + f(a.idx[5]) * a.fx;
+  const R c10 = f(a.idx[2]) * dxInv + f(a.idx[6]) * a.fx;
+  const R c11 = f(a.idx[3]) * dxInv + f(a.idx[7]) * a.fx;
+  const R dyInv = (R)1 - a.fy;
+  const R c0 = c00 * dyInv + c10 * a.fy;
+  const R c1 = c01 * dyInv + c11 * a.fy;
+  return c0 * ((R)1 - a.fz) + c1 * a.fz;
+}
+template <typename R> inline void mix3(V3<R> src, R srcAlpha, V3<R> &dst, R &dstAlpha) {
+  if (srcAlpha > (R)1e-6f) {
+    const R impact = ((R)1 - dstAlpha) * srcAlpha;
+    dst = (dst * dstAlpha + src * impact) / (dstAlpha + impact);
+    dstAlpha += impact;
+  }
+}
+// fmax / fmin (IEEE maxNum / minNum: a NaN operand yields the other one) as
+// fmaxf / fminf in the reference: rays with a zero direction component reach
+// the box test with inf * 0 = NaN terms
+template <typename R, class S> struct Marcher {
+  const S &G;
+  const Physics<R> &ph;
+  const dcg_render_params &rp;
+  R sdf(V3<R> p) const { return ph.scene_sdf(p.x, p.y, p.z); }
+  V3<R> normal(V3<R> p) const {
+    const R e = (R)1e-4f;
+    return normalize3(V3<R>{sdf({p.x + e, p.y, p.z}) - sdf({p.x - e, p.y, p.z}),
+                            sdf({p.x, p.y + e, p.z}) - sdf({p.x, p.y - e, p.z}),
+                            sdf({p.x, p.y, p.z + e}) - sdf({p.x, p.y, p.z - e})});
+  }
+  bool box_hit(R &dNear, R &dFar, V3<R> o, V3<R> dinv) const {
+    const R cx = (R)ph.gx * (R)0.5f, cy = (R)ph.gy * (R)0.5f, cz = (R)ph.gz * (R)0.5f;
+    const R nx = dinv.x * (o.x - cx), ny = dinv.y * (o.y - cy), nz = dinv.z * (o.z - cz);
+    const R kx = std::fabs(dinv.x) * cx, ky = std::fabs(dinv.y) * cy, kz = std::fabs(dinv.z) * cz;
+    dNear = std::fmax(std::fmax(-nx - kx, -ny - ky), -nz - kz);
+    dFar = std::fmin(std::fmin(-nx + kx, -ny + ky), -nz + kz);
+    return dNear < dFar && dFar > (R)0;
+  }
+  R alpha_of(R dist, R dens) const { return (R)1 - std::exp(-dist * ph.dx * dens); }
+  R light_march(V3<R> origin, V3<R> sun, V3<R> suninv) const {
+    R light = 1;
+    if (rp.solids && ph.P->solids) {
+      R dScene = 0;
+      for (int i = 0; i < 100; i++) {
+        const R s = sdf(origin + sun * dScene);
+        light = std::fmin(light, (s / dScene) / (R)0.06f);
+        if (light <= (R)1e-2f) return 0;
+        dScene += s;
+      }
+    }
+    if (rp.channel == DCG_RENDER_FLUID) {
+      R dNear, dFar;
+      if (box_hit(dNear, dFar, origin, suninv)) {
+        V3<R> pos = origin;
+        if (dNear > (R)0) {
+          pos = pos + sun * dNear;
+          dFar -= dNear;
+        }
+        const R step = std::fmax(dFar / (R)100, (R)1e-1f);
+        R dens = 0;
+        March<R> a;
+        for (R d = step; d < dFar && dens < (R)5; d += step) {
+          pos = pos + sun * step;
+          G.sample(pos, rp.precise != 0, a);
+          dens += a.density * ph.dx * step;
+        }
+        light *= std::exp(-dens);
+      }
+    }
+    return light;
+  }
+  void march(V3<R> origin, V3<R> dir, V3<R> sun, R out[4]) const {
+    const R ambient = (R)rp.ambient, ambInv = (R)1 - ambient;
+    const R floorLight = std::fmax((R)0, sun.y);
+    const R sliceZ = (R)ph.gz * (R)0.5f;
+    const V3<R> dinv{(R)1 / dir.x, (R)1 / dir.y, (R)1 / dir.z}, suninv{(R)1 / sun.x, (R)1 / sun.y, (R)1 / sun.z};
+    const V3<R> smoke{(R)rp.smoke_color[0], (R)rp.smoke_color[1], (R)rp.smoke_color[2]};
+    R dCurrent = 0, dSolid = (R)FLT_MAX, light;
+    V3<R> color{0, 0, 0};
+    R alpha = 0;
+    int what = 0;
+    if (rp.channel != DCG_RENDER_FLUID && (sliceZ - origin.z) * dir.z > (R)0) {
+      const R d = (sliceZ - origin.z) / dir.z;
+      const R px = origin.x + d * dir.x, py = origin.y + d * dir.y;
+      if (px >= (R)0 && py >= (R)0 && px < (R)ph.gx && py < (R)ph.gy && d < dSolid) {
+        dSolid = d;
+        what = 3;
+      }
+    }
+    if (rp.solids && ((R)0 - origin.y) * dir.y > (R)0) {
+      const R d = ((R)0 - origin.y) / dir.y;
+      if (d < dSolid) {
+        dSolid = d;
+        what = 2;
+      }
+    }
+    if (rp.solids && ph.P->solids) {
+      R s = (R)FLT_MAX, dScene = dCurrent;
+      for (int i = 0; i < 100; i++) {
+        s = sdf(origin + dir * dScene);
+        if (s < (R)1e-1f || dScene >= dSolid) break;
+        dScene += s;
+      }
+      if (s < (R)1e-1f && dScene < dSolid) {
+        dSolid = dScene;
+        what = 1;
+      }
+    }
+    March<R> a;
+    if (rp.channel == DCG_RENDER_FLUID) {
+      R dNear, dFar;
+      if (box_hit(dNear, dFar, origin, dinv)) {
+        dCurrent = std::fmax(dCurrent, std::fmax(dNear, (R)10));
+        V3<R> pos = origin + dir * dCurrent;
+        const R dMax = std::fmin(dFar, dSolid);
+        while (dCurrent < dMax && alpha <= (R)0.99f) {
+          const V3<R> prev = pos;
+          dCurrent = std::fmin(std::fmax(dCurrent * (R)1, dCurrent + (R)0.5f), dMax);
+          pos = origin + dir * dCurrent;
+          G.sample((prev + pos) * (R)0.5f, rp.precise != 0, a);
+          if (a.density > (R)1e-6f) {
+            const R sa = alpha_of(len3(pos - prev), a.density);
+            light = 1;
+            if (rp.shadows) light *= light_march((prev + pos) * (R)0.5f, sun, suninv);
+            light = ambient + light * ambInv;
+            mix3(smoke * light, sa, color, alpha);
+          }
+        }
+      }
+    }
+    V3<R> pos = origin + dir * dSolid;
+    const R bgAlpha = alpha_of(dSolid, (R)1e-6f);
+    if (what == 1) {
+      light = std::fmax((R)0, dot3(normal(pos), sun));
+      if (rp.shadows) light *= light_march(pos, sun, suninv);
+      light = ambient + light * ambInv;
+      mix3(V3<R>{(R)rp.scene_color[0], (R)rp.scene_color[1], (R)rp.scene_color[2]} * light, (R)1 - bgAlpha, color,
+           alpha);
+    }
+    if (what == 2) {
+      pos.y = 0;
+      light = floorLight;
+      if (rp.shadows) light *= light_march(pos, sun, suninv);
+      light = ambient + light * ambInv;
+      light *= (R)1 + (R)0.1f * std::fmod(std::fabs(std::floor(pos.x / (R)ph.gx) + std::floor(pos.z / (R)ph.gx)), (R)2);
+      mix3(V3<R>{(R)rp.floor_color[0], (R)rp.floor_color[1], (R)rp.floor_color[2]} * light, (R)1 - bgAlpha, color,
+           alpha);
+    }
+    if (what == 3) {
+      pos.z = sliceZ;
+      G.sample(pos, rp.precise != 0, a);
+      if (rp.channel == DCG_RENDER_DENSITY) mix3(V3<R>{a.density * (R)1e2f, 0, 0}, (R)1, color, alpha);
+      if (rp.channel == DCG_RENDER_VELOCITY) {
+        const R v = G.vel_len(a) * (R)1e-1f;
+        mix3(V3<R>{v - (R)2, v - (R)1, v}, (R)1, color, alpha);
+      }
+      if (rp.channel == DCG_RENDER_RESOLUTION) {
+        const R c = (R)((a.ix / 4 + a.iy / 4) % 2);
+        mix3(V3<R>{c, c, c}, (R)1, color, alpha);
+      }
+      if (rp.channel == DCG_RENDER_FLUIDITY) {
+        const R f = G.fluid(a);
+        mix3(V3<R>{f, f, f}, (R)1, color, alpha);
+      }
+    }
+    out[0] = color.x; out[1] = color.y; out[2] = color.z; out[3] = alpha;
+  }
+  void image(double *out) const {
+    const R cx = (R)0.5f * (R)rp.width, cy = (R)0.5f * (R)rp.height;
+    const R s = (R)rp.fov / std::fmax(cx, cy);
+    const R step = (R)1 / (R)rp.aa_samples;
+    const V3<R> origin = V3<R>{(R)rp.eye[0], (R)rp.eye[1], (R)rp.eye[2]} * ph.rdx;
+    const V3<R> sun{(R)rp.sun_dir[0], (R)rp.sun_dir[1], (R)rp.sun_dir[2]};
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int y = 0; y < rp.height; y++)
+      for (int x = 0; x < rp.width; x++) {
+        R acc[4] = {0, 0, 0, 0};
+        for (R dx = 0; dx < (R)1; dx += step)
+          for (R dy = 0; dy < (R)1; dy += step) {
+            const V3<R> v = normalize3(V3<R>{((R)x + dx - cx) * s, ((R)y + dy - cy) * s, (R)1});
+            const V3<R> dir{v.x, v.z * (R)rp.eye_dir[1] - v.y * (R)rp.eye_dir[2],
+                            v.y * (R)rp.eye_dir[1] + v.z * (R)rp.eye_dir[2]};
+            R c[4];
+            march(origin, dir, sun, c);
+            for (int k = 0; k < 4; k++) acc[k] += c[k];
+          }
+        for (int k = 0; k < 4; k++) out[((size_t)y * rp.width + x) * 4 + k] = (double)(acc[k] * (step * step));
+      }
   }
 };
 
@@ -1354,6 +1569,47 @@ template <typename R> struct DC : Base {
           lam_cells[(size_t)b * BV + local_of(lx, ly, lz)] += lam_dense[((size_t)z * gy + y) * gx + x];
         }
   }
+  // ---------------- renderer samplers (dcgrid_rendering.cu:6-56) ----------------
+  struct Sampler {
+    const DC &d;
+    void sample(V3<R> p, bool precise, March<R> &a) const {
+      a.ix = clampi((int)std::floor(p.x), 0, d.gx - 1);
+      a.iy = clampi((int)std::floor(p.y), 0, d.gy - 1);
+      a.iz = clampi((int)std::floor(p.z), 0, d.gz - 1);
+      int level = 0;
+      const int64_t b = d.deep(a.ix, a.iy, a.iz, level);
+      if (!precise) {
+        const int sh = d.P.ref_compat ? 0 : level;  // the reference uses the finest coordinates mod 4
+        const size_t c = (size_t)b * BV + local_of((a.ix >> sh) & 3, (a.iy >> sh) & 3, (a.iz >> sh) & 3);
+        for (int k = 0; k < 8; k++) a.idx[k] = c;
+        a.fx = a.fy = a.fz = 0;
+        a.density = d.q[0][c];
+        return;
+      }
+      const R si = (R)1 / (R)(1 << level);
+      const R x = p.x * si - (R)0.5f, y = p.y * si - (R)0.5f, z = p.z * si - (R)0.5f;
+      const R xf = std::floor(x), yf = std::floor(y), zf = std::floor(z);
+      a.fx = x - xf; a.fy = y - yf; a.fz = z - zf;
+      const int i = (int)xf + 1 - d.bx[b], j = (int)yf + 1 - d.by[b], k = (int)zf + 1 - d.bz[b];
+      const int64_t *ap = &d.apron[(size_t)b * AV + AA * i + AW * j + k];
+      a.idx[0] = ap[0]; a.idx[1] = ap[1]; a.idx[2] = ap[AW]; a.idx[3] = ap[AW + 1];
+      a.idx[4] = ap[AA]; a.idx[5] = ap[AA + 1]; a.idx[6] = ap[AA + AW]; a.idx[7] = ap[AA + AW + 1];
+      a.density = interp(a, [&](size_t c) { return d.q[0][c]; });
+    }
+    R vel_len(const March<R> &a) const {
+      const R vx = interp(a, [&](size_t c) { return d.v[0][c]; });
+      const R vy = interp(a, [&](size_t c) { return d.v[1][c]; });
+      const R vz = interp(a, [&](size_t c) { return d.v[2][c]; });
+      return std::sqrt(vx * vx + vy * vy + vz * vz);
+    }
+    R fluid(const March<R> &a) const { return interp(a, [&](size_t c) { return d.w[c]; }); }
+  };
+  int render(const dcg_render_params &rp, double *out) const override {
+    Sampler S{*this};
+    Marcher<R, Sampler>{S, ph, rp}.image(out);
+    return DCG_OK;
+  }
+
   // this simulation takes another one's whole state (same parameters)
   void copy_state_from(const DC &o) {
     *this = o;
@@ -1802,6 +2058,51 @@ template <typename R> struct UG : Base {
     return DCG_OK;
   }
   int get_dense(int f, double *dst) override { return get_field(f, dst); }
+  // ---------------- renderer samplers (uniformgrid_rendering.cu:5-52) ----------------
+  struct Sampler {
+    const UG &u;
+    void sample(V3<R> p, bool precise, March<R> &a) const {
+      if (!precise) {
+        a.ix = clampi((int)p.x, 0, u.gx - 1);
+        a.iy = clampi((int)p.y, 0, u.gy - 1);
+        a.iz = clampi((int)p.z, 0, u.gz - 1);
+        const size_t c = u.idx3(a.ix, a.iy, a.iz);
+        for (int k = 0; k < 8; k++) a.idx[k] = c;
+        a.fx = a.fy = a.fz = 0;
+        a.density = u.q[0][c];
+        return;
+      }
+      const R x = p.x - (R)0.5f, y = p.y - (R)0.5f, z = p.z - (R)0.5f;
+      const R xf = std::floor(x), yf = std::floor(y), zf = std::floor(z);
+      a.ix = (int)xf; a.iy = (int)yf; a.iz = (int)zf;
+      a.fx = x - xf; a.fy = y - yf; a.fz = z - zf;
+      const int x0 = clampi(a.ix, 0, u.gx - 1), y0 = clampi(a.iy, 0, u.gy - 1), z0 = clampi(a.iz, 0, u.gz - 1);
+      const size_t xs = a.ix < u.gx - 1 ? 1 : 0, ys = a.iy < u.gy - 1 ? (size_t)u.gx : 0,
+                   zs = a.iz < u.gz - 1 ? (size_t)u.gx * u.gy : 0;
+      a.idx[0] = u.idx3(x0, y0, z0);
+      a.idx[1] = a.idx[0] + zs;
+      a.idx[2] = a.idx[0] + ys;
+      a.idx[3] = a.idx[1] + ys;
+      a.idx[4] = a.idx[0] + xs;
+      a.idx[5] = a.idx[4] + zs;
+      a.idx[6] = a.idx[4] + ys;
+      a.idx[7] = a.idx[6] + zs;
+      a.density = interp(a, [&](size_t c) { return u.q[0][c]; });
+    }
+    R vel_len(const March<R> &a) const {
+      const R vx = interp(a, [&](size_t c) { return u.v[0][c]; });
+      const R vy = interp(a, [&](size_t c) { return u.v[1][c]; });
+      const R vz = interp(a, [&](size_t c) { return u.v[2][c]; });
+      return std::sqrt(vx * vx + vy * vy + vz * vz);
+    }
+    R fluid(const March<R> &a) const { return interp(a, [&](size_t c) { return u.w[c]; }); }
+  };
+  int render(const dcg_render_params &rp, double *out) const override {
+    Sampler S{*this};
+    Marcher<R, Sampler>{S, ph, rp}.image(out);
+    return DCG_OK;
+  }
+
   void info(dcg_info *i) const override {
     std::memset(i, 0, sizeof(*i));
     i->mode = DCG_MODE_UNIFORM;
@@ -2010,6 +2311,10 @@ int dcgo_set_emission(dcgo_sim *s, const double *src) {
   return s && src ? s->impl->set_emission(src) : DCG_E_INVALID;
 }
 int dcgo_get_stats(dcgo_sim *s, dcg_stats *st) { return s && st ? s->impl->stats(st) : DCG_E_INVALID; }
+int dcgo_render(dcgo_sim *s, const dcg_render_params *rp, double *rgba) {
+  if (!s || !rp || !rgba || rp->width <= 0 || rp->height <= 0 || rp->aa_samples < 1) return DCG_E_INVALID;
+  return s->impl->render(*rp, rgba);
+}
 int dcgo_adjoint_step(dcgo_sim *s, const double *lam_in, double *lam_out, double *lam_em) {
   if (!lam_in || !lam_out) return DCG_E_INVALID;
   return with_dc(s, [&](auto &d) {

@@ -54,6 +54,7 @@ def lib():
         L.dcgo_get_scores.argtypes = [vp, vp, vp]
         L.dcgo_get_stats.argtypes = [vp, C.POINTER(capi.DcgStats)]
         L.dcgo_set_emission.argtypes = [vp, vp]
+        L.dcgo_render.argtypes = [vp, C.POINTER(capi.DcgRenderParams), vp]
         L.dcgo_adjoint_step.argtypes = [vp, vp, vp, vp]
         L.dcgo_adjoint_dense.argtypes = [vp, vp, vp]
         L.dcgo_copy_state.argtypes = [vp, vp]
@@ -203,6 +204,11 @@ class OracleSim:
         st = capi.DcgStats()
         self._chk(self.L.dcgo_get_stats(self.h, C.byref(st)), "stats")
         return st
+
+    def render(self, rp):
+        out = np.empty((rp.height, rp.width, 4), np.float64)
+        self._chk(self.L.dcgo_render(self.h, C.byref(rp), _ptr(out)), "render")
+        return out
 
     def adjoint_step(self, lam_in, lam_em=None):
         """FP64 transpose of the step that produced the current state; returns

@@ -35,6 +35,7 @@ def test_struct_layouts(dcg_lib):
     assert dcg_lib.dcg_sizeof_stats() == C.sizeof(capi.DcgStats)
     dcg_lib.dcg_sizeof_tuning.restype = C.c_size_t
     assert dcg_lib.dcg_sizeof_tuning() == C.sizeof(capi.DcgTuning)
+    assert dcg_lib.dcg_sizeof_render_params() == C.sizeof(capi.DcgRenderParams)
 
 
 def test_python_defaults_match_c_defaults(dcg_lib):
