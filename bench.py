@@ -282,7 +282,7 @@ def run_batch(args, ctx):
         return b, tune
 
     def batch_cells(b):
-        return sum(m.stats().active_cells for m in b)
+        return sum(st.active_cells for st in b.stats())
 
     # mixed-precision batch: the headline
     bm, tune_m = make_batch(capi.PRECISION_MIXED_FP16)
@@ -343,7 +343,7 @@ def run_batch(args, ctx):
     e2e = {"value": e2e_cells / (e2e_ms * 1e-3), "unit": METRIC,
            "h2d_bytes_per_step": 4 * EM_N ** 3 * BATCH_N, "d2h_bytes_per_step": stats_bytes * BATCH_N,
            "note": "per step: dcg_set_emission of each member from pinned host memory, dcg_batch_step, "
-                   "dcg_get_stats of each member; host clock"}
+                   "dcg_batch_get_stats (every member's statistics); host clock"}
 
     # roofline of the dominant kernel: the batched cooperative cascade
     peak, peak_kind = peaks()

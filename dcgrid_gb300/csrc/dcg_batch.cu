@@ -36,6 +36,14 @@ struct dcg_batch {
   int solve_grid = 0;
   std::map<int, cudaGraphExec_t> graphs;
   long long kernels_per_step = 0;
+  // pinned staging of the members' statistics: red[32] doubles, ctr[C_COUNT]
+  // and load[MAXL] counters, the error word
+  struct StatStage {
+    double red[32];
+    long long ctr[C_COUNT], load[MAXL];
+    uint32_t err, pad;
+  };
+  StatStage *stage = nullptr;
 
   int fail(int code, const std::string &msg) {
     err = msg;
@@ -68,6 +76,7 @@ struct dcg_batch {
     for (cudaStream_t a : aux) cudaStreamDestroy(a);
     for (cudaEvent_t e : joins) cudaEventDestroy(e);
     if (fork) cudaEventDestroy(fork);
+    if (stage) cudaFreeHost(stage);
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
 
@@ -316,6 +325,44 @@ struct dcg_batch {
     return DCG_OK;
   }
 
+  // every member's statistics with one launch per group and one synchronisation
+  int get_stats(dcg_stats *out) {
+    int rc;
+    if (!stage && (rc = cuda(cudaMallocHost(&stage, sizeof(StatStage) * n()), "stats staging"))) return rc;
+    for (dcg_sim *s : m) cudaMemsetAsync(s->D.red, 0, sizeof(double) * 32, stream);
+    for (int g = 0; g < groups(); g++) {
+      CellBatch P{};
+      P.n = std::min(BMAX, n() - g * BMAX);
+      for (int i = 0; i < P.n; i++) P.d[i] = m[g * BMAX + i]->D;
+      launch_cells_batch(4, P, 4, stream);
+    }
+    for (int i = 0; i < n(); i++) {
+      const Dev &D = m[i]->D;
+      cudaMemcpyAsync(stage[i].red, D.red, sizeof(stage[i].red), cudaMemcpyDeviceToHost, stream);
+      cudaMemcpyAsync(stage[i].ctr, D.ctr, sizeof(stage[i].ctr), cudaMemcpyDeviceToHost, stream);
+      cudaMemcpyAsync(stage[i].load, D.load, sizeof(stage[i].load), cudaMemcpyDeviceToHost, stream);
+      cudaMemcpyAsync(&stage[i].err, D.err, 4, cudaMemcpyDeviceToHost, stream);
+    }
+    if ((rc = cuda(cudaStreamSynchronize(stream), "stats"))) return rc;
+    for (int i = 0; i < n(); i++) {
+      dcg_stats &st = out[i];
+      std::memset(&st, 0, sizeof st);
+      const StatStage &x = stage[i];
+      st.steps = m[i]->steps;
+      st.residual = x.red[0];
+      st.mass = x.red[1];
+      for (int l = 0; l < m[i]->D.g.levels; l++) {
+        st.load[l] = x.load[l];
+        st.leaf_cells[l] = (int64_t)x.red[2 + l];
+        st.active_cells += st.leaf_cells[l];
+      }
+      st.moved_blocks = x.ctr[C_MOVES];
+      st.refined_subblocks = x.ctr[C_REFINES];
+      st.device_error = x.err;
+    }
+    return DCG_OK;
+  }
+
   int time_solve(int reps, float *avg_ms, double *bytes_out) {
     int rc;
     if ((rc = sync())) return rc;
@@ -480,6 +527,10 @@ int dcg_batch_get_info(const dcg_batch *b, int32_t *n, int64_t *device_bytes, in
 int dcg_batch_time_solve(dcg_batch *b, int32_t reps, float *avg_ms, double *bytes) {
   if (bad(b) || reps <= 0 || !avg_ms) return DCG_E_INVALID;
   return b->time_solve(reps, avg_ms, bytes);
+}
+int dcg_batch_get_stats(dcg_batch *b, dcg_stats *out) {
+  if (bad(b) || !out) return DCG_E_INVALID;
+  return b->get_stats(out);
 }
 const char *dcg_batch_last_error_string(const dcg_batch *b) { return b ? b->err.c_str() : "null handle"; }
 size_t dcg_sizeof_tuning(void) { return sizeof(dcg_tuning); }

@@ -519,4 +519,46 @@ __device__ inline void back_trace(const Dev &D, int4 bp, int c, size_t cell, flo
   pz = ((float)(bp.z + lz) + 0.5f) * scale - D.v[2][cell] * alpha;
 }
 
+// ---------------------------------------------------------------- statistics
+// k_dcgrid_debug_stats (dcgrid_structure.cu:224-251) for one cell of block b,
+// plus mass and leaf counts, reduced per warp into D.red (every lane of the
+// warp calls this; a warp covers half of one block).
+__device__ inline void stats_cell(const Dev &D, long long b, int c) {
+  double res = 0.0, mass = 0.0;
+  int lev = -1;
+  if (b < D.g.B) {
+    const int4 bp = D.pos[b];
+    const size_t cell = (size_t)b * BV + c;
+    if (bp.w >= 0 && D.child[cell >> 3] == NONE) {
+      lev = bp.w;
+      int lx, ly, lz;
+      local_xyz(c, lx, ly, lz);
+      const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+      const int scale = 1 << bp.w;
+      const double alpha = (double)D.ph.rdx * (double)D.ph.rdx / (double)(scale * scale);
+      const float *P = D.p;
+      const double lap = (double)P[apron_cell(D, (uint32_t)b, bp, ax - 1, ay, az)] +
+                         P[apron_cell(D, (uint32_t)b, bp, ax + 1, ay, az)] +
+                         P[apron_cell(D, (uint32_t)b, bp, ax, ay - 1, az)] +
+                         P[apron_cell(D, (uint32_t)b, bp, ax, ay + 1, az)] +
+                         P[apron_cell(D, (uint32_t)b, bp, ax, ay, az - 1)] +
+                         P[apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1)] - 6.0 * P[cell];
+      res = (double)scale * fabs((double)D.div[cell] - lap * alpha);
+      mass = (double)q_ld(D, 0, cell) * (double)D.w[cell] * scale * scale * scale;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    res += __shfl_xor_sync(0xffffffffu, res, o);
+    mass += __shfl_xor_sync(0xffffffffu, mass, o);
+  }
+  // a warp covers half of one block, so all its leaf cells share one level
+  const unsigned leafmask = __ballot_sync(0xffffffffu, lev >= 0);
+  const int lvl0 = __shfl_sync(0xffffffffu, lev, leafmask ? __ffs(leafmask) - 1 : 0);
+  if ((threadIdx.x & 31) == 0) {
+    if (res != 0.0) atomicAdd(&D.red[0], res);
+    if (mass != 0.0) atomicAdd(&D.red[1], mass);
+    if (leafmask) atomicAdd(&D.red[2 + lvl0], (double)__popc(leafmask));
+  }
+}
+
 }  // namespace dcg

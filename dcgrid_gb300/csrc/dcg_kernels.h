@@ -42,7 +42,8 @@ void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int gr
 // Member devices travel in the kernel parameters (__grid_constant__, read
 // through the constant cache); BMAX members fit the 32 KB parameter space.
 constexpr int BMAX = 16;
-// cell stages: 0 advect velocity, 1 advect scalars, 2 divergence, 3 apply pressure
+// cell stages: 0 advect velocity, 1 advect scalars, 2 divergence, 3 apply
+// pressure, 4 statistics (into each member's red; zero it first)
 struct CellBatch {
   int n, pad;
   long long end[BMAX];  // cumulative CTA count of members 0..s

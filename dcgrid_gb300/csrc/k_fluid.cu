@@ -543,7 +543,8 @@ __global__ void __launch_bounds__(64 * TB) k_cells_batch(const __grid_constant__
   if (STAGE == 0) advect_velocity_cell(D, b, c);
   else if (STAGE == 1) advect_scalars_cell(D, b, c);
   else if (STAGE == 2) divergence_cell(D, b, c);
-  else apply_pressure_cell(D, b, c);
+  else if (STAGE == 3) apply_pressure_cell(D, b, c);
+  else stats_cell(D, b, c);
 }
 
 __global__ void __launch_bounds__(256) k_restrict_batch(const __grid_constant__ RestrictBatch P) {
@@ -849,7 +850,8 @@ static void cells_batch_tb(int stage, const CellBatch &P, unsigned grid, cudaStr
     case 0: k_cells_batch<TB, 0><<<grid, 64 * TB, 0, st>>>(P); break;
     case 1: k_cells_batch<TB, 1><<<grid, 64 * TB, 0, st>>>(P); break;
     case 2: k_cells_batch<TB, 2><<<grid, 64 * TB, 0, st>>>(P); break;
-    default: k_cells_batch<TB, 3><<<grid, 64 * TB, 0, st>>>(P); break;
+    case 3: k_cells_batch<TB, 3><<<grid, 64 * TB, 0, st>>>(P); break;
+    default: k_cells_batch<TB, 4><<<grid, 64 * TB, 0, st>>>(P); break;
   }
 }
 void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st) {

@@ -575,43 +575,7 @@ void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *
 // k_dcgrid_debug_stats (dcgrid_structure.cu:224-251) plus mass and leaf
 // counts; warp-shuffle reductions, one double atomic per warp.
 __global__ void __launch_bounds__(256) k_stats(Dev D) {
-  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
-  double res = 0.0, mass = 0.0;
-  int lev = -1;
-  if (b < D.g.B) {
-    const int4 bp = D.pos[b];
-    const int c = threadIdx.x & 63;
-    const size_t cell = (size_t)b * BV + c;
-    if (bp.w >= 0 && D.child[cell >> 3] == NONE) {
-      lev = bp.w;
-      int lx, ly, lz;
-      local_xyz(c, lx, ly, lz);
-      const int ax = lx + 1, ay = ly + 1, az = lz + 1;
-      const int scale = 1 << bp.w;
-      const double alpha = (double)D.ph.rdx * (double)D.ph.rdx / (double)(scale * scale);
-      const float *P = D.p;
-      const double lap = (double)P[apron_cell(D, (uint32_t)b, bp, ax - 1, ay, az)] +
-                         P[apron_cell(D, (uint32_t)b, bp, ax + 1, ay, az)] +
-                         P[apron_cell(D, (uint32_t)b, bp, ax, ay - 1, az)] +
-                         P[apron_cell(D, (uint32_t)b, bp, ax, ay + 1, az)] +
-                         P[apron_cell(D, (uint32_t)b, bp, ax, ay, az - 1)] +
-                         P[apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1)] - 6.0 * P[cell];
-      res = (double)scale * fabs((double)D.div[cell] - lap * alpha);
-      mass = (double)q_ld(D, 0, cell) * (double)D.w[cell] * scale * scale * scale;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    res += __shfl_xor_sync(0xffffffffu, res, o);
-    mass += __shfl_xor_sync(0xffffffffu, mass, o);
-  }
-  // a warp covers half of one block, so all its leaf cells share one level
-  const unsigned leafmask = __ballot_sync(0xffffffffu, lev >= 0);
-  const int lvl0 = __shfl_sync(0xffffffffu, lev, leafmask ? __ffs(leafmask) - 1 : 0);
-  if ((threadIdx.x & 31) == 0) {
-    if (res != 0.0) atomicAdd(&D.red[0], res);
-    if (mass != 0.0) atomicAdd(&D.red[1], mass);
-    if (leafmask) atomicAdd(&D.red[2 + lvl0], (double)__popc(leafmask));
-  }
+  stats_cell(D, (long long)blockIdx.x * 4 + (threadIdx.x >> 6), threadIdx.x & 63);
 }
 void launch_stats(const Dev &D, cudaStream_t st) {
   cudaMemsetAsync(D.red, 0, sizeof(double) * 32, st);

@@ -80,6 +80,7 @@ def lib():
         L.dcg_batch_set_tuning.argtypes = [vp, C.POINTER(capi.DcgTuning)]
         L.dcg_batch_get_info.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.dcg_batch_time_solve.argtypes = [vp, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_double)]
+        L.dcg_batch_get_stats.argtypes = [vp, vp]
         L.dcg_batch_last_error_string.argtypes = [vp]
         L.dcg_batch_last_error_string.restype = C.c_char_p
         for name in ["dcg_sizeof_params", "dcg_sizeof_info", "dcg_sizeof_stats", "dcg_sizeof_tuning",
@@ -506,6 +507,12 @@ class Batch:
         n, nb, nl = C.c_int32(), C.c_int64(), C.c_int64()
         self._chk(self.L.dcg_batch_get_info(self.h, C.byref(n), C.byref(nb), C.byref(nl)), "get_info")
         return {"n": n.value, "device_bytes": nb.value, "launches_per_step": nl.value}
+
+    def stats(self):
+        """dcg_get_stats of every member, with one synchronisation."""
+        arr = (capi.DcgStats * len(self.members))()
+        self._chk(self.L.dcg_batch_get_stats(self.h, C.cast(arr, C.c_void_p)), "stats")
+        return list(arr)
 
     def time_solve(self, reps=5):
         ms, b = C.c_float(), C.c_double()

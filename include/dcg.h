@@ -325,6 +325,9 @@ int dcg_batch_autotune(dcg_batch *batch, int32_t spinup_steps, int32_t reps, dcg
 int dcg_batch_get_tuning(const dcg_batch *batch, dcg_tuning *out);
 int dcg_batch_set_tuning(dcg_batch *batch, const dcg_tuning *tuning);
 int dcg_batch_get_info(const dcg_batch *batch, int32_t *n, int64_t *device_bytes, int64_t *launches_per_step);
+/* dcg_get_stats of every member (out: n entries), one launch per group of 16
+ * members and one synchronisation */
+int dcg_batch_get_stats(dcg_batch *batch, dcg_stats *out);
 /* Times the pressure cascade of the current state (all rounds, the members'
  * jacobi_iters sweeps each) `reps` times; *bytes = algorithmic bytes of one
  * cascade, 12 per cell-sweep (p read, div read, p~ write). Leaves p and p~ in

@@ -140,3 +140,12 @@ def test_time_solve_reports_bytes():
     b = batch_run(params, 2)
     ms, nbytes = b.time_solve(3)
     assert ms > 0 and nbytes > 0
+
+
+def test_batch_stats_equal_member_stats():
+    params = small_batch(4, 6)
+    b = batch_run(params, 3)
+    for st, m in zip(b.stats(), b):
+        one = m.stats()
+        assert st.active_cells == one.active_cells and list(st.load) == list(one.load)
+        assert st.mass == pytest.approx(one.mass, rel=1e-12) and st.residual == pytest.approx(one.residual, rel=1e-9)
