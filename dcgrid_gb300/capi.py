@@ -98,7 +98,8 @@ class DcgParams(C.Structure):
         ("emission_n", C.c_int32),
         ("emission_band", C.c_float),
         ("src_jitter", C.c_float), ("src_jitter_seed", C.c_uint32),
-        ("reserved", C.c_int32 * 4),
+        ("defect_passes", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
 
@@ -119,6 +120,7 @@ class DcgStats(C.Structure):
         ("refined_subblocks", C.c_int64), ("steps", C.c_int64),
         ("residual", C.c_double), ("mass", C.c_double),
         ("device_error", C.c_uint32), ("pad", C.c_uint32),
+        ("defect_rel_residual", C.c_double * 2),
     ]
 
 
@@ -201,9 +203,9 @@ def params_to_dict(p):
 
 
 def params_from_dict(d):
-    """Inverse of params_to_dict. Dicts written before src_jitter and
-    src_jitter_seed took two of the six reserved words carry six zero
-    reserved entries; the extra zeros are dropped."""
+    """Inverse of params_to_dict. Dicts written before src_jitter,
+    src_jitter_seed and defect_passes took three of the six reserved words
+    carry more (zero) reserved entries; the extra zeros are dropped."""
     p = DcgParams()
     for k, v in d.items():
         if isinstance(v, (list, tuple)):

@@ -103,8 +103,9 @@ int dcg_set_params(dcg_sim *s, const dcg_params *p) {
   if (member_refused(s)) return DCG_E_INVALID;
   if (p->gx != s->P.gx || p->gy != s->P.gy || p->gz != s->P.gz || p->levels != s->P.levels ||
       p->max_blocks != s->P.max_blocks || p->n_scalars != s->P.n_scalars || p->precision != s->P.precision ||
-      p->ref_compat != s->P.ref_compat)
-    return s->fail(DCG_E_INVALID, "geometry, budget, scalars, precision and compat mode are fixed at creation");
+      p->ref_compat != s->P.ref_compat || p->defect_passes != s->P.defect_passes)
+    return s->fail(DCG_E_INVALID,
+                   "geometry, budget, scalars, precision, compat mode and defect passes are fixed at creation");
   if (p->jacobi_iters < 0 || (p->jacobi_iters & 1)) return s->fail(DCG_E_INVALID, "jacobi_iters must be even");
   if (p->emission_n != s->P.emission_n) return s->fail(DCG_E_INVALID, "emission_n is fixed at creation");
   const Phys before = s->mode == DCG_MODE_ADAPTIVE ? s->D.ph : s->U.ph;
@@ -411,6 +412,14 @@ int dcg_get_stats(dcg_sim *s, dcg_stats *st) {
     st->moved_blocks = ctr[C_MOVES];
     st->refined_subblocks = ctr[C_REFINES];
     st->device_error = e;
+    if (s->P.defect_passes > 0) {
+      const int K = s->P.defect_passes;
+      std::vector<double> dn(2 * (K + 1));
+      if ((rc = s->cuda(cudaMemcpy(dn.data(), s->D.dnorm, dn.size() * 8, cudaMemcpyDeviceToHost), "stats"))) return rc;
+      auto rel = [](double r2, double b2) { return b2 > 0 ? std::sqrt(r2 / b2) : 0.0; };
+      st->defect_rel_residual[0] = rel(dn[0], dn[1]);
+      st->defect_rel_residual[1] = rel(dn[2 * K], dn[2 * K + 1]);
+    }
   } else {
     launch_u_stats(s->U, s->stream);
     if ((rc = s->cuda(cudaMemcpyAsync(red, s->U.red, sizeof(red), cudaMemcpyDeviceToHost, s->stream), "stats"))) return rc;

@@ -403,9 +403,9 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
       delete b;
       return DCG_E_INVALID;  // one sweep schedule per batch
     }
-    if (params[i].max_blocks <= 0 || params[i].max_blocks >= (1ll << 28)) {
+    if (params[i].max_blocks <= 0 || params[i].max_blocks >= (1ll << 28) || params[i].defect_passes != 0) {
       delete b;
-      return DCG_E_INVALID;
+      return DCG_E_INVALID;  // defect correction runs on single simulations
     }
     b->arena_off.push_back(cells);
     cells += (unsigned long long)params[i].max_blocks * BV;

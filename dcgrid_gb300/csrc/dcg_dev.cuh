@@ -96,6 +96,8 @@ struct Dev {
   uint32_t *bar;           // grid barrier {arrivals, generation}
   uint32_t *epoch;         // per block: sweeps completed in the running level solve
   uint32_t *binfo;         // level solve: block descriptions of the running level (13 words per block)
+  float *rr, *e, *et;      // defect correction: residual, correction and its ping-pong plane
+  double *dnorm;           // defect correction: FP64 ||r||^2, ||div||^2 per pass
 };
 
 // Two-level grid barrier: CTAs arrive on one of 16 group counters (separate

@@ -34,6 +34,9 @@ void launch_divergence(const Dev &D, cudaStream_t st);
 void launch_jacobi(const Dev &D, int level, const float *src, float *dst, cudaStream_t st);
 void launch_prolongate(const Dev &D, int level, cudaStream_t st);
 void launch_apply_pressure(const Dev &D, cudaStream_t st);
+// defect correction: FP64 residual into D.rr (+ norms), p += e
+void launch_defect_residual(const Dev &D, double *norms, cudaStream_t st);
+void launch_add_correction(const Dev &D, cudaStream_t st);
 // cooperative persistent solve of one level (prolongation + sweeps)
 int level_solve_grid(int sms);
 void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int grid, int epoch_sync, cudaStream_t st);

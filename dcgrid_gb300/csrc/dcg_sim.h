@@ -178,6 +178,7 @@ struct dcg_sim {
     if (P.precision != DCG_PRECISION_FP32 && P.precision != DCG_PRECISION_MIXED &&
         P.precision != DCG_PRECISION_MIXED_FP16)
       return fail(DCG_E_INVALID, "unknown precision");
+    if (P.defect_passes < 0 || P.defect_passes > 16) return fail(DCG_E_INVALID, "defect_passes must be in [0, 16]");
     return DCG_OK;
   }
 
@@ -268,6 +269,12 @@ struct dcg_sim {
     if ((rc = alloc(&D.bar, 64 + 32 * 18))) return rc;
     if ((rc = alloc(&D.epoch, B))) return rc;
     if ((rc = alloc(&D.binfo, 13 * B))) return rc;
+    if (P.defect_passes > 0) {
+      if ((rc = alloc(&D.rr, nc))) return rc;
+      if ((rc = alloc(&D.e, nc))) return rc;
+      if ((rc = alloc(&D.et, nc))) return rc;
+      if ((rc = alloc(&D.dnorm, 2 * (P.defect_passes + 1)))) return rc;
+    }
     if (plan_only) return plan_tail_adaptive(B);
     ls_grid = level_solve_grid(sms);
     if (const char *m = std::getenv("DCG_SOLVE_SYNC"))
@@ -387,6 +394,7 @@ struct dcg_sim {
       const int sweeps = local ? 2 * P.jacobi_iters : P.jacobi_iters;
       if (ls_epoch == 3) {
         for (int l = top; l >= 0; l--) solve_staged(l, local ? 0 : 1, sweeps);
+        if (!local && P.defect_passes > 0) defect_correct(sweeps);
       } else {
         for (int l = top; l >= 0; l--)
           launch_level_solve(D, l, (!local && l < top) ? 1 : 0, sweeps, ls_grid, ls_epoch, stream);
@@ -439,21 +447,43 @@ struct dcg_sim {
     return s;
   }
 
+  // FP64 defect correction after the cascade: per pass the FP64 residual of
+  // every level's equations (norms into dnorm), the cascade on the residual
+  // into e, and p += e; a last residual measures the result
+  void defect_correct(int sweeps) {
+    const int K = P.defect_passes, top = D.g.levels - 1;
+    cudaMemsetAsync(D.dnorm, 0, sizeof(double) * 2 * (K + 1), stream);
+    for (int k = 0; k <= K; k++) {
+      launch_defect_residual(D, D.dnorm + 2 * k, stream);
+      if (k == K) break;
+      cudaMemsetAsync(D.e, 0, (size_t)D.g.B * BV * sizeof(float), stream);
+      for (int l = top; l >= 0; l--) solve_staged(l, 1, sweeps, D.e, D.et, D.rr);
+      launch_add_correction(D, stream);
+    }
+  }
+
   // one level of the cascade through the staged solve, as a batch of one
-  // (prolongation only below the coarsest level)
-  void solve_staged(int level, int prolong, int sweeps) {
+  // (prolongation only below the coarsest level), on p / p~ / div or on the
+  // given planes
+  void solve_staged(int level, int prolong, int sweeps, float *pp = nullptr, float *ppt = nullptr,
+                    float *pdiv = nullptr) {
     SolveBatch SB{};
     SB.n = 1;
     SB.maxtop = D.g.levels - 1;
     SB.prolong = prolong;
-    SB.p = D.p;
-    SB.pt = D.pt;
-    SB.div = D.div;
+    SB.p = pp ? pp : D.p;
+    SB.pt = ppt ? ppt : D.pt;
+    SB.div = pdiv ? pdiv : D.div;
     SB.binfo = D.binfo;
     SB.bar = D.bar;
     SB.err = D.err;
     SB.arena[0] = 0;
     SB.d[0] = D;
+    if (pp) {  // the prolongation and the cached alpha*div read these through D
+      SB.d[0].p = pp;
+      SB.d[0].pt = ppt;
+      SB.d[0].div = pdiv;
+    }
     launch_level_solve_batch(SB, SB.maxtop - level, sweeps, ls_grid_staged, 4, 1, stream);
   }
   void a_advect_scalars() {
@@ -467,6 +497,7 @@ struct dcg_sim {
   int create_uniform() {
     int rc = validate_common();
     if (rc) return rc;
+    if (P.defect_passes) return fail(DCG_E_INVALID, "defect correction is implemented for the adaptive grid");
     std::memset(&U, 0, sizeof(U));
     U.gx = P.gx; U.gy = P.gy; U.gz = P.gz;
     const int minDim = std::min(P.gx, std::min(P.gy, P.gz));

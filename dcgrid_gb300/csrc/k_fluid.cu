@@ -454,6 +454,47 @@ __device__ __forceinline__ void apply_pressure_cell(const Dev &D, long long b, i
   D.v[2][cell] = D.v[2][cell] - alpha * (W[F] * (P[F] - pc) + W[Bk] * (pc - P[Bk]));
 }
 
+// ---------------------------------------------------------------- defect correction
+// FP64 residual of every allocated cell's Jacobi equation (the fixed point of
+// k_jacobi: sum6 p - 6 p = alpha div, alpha = (2^L dx)^2 in float as there),
+// r = div - (sum6 p - 6 p) / alpha, stored in FP32, with FP64 sums of r^2 and
+// div^2 reduced per warp into norms[0..1].
+__global__ void __launch_bounds__(256) k_defect_residual(Dev D, double *norms) {
+  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+  double r2 = 0.0, b2 = 0.0;
+  if (b < D.g.B) {
+    const int4 bp = D.pos[b];
+    if (bp.w >= 0) {
+      const long long cell = b * BV + (threadIdx.x & 63);
+      const Nb6 n = jacobi_neighbours(D, cell);
+      const int s = 1 << bp.w;
+      const float alpha = (float)(s * s) * D.ph.dx * D.ph.dx;
+      const double lap = (double)D.p[n.i0] + (double)D.p[n.i1] + (double)D.p[n.i2] + (double)D.p[n.i3] +
+                         (double)D.p[n.i4] + (double)D.p[n.i5] - 6.0 * (double)D.p[cell];
+      const double dv = (double)D.div[cell];
+      const double r = dv - lap / (double)alpha;
+      D.rr[cell] = (float)r;
+      r2 = r * r;
+      b2 = dv * dv;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+    b2 += __shfl_xor_sync(0xffffffffu, b2, o);
+  }
+  if ((threadIdx.x & 31) == 0 && (r2 != 0.0 || b2 != 0.0)) {
+    atomicAdd(norms, r2);
+    atomicAdd(norms + 1, b2);
+  }
+}
+// p += e on every allocated cell
+__global__ void __launch_bounds__(256) k_add_correction(Dev D) {
+  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+  if (b >= D.g.B || D.pos[b].w < 0) return;
+  const long long cell = b * BV + (threadIdx.x & 63);
+  D.p[cell] = D.p[cell] + D.e[cell];
+}
+
 // ------------------------------------------------------------ single-simulation kernels
 // 256-thread CTAs, 4 blocks of 64 cells per CTA.
 __device__ __forceinline__ long long cta_block4() { return (long long)blockIdx.x * 4 + (threadIdx.x >> 6); }
@@ -491,6 +532,10 @@ void launch_jacobi(const Dev &D, int level, const float *src, float *dst, cudaSt
 void launch_prolongate(const Dev &D, int level, cudaStream_t st) {
   k_prolongate<<<cta_blocks(D.g.budget[level]), 256, 0, st>>>(D, level);
 }
+void launch_defect_residual(const Dev &D, double *norms, cudaStream_t st) {
+  k_defect_residual<<<cta_blocks(D.g.B), 256, 0, st>>>(D, norms);
+}
+void launch_add_correction(const Dev &D, cudaStream_t st) { k_add_correction<<<cta_blocks(D.g.B), 256, 0, st>>>(D); }
 void launch_apply_pressure(const Dev &D, cudaStream_t st) {
   k_apply_pressure<<<cta_blocks(D.g.B), 256, 0, st>>>(D);
 }

@@ -128,7 +128,13 @@ typedef struct dcg_params {
    * + src_jitter * u with u in [-1, 1) from the cell's level-local position */
   float src_jitter;
   uint32_t src_jitter_seed;
-  int32_t reserved[4];
+  /* extension: FP64 defect correction of the pressure solve. After the
+   * cascade, each pass computes the residual r = div - A p of every level's
+   * Jacobi equation in FP64 (with FP64 norms), solves A e = r with the same
+   * FP32 cascade, and adds e to p. 0 = the reference's cascade alone.
+   * Adaptive grid, single simulations. */
+  int32_t defect_passes;
+  int32_t reserved[3];
 } dcg_params;
 
 /* Fills *p with the reference's defaults (src/data/sim_params.cpp:4-34) for a
@@ -178,6 +184,9 @@ typedef struct dcg_stats {
   double mass;                 /* sum rho*fluidity*scale^3 over leaf cells     */
   uint32_t device_error;       /* device error word (DCG_DEVERR_* bits)         */
   uint32_t pad;
+  double defect_rel_residual[2]; /* FP64 ||r|| / ||div|| of the last projection's
+                                    equations before the first and after the last
+                                    defect-correction pass (0 without passes)   */
 } dcg_stats;
 
 enum {

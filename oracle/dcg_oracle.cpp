@@ -1063,9 +1063,8 @@ template <typename R> struct DC : Base {
     }
   }
   // FluidSimulationDCGrid::project (cu:270-294)
-  int project() override {
-    calc_divergence();
-    accumulate_div();
+  // the cascade of FluidSimulationDCGrid::project (cu:274-290) on p / pt / dv
+  void cascade() {
     const int pairs = P.jacobi_iters / 2;
     for (int i = 0; i < pairs; i++) {
       jacobi(levels - 1, p, pt);
@@ -1078,9 +1077,64 @@ template <typename R> struct DC : Base {
         jacobi(level, pt, p);
       }
     }
+  }
+  int project() override {
+    calc_divergence();
+    accumulate_div();
+    cascade();
+    if (P.defect_passes > 0) defect_correct();
     apply_pressure();
     accumulate_v();
     return DCG_OK;
+  }
+  // FP64 defect correction (extension): per pass the residual of every
+  // allocated cell's Jacobi equation, r = div - (sum6 p - 6 p) / alpha, in
+  // FP64 (stored in the field type), the cascade on r into e, p += e; a last
+  // residual measures the result. dnorm[2k], dnorm[2k+1]: ||r||^2, ||div||^2.
+  std::vector<R> e_, et_, rr_;
+  std::vector<double> dnorm;
+  void defect_correct() {
+    const size_t nc = (size_t)B * BV;
+    const int K = P.defect_passes;
+    e_.assign(nc, 0); et_.assign(nc, 0); rr_.assign(nc, 0);
+    dnorm.assign(2 * (K + 1), 0.0);
+    for (int k = 0; k <= K; k++) {
+      double r2 = 0, b2 = 0;
+      for (int64_t b = 0; b < B; b++) {
+        if (lvl[b] == FREE) continue;
+        const int s = 1 << lvl[b];
+        const R alpha = (R)(s * s) * ph.dx * ph.dx;
+        for (int c = 0; c < BV; c++) {
+          int lx, ly, lz;
+          local_xyz(c, lx, ly, lz);
+          const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+          const size_t cell = (size_t)b * BV + c;
+          const double lap = (double)p[apr(b, ax - 1, ay, az)] + (double)p[apr(b, ax + 1, ay, az)] +
+                             (double)p[apr(b, ax, ay - 1, az)] + (double)p[apr(b, ax, ay + 1, az)] +
+                             (double)p[apr(b, ax, ay, az - 1)] + (double)p[apr(b, ax, ay, az + 1)] -
+                             6.0 * (double)p[cell];
+          const double r = (double)dv[cell] - lap / (double)alpha;
+          rr_[cell] = (R)r;
+          r2 += r * r;
+          b2 += (double)dv[cell] * (double)dv[cell];
+        }
+      }
+      dnorm[2 * k] = r2;
+      dnorm[2 * k + 1] = b2;
+      if (k == K) break;
+      std::swap(p, e_);
+      std::swap(pt, et_);
+      std::swap(dv, rr_);
+      std::fill(p.begin(), p.end(), (R)0);
+      cascade();
+      std::swap(p, e_);
+      std::swap(pt, et_);
+      std::swap(dv, rr_);
+      for (int64_t b = 0; b < B; b++) {
+        if (lvl[b] == FREE) continue;
+        for (int c = 0; c < BV; c++) p[(size_t)b * BV + c] = p[(size_t)b * BV + c] + e_[(size_t)b * BV + c];
+      }
+    }
   }
   // FluidSimulationDCGrid::projectLocal (cu:296-311): 2x the pairs per level,
   // coarse to fine, no prolongation.
@@ -1664,6 +1718,12 @@ template <typename R> struct DC : Base {
     st->steps = steps;
     st->residual = res;
     st->mass = mass;
+    if (P.defect_passes > 0 && !dnorm.empty()) {
+      const int K = P.defect_passes;
+      auto rel = [](double r2, double b2) { return b2 > 0 ? std::sqrt(r2 / b2) : 0.0; };
+      st->defect_rel_residual[0] = rel(dnorm[0], dnorm[1]);
+      st->defect_rel_residual[1] = rel(dnorm[2 * K], dnorm[2 * K + 1]);
+    }
     return DCG_OK;
   }
   int64_t apron_mismatches() const {

@@ -78,6 +78,8 @@ SCENARIOS = {
     "ref_sphere": lambda: scenarios.sphere_obstacle(64, 128, 64, 3000),
     "ref_nocompat": lambda: (lambda p: (setattr(p, "ref_compat", 0), p)[1])(scenarios.ref_default(64, 128, 64, 3000)),
     "plume": lambda: scenarios.plume(32, 64, 32, None, 2, 20),
+    "plume_defect": lambda: (lambda p: (setattr(p, "defect_passes", 2), p)[1])(scenarios.plume(32, 64, 32, None, 2, 20)),
+    "cloud_defect": lambda: (lambda p: (setattr(p, "defect_passes", 1), p)[1])(scenarios.cloud(64, 1500, 3, 10, 0)),
     "plume_jitter": lambda: (lambda p: (setattr(p, "src_jitter", 3.0), setattr(p, "src_jitter_seed", 5), p)[2])(
         scenarios.plume(32, 64, 32, None, 2, 20)),
     "cloud": lambda: scenarios.cloud(64, 1500, 3, 10, 0),
@@ -251,3 +253,16 @@ def test_invalid_configurations_return_status():
     with pytest.raises(DcgError) as e:
         Simulation(p)
     assert e.value.code == capi.DCG_E_INVALID
+
+
+def test_defect_residuals_match_the_oracle():
+    p = scenarios.plume(32, 64, 32, None, 2, 20)
+    p.defect_passes = 3
+    g, o = gpu(p), orc(p)
+    for s in (g, o):
+        s.add_velocity_noise(5, 0.5)
+        s.step(2)
+    g.sync()
+    a, b = g.stats().defect_rel_residual, o.stats().defect_rel_residual
+    assert a[1] < a[0]
+    assert list(a) == pytest.approx(list(b), rel=1e-6)
