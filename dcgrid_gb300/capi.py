@@ -127,8 +127,8 @@ class DcgStats(C.Structure):
 class DcgTuning(C.Structure):
     _fields_ = [
         ("tile", C.c_int32 * 4), ("solve_cache", C.c_int32),
-        ("solve_ctas_per_sm", C.c_int32), ("solve_barrier", C.c_int32),
-        ("reserved", C.c_int32 * 5), ("solve_ms", C.c_float), ("cells_ms", C.c_float * 4),
+        ("solve_ctas_per_sm", C.c_int32), ("solve_barrier", C.c_int32), ("persistent", C.c_int32),
+        ("reserved", C.c_int32 * 4), ("solve_ms", C.c_float), ("cells_ms", C.c_float * 4),
     ]
 
 
@@ -147,7 +147,8 @@ class DcgRenderParams(C.Structure):
 
 def tuning_to_dict(t):
     return {"tile": list(t.tile), "solve_cache": t.solve_cache, "solve_ctas_per_sm": t.solve_ctas_per_sm,
-            "solve_barrier": t.solve_barrier, "solve_ms": t.solve_ms, "cells_ms": list(t.cells_ms)}
+            "solve_barrier": t.solve_barrier, "persistent": t.persistent, "solve_ms": t.solve_ms,
+            "cells_ms": list(t.cells_ms)}
 
 
 def default_params(gx, gy, gz, max_blocks):

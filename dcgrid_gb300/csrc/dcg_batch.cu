@@ -100,7 +100,7 @@ struct dcg_batch {
       CellBatch P{};
       P.n = std::min(BMAX, n() - g * BMAX);
       for (int i = 0; i < P.n; i++) P.d[i] = m[g * BMAX + i]->D;
-      launch_cells_batch(stage, P, tune.tile[stage], stream);
+      launch_cells_batch(stage, P, tune.tile[stage], stream, tune.persistent != 0);
     }
   }
   // field: 0 velocity, 1 scalars, 2 divergence
@@ -283,21 +283,36 @@ struct dcg_batch {
     if ((rc = reset())) return rc;
     if ((rc = step(spinup))) return rc;
     if ((rc = sync())) return rc;
-    // cell stages: every tile, each stage independently
+    // cell stages: every tile of each stage, launched one CTA per block or
+    // persistent; the launch form that gives the lower total is kept
     const int tiles[3] = {2, 4, 8};
     dcg_tuning best = tune;
-    for (int stage = 0; stage < 4; stage++) {
-      float best_ms = 1e30f;
-      for (int tile : tiles) {
-        tune.tile[stage] = tile;
-        const float ms = time_ms(reps, [&] { cells(stage); });
-        if (ms < best_ms) {
-          best_ms = ms;
-          best.tile[stage] = tile;
+    float total[2] = {0.f, 0.f};
+    int tile_of[2][4];
+    float ms_of[2][4];
+    for (int pers = 0; pers < 2; pers++) {
+      tune.persistent = pers;
+      for (int stage = 0; stage < 4; stage++) {
+        float best_ms = 1e30f;
+        for (int tile : tiles) {
+          tune.tile[stage] = tile;
+          const float ms = time_ms(reps, [&] { cells(stage); });
+          if (ms < best_ms) {
+            best_ms = ms;
+            tile_of[pers][stage] = tile;
+          }
         }
+        ms_of[pers][stage] = best_ms;
+        total[pers] += best_ms;
+        tune.tile[stage] = tile_of[pers][stage];
       }
-      best.cells_ms[stage] = best_ms;
-      tune.tile[stage] = best.tile[stage];
+    }
+    const int pick = total[1] < total[0] ? 1 : 0;
+    best.persistent = pick;
+    tune.persistent = pick;
+    for (int stage = 0; stage < 4; stage++) {
+      best.tile[stage] = tune.tile[stage] = tile_of[pick][stage];
+      best.cells_ms[stage] = ms_of[pick][stage];
     }
     // level solve: cache depth x CTAs per SM x barrier kind
     float best_solve = 1e30f;
@@ -334,7 +349,7 @@ struct dcg_batch {
       CellBatch P{};
       P.n = std::min(BMAX, n() - g * BMAX);
       for (int i = 0; i < P.n; i++) P.d[i] = m[g * BMAX + i]->D;
-      launch_cells_batch(4, P, 4, stream);
+      launch_cells_batch(4, P, 4, stream, tune.persistent != 0);
     }
     for (int i = 0; i < n(); i++) {
       const Dev &D = m[i]->D;

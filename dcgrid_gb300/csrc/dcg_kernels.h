@@ -70,7 +70,8 @@ struct SolveBatch {
   Dev d[BMAX];
 };
 static_assert(sizeof(RestrictBatch) < 32000 && sizeof(SolveBatch) < 32000, "kernel parameter space");
-void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st);
+// persistent: a grid of a few CTAs per SM over the allocated blocks only
+void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st, bool persistent = false);
 void launch_restrict_batch(RestrictBatch &P, cudaStream_t st);
 // CTAs of the batched solve for a cache depth (0, 4, 8) and CTAs per SM (0 = occupancy limit)
 int batch_solve_grid(int sms, int cache, int ctas_per_sm);

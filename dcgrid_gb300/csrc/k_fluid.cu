@@ -50,29 +50,53 @@ __device__ __forceinline__ void advect_velocity_cell(const Dev &D, long long b, 
 
 // k_dcgrid_advect_density (dcgrid_fluid.cu:129-144) for every scalar; sphere
 // sources (extension) overwrite leaf cells inside the source.
-__device__ __forceinline__ void advect_scalars_cell(const Dev &D, long long b, int c) {
+// Scalar storage with the format as a template argument (0 FP32, 1 BF16, 2 FP16).
+template <int MODE> __device__ __forceinline__ float q_ldm(const Dev &D, int k, size_t i) {
+  if (MODE == 0) return D.q[k][i];
+  return h16_to_f(D.qh[k][i], MODE);
+}
+template <int MODE> __device__ __forceinline__ void tq_stm(const Dev &D, int k, size_t i, float v) {
+  if (MODE == 0) D.tq[k][i] = v;
+  else D.tqh[k][i] = f_to_h16(v, MODE);
+}
+// q_bc decided once per stencil corner for all scalars: 0 the sampled value
+// passes, 1 inlet (density d_emit, other scalars 0), 2 zero
+__device__ __forceinline__ int q_bc_mode(const Geom &g, const Phys &P, int x, int y, int z, int scale) {
+  if (in_inlet(g, P, x, y, z, scale)) return 1;
+  if (P.wind && yz_inside(g, y, z, scale)) {
+    if (x < 0) return 2;
+    if (x * scale >= g.gx) return 0;
+  }
+  return outside(g, x, y, z, scale) ? 2 : 0;
+}
+
+template <int MODE, int NQ>
+__device__ __forceinline__ void advect_scalars_cell_t(const Dev &D, long long b, int c) {
   if (b >= D.g.B) return;
   const int4 bp = D.pos[b];
   if (bp.w < 0) return;
   const size_t cell = (size_t)b * BV + c;
-  const int nq = D.g.nq;
-  float o[3] = {0.f, 0.f, 0.f};
+  float o[NQ];
+#pragma unroll
+  for (int kq = 0; kq < NQ; kq++) o[kq] = 0.f;
   if (D.child[cell >> 3] == NONE) {
     float px, py, pz;
     back_trace(D, bp, c, cell, px, py, pz);
     Smp s;
     sample_at(D, (uint32_t)b, bp, px, py, pz, s);
     if (!(s.wAcc < 1e-6f)) {
-      for (int kq = 0; kq < nq; kq++) {
-        float acc = 0.f;
+      // per scalar the sum runs over the corners in order, as in
+      // k_dcgrid_advect_density (dcgrid_fluid.cu:129-144)
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
-          int x, y, z;
-          corner_of(s, k, x, y, z);
-          const float qc = q_bc(D.g, D.ph, q_ld(D, kq, s.idx[k]), kq, x, y, z, s.scale);
-          acc = (k == 0) ? qc * s.wt[0] : acc + qc * s.wt[k];
+      for (int k = 0; k < 8; k++) {
+        int x, y, z;
+        corner_of(s, k, x, y, z);
+        const int mode = q_bc_mode(D.g, D.ph, x, y, z, s.scale);
+#pragma unroll
+        for (int kq = 0; kq < NQ; kq++) {
+          const float qc = mode == 0 ? q_ldm<MODE>(D, kq, s.idx[k]) : (mode == 1 && kq == 0 ? D.ph.d_emit : 0.f);
+          o[kq] = (k == 0) ? qc * s.wt[0] : o[kq] + qc * s.wt[k];
         }
-        o[kq] = acc;
       }
     }
     int lx, ly, lz;
@@ -81,10 +105,24 @@ __device__ __forceinline__ void advect_scalars_cell(const Dev &D, long long b, i
       o[0] = o[0] + D.ph.dt * emission_at(D.g, D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w);
     if (D.ph.src) {
       if (in_source(D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w))
-        for (int kq = 0; kq < nq; kq++) o[kq] = src_value_at(D.ph, kq, bp.x + lx, bp.y + ly, bp.z + lz, bp.w);
+#pragma unroll
+        for (int kq = 0; kq < NQ; kq++) o[kq] = src_value_at(D.ph, kq, bp.x + lx, bp.y + ly, bp.z + lz, bp.w);
     }
   }
-  for (int kq = 0; kq < nq; kq++) tq_st(D, kq, cell, o[kq]);
+#pragma unroll
+  for (int kq = 0; kq < NQ; kq++) tq_stm<MODE>(D, kq, cell, o[kq]);
+}
+__device__ __forceinline__ void advect_scalars_cell(const Dev &D, long long b, int c) {
+  const int m = D.g.mixed;
+  if (D.g.nq == 3) {
+    if (m == 0) advect_scalars_cell_t<0, 3>(D, b, c);
+    else if (m == 1) advect_scalars_cell_t<1, 3>(D, b, c);
+    else advect_scalars_cell_t<2, 3>(D, b, c);
+  } else {
+    if (m == 0) advect_scalars_cell_t<0, 1>(D, b, c);
+    else if (m == 1) advect_scalars_cell_t<1, 1>(D, b, c);
+    else advect_scalars_cell_t<2, 1>(D, b, c);
+  }
 }
 
 // Source cells set on every leaf cell (used once at initialisation).
@@ -592,6 +630,50 @@ __global__ void __launch_bounds__(64 * TB) k_cells_batch(const __grid_constant__
   else stats_cell(D, b, c);
 }
 
+// Persistent form: a grid of a few CTAs per SM walks only the allocated
+// blocks. Segment (member m, level l) holds ceil(load_m[l] / TB) tiles of TB
+// blocks starting at off_m[l]; every CTA builds the cumulative tile counts in
+// shared memory from the device-side loads, then takes tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ...
+template <int TB, int STAGE>
+__global__ void __launch_bounds__(64 * TB) k_cells_persist(const __grid_constant__ CellBatch P) {
+  __shared__ long long s_end[BMAX * MAXL];
+  __shared__ long long s_cnt[BMAX * MAXL];
+  const int nseg = P.n * MAXL;
+  for (int i = threadIdx.x; i < nseg; i += blockDim.x) {
+    const Dev &D = P.d[i / MAXL];
+    const int l = i % MAXL;
+    const long long cnt = l < D.g.levels ? __ldcg(D.load + l) : 0;
+    s_cnt[i] = cnt;
+    s_end[i] = (cnt + TB - 1) / TB;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int i = 1; i < nseg; i++) s_end[i] += s_end[i - 1];
+  __syncthreads();
+  const long long total = s_end[nseg - 1];
+  const int c = threadIdx.x & 63;
+  for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (t < s_end[mid]) hi = mid;
+      else lo = mid + 1;
+    }
+    const Dev &D = P.d[lo / MAXL];
+    const int l = lo % MAXL;
+    const long long k = (t - (lo ? s_end[lo - 1] : 0)) * TB + (threadIdx.x >> 6);
+    // out-of-segment lanes get b = B: every body returns there (the statistics
+    // body still joins its warp reductions)
+    const long long b = k < s_cnt[lo] ? D.g.off[l] + k : D.g.B;
+    if (STAGE == 0) advect_velocity_cell(D, b, c);
+    else if (STAGE == 1) advect_scalars_cell(D, b, c);
+    else if (STAGE == 2) divergence_cell(D, b, c);
+    else if (STAGE == 3) apply_pressure_cell(D, b, c);
+    else stats_cell(D, b, c);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_restrict_batch(const __grid_constant__ RestrictBatch P) {
   const int s = batch_member(P.end, P.n, blockIdx.x);
   const Dev &D = P.d[s];
@@ -889,6 +971,27 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
   }
 }
 
+template <int TB, int STAGE> static unsigned persist_grid() {
+  static unsigned g = 0;
+  if (!g) {
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cells_persist<TB, STAGE>, 64 * TB, 0);
+    g = (unsigned)(sms * (occ > 0 ? occ : 1));
+  }
+  return g;
+}
+template <int TB>
+static void cells_persist_tb(int stage, const CellBatch &P, cudaStream_t st) {
+  switch (stage) {
+    case 0: k_cells_persist<TB, 0><<<persist_grid<TB, 0>(), 64 * TB, 0, st>>>(P); break;
+    case 1: k_cells_persist<TB, 1><<<persist_grid<TB, 1>(), 64 * TB, 0, st>>>(P); break;
+    case 2: k_cells_persist<TB, 2><<<persist_grid<TB, 2>(), 64 * TB, 0, st>>>(P); break;
+    case 3: k_cells_persist<TB, 3><<<persist_grid<TB, 3>(), 64 * TB, 0, st>>>(P); break;
+    default: k_cells_persist<TB, 4><<<persist_grid<TB, 4>(), 64 * TB, 0, st>>>(P); break;
+  }
+}
 template <int TB>
 static void cells_batch_tb(int stage, const CellBatch &P, unsigned grid, cudaStream_t st) {
   switch (stage) {
@@ -899,8 +1002,14 @@ static void cells_batch_tb(int stage, const CellBatch &P, unsigned grid, cudaStr
     default: k_cells_batch<TB, 4><<<grid, 64 * TB, 0, st>>>(P); break;
   }
 }
-void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st) {
+void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st, bool persistent) {
   if (tile != 2 && tile != 8) tile = 4;
+  if (persistent) {
+    if (tile == 2) cells_persist_tb<2>(stage, P, st);
+    else if (tile == 8) cells_persist_tb<8>(stage, P, st);
+    else cells_persist_tb<4>(stage, P, st);
+    return;
+  }
   long long acc = 0;
   for (int m = 0; m < P.n; m++) {
     acc += (P.d[m].g.B + tile - 1) / tile;

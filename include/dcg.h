@@ -311,7 +311,8 @@ typedef struct {
                                 shared memory: 0, 3, 4 or 8 (8 KB of shared memory each)    */
   int32_t solve_ctas_per_sm; /* CTAs per SM of the cooperative solve (0 = occupancy limit) */
   int32_t solve_barrier;     /* grid barrier between sweeps: 0 flat, 1 two-level            */
-  int32_t reserved[5];
+  int32_t persistent;        /* cell stages as persistent kernels over the allocated blocks */
+  int32_t reserved[4];
   float solve_ms;            /* autotune: measured time of the whole cascade (all rounds)  */
   float cells_ms[4];         /* autotune: measured time of each cell stage at its tile     */
 } dcg_tuning;

@@ -66,18 +66,20 @@ def test_batch_member_equals_oracle():
         compare(b[i], o, p, f"member {i} vs oracle")
 
 
-def tuning(tile, cache, ctas, barrier):
+def tuning(tile, cache, ctas, barrier, persistent=0):
     t = capi.DcgTuning()
     for k in range(4):
         t.tile[k] = tile
     t.solve_cache, t.solve_ctas_per_sm, t.solve_barrier = cache, ctas, barrier
+    t.persistent = persistent
     return t
 
 
 def test_results_do_not_depend_on_tuning():
     params = small_batch(5, 13)
     ref = batch_run(params, 5, tuning(4, 4, 0, 1))
-    for t in [tuning(2, 0, 1, 0), tuning(8, 8, 2, 1), tuning(2, 8, 1, 0), tuning(8, 0, 0, 1)]:
+    for t in [tuning(2, 0, 1, 0), tuning(8, 8, 2, 1, 1), tuning(2, 8, 1, 0, 1), tuning(8, 0, 0, 1),
+              tuning(4, 3, 0, 0, 1)]:
         b = batch_run(params, 5, t)
         for i, p in enumerate(params):
             compare(b[i], ref[i], p, f"tiles {list(t.tile)} cache {t.solve_cache} member {i}")
@@ -142,9 +144,10 @@ def test_time_solve_reports_bytes():
     assert ms > 0 and nbytes > 0
 
 
-def test_batch_stats_equal_member_stats():
+@pytest.mark.parametrize("persistent", [0, 1])
+def test_batch_stats_equal_member_stats(persistent):
     params = small_batch(4, 6)
-    b = batch_run(params, 3)
+    b = batch_run(params, 3, tuning(4, 4, 0, 1, persistent))
     for st, m in zip(b.stats(), b):
         one = m.stats()
         assert st.active_cells == one.active_cells and list(st.load) == list(one.load)
