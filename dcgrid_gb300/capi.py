@@ -128,7 +128,7 @@ class DcgTuning(C.Structure):
     _fields_ = [
         ("tile", C.c_int32 * 4), ("solve_cache", C.c_int32),
         ("solve_ctas_per_sm", C.c_int32), ("solve_barrier", C.c_int32), ("persistent", C.c_int32),
-        ("reserved", C.c_int32 * 4), ("solve_ms", C.c_float), ("cells_ms", C.c_float * 4),
+        ("round_ctas_per_sm", C.c_int16 * 4), ("round_cache", C.c_int8 * 4), ("round_barrier", C.c_int8 * 4), ("solve_ms", C.c_float), ("cells_ms", C.c_float * 4),
     ]
 
 
@@ -148,7 +148,8 @@ class DcgRenderParams(C.Structure):
 def tuning_to_dict(t):
     return {"tile": list(t.tile), "solve_cache": t.solve_cache, "solve_ctas_per_sm": t.solve_ctas_per_sm,
             "solve_barrier": t.solve_barrier, "persistent": t.persistent, "solve_ms": t.solve_ms,
-            "cells_ms": list(t.cells_ms)}
+            "cells_ms": list(t.cells_ms), "round_ctas_per_sm": list(t.round_ctas_per_sm),
+            "round_cache": list(t.round_cache), "round_barrier": list(t.round_barrier)}
 
 
 def default_params(gx, gy, gz, max_blocks):

@@ -91,6 +91,14 @@ struct dcg_batch {
         return fail(DCG_E_INVALID, "tiles must be 2, 4 or 8 blocks");
     solve_grid = batch_solve_grid(sms, tune.solve_cache, tune.solve_ctas_per_sm);
     if (solve_grid <= 0) return fail(DCG_E_CUDA, "cooperative level solve cannot be resident");
+    for (int r = 0; r < 4; r++) {
+      if (tune.round_ctas_per_sm[r] <= 0) continue;
+      const int c = tune.round_cache[r];
+      if ((c != 0 && c != 3 && c != 4 && c != 8) || (tune.round_barrier[r] != 0 && tune.round_barrier[r] != 1))
+        return fail(DCG_E_INVALID, "round schedule: cache 0, 3, 4 or 8 and barrier 0 or 1");
+      if (batch_solve_grid(sms, c, tune.round_ctas_per_sm[r]) <= 0)
+        return fail(DCG_E_CUDA, "round schedule cannot be resident");
+    }
     return DCG_OK;
   }
 
@@ -133,8 +141,21 @@ struct dcg_batch {
         launch_restrict_batch(P, stream);
       }
   }
+  // the cascade with the tuned schedule of each round
+  void solve_tuned() {
+    for (int round = 0; round <= maxtop; round++) {
+      if (round < 4 && tune.round_ctas_per_sm[round] > 0)
+        solve_round(round, batch_solve_grid(sms, tune.round_cache[round], tune.round_ctas_per_sm[round]),
+                    tune.round_cache[round], tune.round_barrier[round]);
+      else
+        solve_round(round, solve_grid, tune.solve_cache, tune.solve_barrier);
+    }
+  }
   void solve(int grid, int cache, int tree) {
-    for (int round = 0; round <= maxtop; round++)
+    for (int round = 0; round <= maxtop; round++) solve_round(round, grid, cache, tree);
+  }
+  void solve_round(int round, int grid, int cache, int tree) {
+    {
       for (int g = 0; g < groups(); g++) {
         SolveBatch P{};
         P.n = std::min(BMAX, n() - g * BMAX);
@@ -152,6 +173,7 @@ struct dcg_batch {
         }
         launch_level_solve_batch(P, round, iters, grid, cache, tree, stream);
       }
+    }
   }
   void flip_v() {
     for (dcg_sim *s : m) {
@@ -183,7 +205,7 @@ struct dcg_batch {
     adapt_branches();
     cells(2);  // divergence
     restrict_fields(2);
-    solve(solve_grid, tune.solve_cache, tune.solve_barrier);
+    solve_tuned();
     cells(3);  // apply pressure
     restrict_fields(0);
     cells(1);  // advect scalars (+ sources, emission)
@@ -330,6 +352,31 @@ struct dcg_batch {
           }
         }
     }
+    // each round of the first four on its own: the best schedule if it beats
+    // the whole-cascade choice for that round
+    for (int r = 0; r < 4 && r <= maxtop; r++) {
+      const float base = time_ms(reps, [&] {
+        solve_round(r, batch_solve_grid(sms, best.solve_cache, best.solve_ctas_per_sm), best.solve_cache,
+                    best.solve_barrier);
+      });
+      float bms = base;
+      best.round_ctas_per_sm[r] = 0;
+      for (int cache : {0, 3, 4, 8}) {
+        const int occ = batch_solve_grid(sms, cache, 0) / std::max(1, sms);
+        for (int k = 1; k <= occ; k++)
+          for (int tree = 0; tree < 2; tree++) {
+            const int grid = batch_solve_grid(sms, cache, k);
+            const float ms = time_ms(reps, [&] { solve_round(r, grid, cache, tree); });
+            if (ms < 0.97f * bms) {
+              bms = ms;
+              best.round_ctas_per_sm[r] = (int16_t)k;
+              best.round_cache[r] = (int8_t)cache;
+              best.round_barrier[r] = (int8_t)tree;
+            }
+          }
+      }
+      best_solve += bms - base;
+    }
     best.solve_ms = best_solve;
     if ((rc = sync())) return rc;
     tune = best;
@@ -387,7 +434,7 @@ struct dcg_batch {
       if ((rc = cuda(cudaMemcpy(load, s->D.load, sizeof(load), cudaMemcpyDeviceToHost), "load"))) return rc;
       for (int l = 0; l < s->D.g.levels; l++) cells_sweeps += 64.0 * (double)load[l] * iters;
     }
-    *avg_ms = time_ms(reps, [&] { solve(solve_grid, tune.solve_cache, tune.solve_barrier); });
+    *avg_ms = time_ms(reps, [&] { solve_tuned(); });
     if (bytes_out) *bytes_out = 12.0 * cells_sweeps;
     return sync();
   }

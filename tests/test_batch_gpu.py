@@ -78,8 +78,11 @@ def tuning(tile, cache, ctas, barrier, persistent=0):
 def test_results_do_not_depend_on_tuning():
     params = small_batch(5, 13)
     ref = batch_run(params, 5, tuning(4, 4, 0, 1))
+    rounds = tuning(4, 4, 0, 1, 1)
+    rounds.round_ctas_per_sm[0], rounds.round_cache[0], rounds.round_barrier[0] = 1, 0, 1
+    rounds.round_ctas_per_sm[1], rounds.round_cache[1], rounds.round_barrier[1] = 2, 3, 0
     for t in [tuning(2, 0, 1, 0), tuning(8, 8, 2, 1, 1), tuning(2, 8, 1, 0, 1), tuning(8, 0, 0, 1),
-              tuning(4, 3, 0, 0, 1)]:
+              tuning(4, 3, 0, 0, 1), rounds]:
         b = batch_run(params, 5, t)
         for i, p in enumerate(params):
             compare(b[i], ref[i], p, f"tiles {list(t.tile)} cache {t.solve_cache} member {i}")
