@@ -8,9 +8,10 @@
 // parameters, and a CTA picks its member from the cumulative CTA counts.
 // The pressure cascade is one cooperative launch per round over the members'
 // concatenated cells of one level; p, p~ and div of all members are slices of
-// three batch arenas so the solve addresses them with one base pointer. Member
-// adaptations (sorts and selections of one simulation's blocks) run as
-// parallel branches of the captured step graph. Per-member arithmetic is the
+// three batch arenas so the solve addresses them with one base pointer. The
+// adaptation (scores, radix sorts, selections, moves, refinements, neighbour
+// rebuild, propagation) is likewise one launch per adaptation kernel over all
+// members, each member's sorts and counters kept separate. Per-member arithmetic is the
 // single simulation's, so results are bit-identical to standalone runs.
 #include <chrono>
 
@@ -20,9 +21,7 @@ struct dcg_batch {
   std::vector<dcg_sim *> m;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  std::vector<cudaStream_t> aux;
-  std::vector<cudaEvent_t> joins;
-  cudaEvent_t fork = nullptr;
+  std::vector<SortScratch> S2;  // members' second sort scratch (block sorts)
   int device = 0, sms = 148;
   std::string err;
   std::vector<void *> allocs;
@@ -36,14 +35,9 @@ struct dcg_batch {
   int solve_grid = 0;
   std::map<int, cudaGraphExec_t> graphs;
   long long kernels_per_step = 0;
-  // pinned staging of the members' statistics: red[32] doubles, ctr[C_COUNT]
-  // and load[MAXL] counters, the error word
-  struct StatStage {
-    double red[32];
-    long long ctr[C_COUNT], load[MAXL];
-    uint32_t err, pad;
-  };
-  StatStage *stage = nullptr;
+  // the members' statistics: one device record per member, read back with
+  // one copy into pinned memory
+  StatRecord *stage = nullptr, *stage_dev = nullptr;
 
   int fail(int code, const std::string &msg) {
     err = msg;
@@ -73,9 +67,6 @@ struct dcg_batch {
     drop_graphs();
     for (dcg_sim *s : m) delete s;
     for (void *p : allocs) cudaFree(p);
-    for (cudaStream_t a : aux) cudaStreamDestroy(a);
-    for (cudaEvent_t e : joins) cudaEventDestroy(e);
-    if (fork) cudaEventDestroy(fork);
     if (stage) cudaFreeHost(stage);
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
@@ -187,22 +178,24 @@ struct dcg_batch {
       s->bind_parity();
     }
   }
-  void adapt_branches() {
-    cudaEventRecord(fork, stream);
-    for (int i = 0; i < n(); i++) {
-      cudaStreamWaitEvent(aux[i], fork, 0);
-      dcg_sim *s = m[i];
-      launch_adapt(s->D, s->S, s->keys, s->vals, s->keys2, s->vals2, s->sms, aux[i]);
-      cudaEventRecord(joins[i], aux[i]);
+  // every member's adaptation, one launch per adaptation kernel and group
+  void adapt() {
+    for (int g = 0; g < groups(); g++) {
+      AdaptMember A[BMAX];
+      const int k = std::min(BMAX, n() - g * BMAX);
+      for (int i = 0; i < k; i++) {
+        const dcg_sim *s = m[g * BMAX + i];
+        A[i] = AdaptMember{s->D, s->S, S2[g * BMAX + i], s->keys, s->vals, s->keys2, s->vals2};
+      }
+      launch_adapt_batch(A, k, sms, stream);
     }
-    for (int i = 0; i < n(); i++) cudaStreamWaitEvent(stream, joins[i], 0);
   }
   // Simulation::updateSimulation (simulation.cpp:104-112) for every member
   void step_once() {
     cells(0);  // advect velocity (+ buoyancy)
     flip_v();
     restrict_fields(0);
-    adapt_branches();
+    adapt();
     cells(2);  // divergence
     restrict_fields(2);
     solve_tuned();
@@ -390,26 +383,22 @@ struct dcg_batch {
   // every member's statistics with one launch per group and one synchronisation
   int get_stats(dcg_stats *out) {
     int rc;
-    if (!stage && (rc = cuda(cudaMallocHost(&stage, sizeof(StatStage) * n()), "stats staging"))) return rc;
-    for (dcg_sim *s : m) cudaMemsetAsync(s->D.red, 0, sizeof(double) * 32, stream);
+    if (!stage && (rc = cuda(cudaMallocHost(&stage, sizeof(StatRecord) * n()), "stats staging"))) return rc;
+    if (!stage_dev && (rc = alloc(&stage_dev, n()))) return rc;
     for (int g = 0; g < groups(); g++) {
       CellBatch P{};
       P.n = std::min(BMAX, n() - g * BMAX);
       for (int i = 0; i < P.n; i++) P.d[i] = m[g * BMAX + i]->D;
+      launch_stats_zero(P, stream);
       launch_cells_batch(4, P, 4, stream, tune.persistent != 0);
+      launch_stats_gather(P, stage_dev + g * BMAX, stream);
     }
-    for (int i = 0; i < n(); i++) {
-      const Dev &D = m[i]->D;
-      cudaMemcpyAsync(stage[i].red, D.red, sizeof(stage[i].red), cudaMemcpyDeviceToHost, stream);
-      cudaMemcpyAsync(stage[i].ctr, D.ctr, sizeof(stage[i].ctr), cudaMemcpyDeviceToHost, stream);
-      cudaMemcpyAsync(stage[i].load, D.load, sizeof(stage[i].load), cudaMemcpyDeviceToHost, stream);
-      cudaMemcpyAsync(&stage[i].err, D.err, 4, cudaMemcpyDeviceToHost, stream);
-    }
+    cudaMemcpyAsync(stage, stage_dev, sizeof(StatRecord) * n(), cudaMemcpyDeviceToHost, stream);
     if ((rc = cuda(cudaStreamSynchronize(stream), "stats"))) return rc;
     for (int i = 0; i < n(); i++) {
       dcg_stats &st = out[i];
       std::memset(&st, 0, sizeof st);
-      const StatStage &x = stage[i];
+      const StatRecord &x = stage[i];
       st.steps = m[i]->steps;
       st.residual = x.red[0];
       st.mass = x.red[1];
@@ -451,7 +440,6 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
   cudaError_t e = cudaGetDevice(&b->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     delete b;
     return DCG_E_CUDA;
@@ -504,15 +492,15 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
       return rc;
     }
     b->maxtop = std::max(b->maxtop, s->D.g.levels - 1);
-    cudaStream_t a = nullptr;
-    cudaEvent_t j = nullptr;
-    if (cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&j, cudaEventDisableTiming) != cudaSuccess) {
+    SortScratch S2{};
+    const long long nb = s->D.g.B, nt = sort_tiles(nb);
+    if ((rc = b->alloc(&S2.k1, nb)) || (rc = b->alloc(&S2.v1, nb)) || (rc = b->alloc(&S2.hist, 256 * nt)) ||
+        (rc = b->alloc(&S2.totals, 256))) {
       delete b;
-      return DCG_E_CUDA;
+      return rc;
     }
-    b->aux.push_back(a);
-    b->joins.push_back(j);
+    S2.max_n = nb;
+    b->S2.push_back(S2);
   }
   for (int k = 0; k < 4; k++) b->tune.tile[k] = 4;
   b->tune.solve_cache = 4;

@@ -525,7 +525,14 @@ __device__ inline void back_trace(const Dev &D, int4 bp, int c, size_t cell, flo
 // k_dcgrid_debug_stats (dcgrid_structure.cu:224-251) for one cell of block b,
 // plus mass and leaf counts, reduced per warp into D.red (every lane of the
 // warp calls this; a warp covers half of one block).
-__device__ inline void stats_cell(const Dev &D, long long b, int c) {
+// Warp totals of the statistics of k_dcgrid_debug_stats (dcgrid_structure.cu:224-251)
+// plus mass and leaf counts; every lane receives them. A warp covers half of
+// one block, so all its leaf cells share one level (lvl, cnt leaf cells).
+struct WarpStats {
+  double res, mass;
+  int lvl, cnt;
+};
+__device__ inline WarpStats stats_warp(const Dev &D, long long b, int c) {
   double res = 0.0, mass = 0.0;
   int lev = -1;
   if (b < D.g.B) {
@@ -553,14 +560,26 @@ __device__ inline void stats_cell(const Dev &D, long long b, int c) {
     res += __shfl_xor_sync(0xffffffffu, res, o);
     mass += __shfl_xor_sync(0xffffffffu, mass, o);
   }
-  // a warp covers half of one block, so all its leaf cells share one level
   const unsigned leafmask = __ballot_sync(0xffffffffu, lev >= 0);
-  const int lvl0 = __shfl_sync(0xffffffffu, lev, leafmask ? __ffs(leafmask) - 1 : 0);
+  WarpStats w;
+  w.res = res;
+  w.mass = mass;
+  w.cnt = __popc(leafmask);
+  w.lvl = __shfl_sync(0xffffffffu, lev, leafmask ? __ffs(leafmask) - 1 : 0);
+  return w;
+}
+// adds warp totals into the member's reduction slots (lane 0)
+__device__ inline void stats_flush(const Dev &D, double res, double mass, int lvl, double cnt) {
   if ((threadIdx.x & 31) == 0) {
     if (res != 0.0) atomicAdd(&D.red[0], res);
     if (mass != 0.0) atomicAdd(&D.red[1], mass);
-    if (leafmask) atomicAdd(&D.red[2 + lvl0], (double)__popc(leafmask));
+    if (cnt != 0.0) atomicAdd(&D.red[2 + lvl], cnt);
   }
+}
+// statistics of one cell, one double atomic per warp and quantity
+__device__ inline void stats_cell(const Dev &D, long long b, int c) {
+  const WarpStats w = stats_warp(D, b, c);
+  stats_flush(D, w.res, w.mass, w.lvl, (double)w.cnt);
 }
 
 }  // namespace dcg

@@ -23,6 +23,15 @@ struct SortScratch {
 long long sort_tiles(long long n);
 void launch_radix_sort(uint32_t *keys, uint32_t *vals, long long n, const SortScratch &s,
                        const long long *active, cudaStream_t st);
+// many sorts in the same launches (at most SORT_SEGS segments, each with its own scratch)
+constexpr int SORT_SEGS = 32;
+struct SortSeg {
+  uint32_t *keys, *vals;
+  long long n;
+  const long long *active;
+  SortScratch s;
+};
+void launch_radix_sort_batch(const SortSeg *seg, int nseg, cudaStream_t st);
 
 // k_fluid.cu
 void launch_advect_velocity(const Dev &D, cudaStream_t st);
@@ -73,6 +82,15 @@ static_assert(sizeof(RestrictBatch) < 32000 && sizeof(SolveBatch) < 32000, "kern
 // persistent: a grid of a few CTAs per SM over the allocated blocks only
 void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st, bool persistent = false);
 void launch_restrict_batch(RestrictBatch &P, cudaStream_t st);
+// statistics read-out of a batch: zero the members' reduction slots; copy
+// every member's slots, counters, loads and error word into one record array
+struct StatRecord {
+  double red[32];
+  long long ctr[C_COUNT], load[MAXL];
+  uint32_t err, pad;
+};
+void launch_stats_zero(const CellBatch &P, cudaStream_t st);
+void launch_stats_gather(const CellBatch &P, StatRecord *dst, cudaStream_t st);
 // CTAs of the batched solve for a cache depth (0, 4, 8) and CTAs per SM (0 = occupancy limit)
 int batch_solve_grid(int sms, int cache, int ctas_per_sm);
 void launch_level_solve_batch(const SolveBatch &P, int round, int sweeps, int grid, int cache, int tree,
@@ -84,6 +102,14 @@ void launch_activate_level(const Dev &D, int level, cudaStream_t st);
 void launch_build_nbr(const Dev &D, bool only_if_touched, cudaStream_t st);
 void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *vals,
                   uint32_t *keys2, uint32_t *vals2, int sms, cudaStream_t st);
+// launch_adapt for up to BMAX members, one launch per adaptation kernel;
+// S2 is a second sort scratch (at least B keys) so two sorts share launches
+struct AdaptMember {
+  Dev D;
+  SortScratch S, S2;
+  uint32_t *keys, *vals, *keys2, *vals2;
+};
+void launch_adapt_batch(const AdaptMember *m, int n, int sms, cudaStream_t st);
 void launch_stats(const Dev &D, cudaStream_t st);
 void launch_fields_to_dense(const Dev &D, const void *src, int mode, float *dst, cudaStream_t st);
 void launch_h16_to_f32(const uint16_t *src, float *dst, long long n, int mode, cudaStream_t st);

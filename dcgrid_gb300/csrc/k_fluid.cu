@@ -653,6 +653,10 @@ __global__ void __launch_bounds__(64 * TB) k_cells_persist(const __grid_constant
   __syncthreads();
   const long long total = s_end[nseg - 1];
   const int c = threadIdx.x & 63;
+  // statistics: warp totals accumulate in registers while the member and
+  // level stay the same and are flushed with one atomic per quantity
+  double a_res = 0.0, a_mass = 0.0, a_cnt = 0.0;
+  int a_mem = -1, a_lvl = 0;
   for (long long t = blockIdx.x; t < total; t += gridDim.x) {
     int lo = 0, hi = nseg - 1;
     while (lo < hi) {
@@ -670,8 +674,40 @@ __global__ void __launch_bounds__(64 * TB) k_cells_persist(const __grid_constant
     else if (STAGE == 1) advect_scalars_cell(D, b, c);
     else if (STAGE == 2) divergence_cell(D, b, c);
     else if (STAGE == 3) apply_pressure_cell(D, b, c);
-    else stats_cell(D, b, c);
+    else {
+      const WarpStats w = stats_warp(D, b, c);
+      const int mem = lo / MAXL;
+      if (w.cnt) {
+        if (mem != a_mem || w.lvl != a_lvl) {
+          if (a_mem >= 0) stats_flush(P.d[a_mem], a_res, a_mass, a_lvl, a_cnt);
+          a_mem = mem;
+          a_lvl = w.lvl;
+          a_res = a_mass = a_cnt = 0.0;
+        }
+        a_res += w.res;
+        a_mass += w.mass;
+        a_cnt += (double)w.cnt;
+      }
+    }
   }
+  if (STAGE == 4 && a_mem >= 0) stats_flush(P.d[a_mem], a_res, a_mass, a_lvl, a_cnt);
+}
+
+__global__ void __launch_bounds__(128) k_stats_zero(const __grid_constant__ CellBatch P) {
+  if (threadIdx.x < 32) P.d[blockIdx.x].red[threadIdx.x] = 0.0;
+}
+__global__ void __launch_bounds__(128) k_stats_gather(const __grid_constant__ CellBatch P, StatRecord *dst) {
+  const Dev &D = P.d[blockIdx.x];
+  StatRecord &r = dst[blockIdx.x];
+  const int t = threadIdx.x;
+  if (t < 32) r.red[t] = __ldcg(D.red + t);
+  if (t < C_COUNT) r.ctr[t] = __ldcg(D.ctr + t);
+  if (t < MAXL) r.load[t] = __ldcg(D.load + t);
+  if (t == 0) r.err = __ldcg(D.err);
+}
+void launch_stats_zero(const CellBatch &P, cudaStream_t st) { k_stats_zero<<<P.n, 128, 0, st>>>(P); }
+void launch_stats_gather(const CellBatch &P, StatRecord *dst, cudaStream_t st) {
+  k_stats_gather<<<P.n, 128, 0, st>>>(P, dst);
 }
 
 __global__ void __launch_bounds__(256) k_restrict_batch(const __grid_constant__ RestrictBatch P) {

@@ -7,7 +7,9 @@
 // fluid_simulation_dcgrid.cu:348-483). Here every decision is made on the
 // device from counters in device memory, so a whole step has a fixed launch
 // sequence and can be captured in a CUDA graph.
+#include <algorithm>
 #include <cfloat>
+#include <vector>
 
 #include "dcg_kernels.h"
 
@@ -59,9 +61,9 @@ __global__ void __launch_bounds__(256) k_activate_level(Dev D, int level) {
 // neighbouring block position, or OUT. This equals what the reference's
 // apron refresh (dcgrid_structure.cu:30-92) and activation (:104-178) store
 // for the border apron cells of that direction.
-__global__ void __launch_bounds__(256) k_build_nbr(Dev D, int only_if_touched) {
+__device__ __forceinline__ void build_nbr_body(const Dev &D, int only_if_touched, unsigned bx, unsigned gx) {
   if (only_if_touched && D.ctr[C_TOUCHED] == 0) return;
-  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gid = (long long)bx * blockDim.x + threadIdx.x;
   const long long b = gid / 27;
   if (b >= D.g.B) return;
   const int d = (int)(gid % 27);
@@ -83,6 +85,7 @@ __global__ void __launch_bounds__(256) k_build_nbr(Dev D, int only_if_touched) {
   }
   D.nbr[27 * b + d] = e;
 }
+__global__ void __launch_bounds__(256) k_build_nbr(Dev D, int only_if_touched) { build_nbr_body(D, only_if_touched, blockIdx.x, gridDim.x); }
 
 // ------------------------------------------------------------------ scores
 __device__ inline bool level_blocked(const Dev &D, int level) {
@@ -91,33 +94,69 @@ __device__ inline bool level_blocked(const Dev &D, int level) {
 }
 
 // k_dcgrid_calc_subblock_scores (dcgrid_adaptation.cu:10-40), geometric score.
-__global__ void __launch_bounds__(256) k_scores_geo(Dev D) {
-  const long long sb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (sb >= 8 * D.g.B) {
-    if (sb == 8 * D.g.B) D.ss[sb] = 0.f;
-    return;
-  }
+__device__ __forceinline__ float geo_score(const Dev &D, long long sb) {
   const long long b = sb >> 3;
   const int4 bp = D.pos[b];
-  if (D.child[sb] != NONE || bp.w < 0 || level_blocked(D, bp.w)) {
-    D.ss[sb] = -FLT_MAX;
-    return;
-  }
+  if (D.child[sb] != NONE || bp.w < 0 || level_blocked(D, bp.w)) return -FLT_MAX;
   const float sc = (float)(1 << bp.w);
   const float px = sc * ((float)bp.x + 2.f * (float)((sb >> 2) & 1) + 1.f);
   const float py = sc * ((float)bp.y + 2.f * (float)((sb >> 1) & 1) + 1.f);
   const float pz = sc * ((float)bp.z + 2.f * (float)(sb & 1) + 1.f);
   const float ddx = px - .5f * (float)D.g.gx, ddy = py - .45f * (float)D.g.gy, ddz = pz - .5f * (float)D.g.gz;
   const float dd = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
-  D.ss[sb] = dd < .2f * (float)D.g.gx ? 0.f : (float)D.g.gx / dd;
+  return dd < .2f * (float)D.g.gx ? 0.f : (float)D.g.gx / dd;
 }
+__device__ __forceinline__ void scores_geo_body(const Dev &D, unsigned bx, unsigned gx) {
+  const long long sb = (long long)bx * blockDim.x + threadIdx.x;
+  if (sb >= 8 * D.g.B) {
+    if (sb == 8 * D.g.B) D.ss[sb] = 0.f;
+    return;
+  }
+  D.ss[sb] = geo_score(D, sb);
+}
+__global__ void __launch_bounds__(256) k_scores_geo(Dev D) { scores_geo_body(D, blockIdx.x, gridDim.x); }
 
 // Field criterion (extension): per cell max(|curl v|/vort_t, |grad rho|/grad_t)
 // with the central differences of k_dcgrid_calc_vorticity
 // (dcgrid_fluid.cu:146-172); subblock score = max over its 8 cells, reduced
 // with warp shuffles (a subblock is 8 consecutive lanes).
-__global__ void __launch_bounds__(256) k_scores_fields(Dev D) {
-  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ bool subblock_blocked(const Dev &D, long long sb, int4 bp) {
+  return D.child[sb] != NONE || bp.w < 0 || (bp.w >= 0 && level_blocked(D, bp.w));
+}
+__device__ __forceinline__ float field_cell_score(const Dev &D, long long b, int4 bp, int c) {
+  int lx, ly, lz;
+  local_xyz(c, lx, ly, lz);
+  const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+  const int scale = 1 << bp.w;
+  const float alpha = 0.5f * D.ph.rdx / (float)scale;
+  const unsigned long long L = apron_cell(D, (uint32_t)b, bp, ax - 1, ay, az);
+  const unsigned long long R = apron_cell(D, (uint32_t)b, bp, ax + 1, ay, az);
+  const unsigned long long Dn = apron_cell(D, (uint32_t)b, bp, ax, ay - 1, az);
+  const unsigned long long U = apron_cell(D, (uint32_t)b, bp, ax, ay + 1, az);
+  const unsigned long long Bk = apron_cell(D, (uint32_t)b, bp, ax, ay, az - 1);
+  const unsigned long long F = apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1);
+  const float *W = D.w;
+  const float wl = W[L], wr = W[R], wd = W[Dn], wu = W[U], wb = W[Bk], wf = W[F];
+  const float *V0 = D.v[0], *V1 = D.v[1], *V2 = D.v[2];
+  const float ox = alpha * ((wu * V2[U] - wd * V2[Dn]) - (wf * V1[F] - wb * V1[Bk]));
+  const float oy = alpha * ((wf * V0[F] - wb * V0[Bk]) - (wr * V2[R] - wl * V2[L]));
+  const float oz = alpha * ((wr * V1[R] - wl * V1[L]) - (wu * V0[U] - wd * V0[Dn]));
+  const float gxr = alpha * (q_ld(D, 0, R) - q_ld(D, 0, L));
+  const float gyr = alpha * (q_ld(D, 0, U) - q_ld(D, 0, Dn));
+  const float gzr = alpha * (q_ld(D, 0, F) - q_ld(D, 0, Bk));
+  const float om = sqrtf(ox * ox + oy * oy + oz * oz);
+  const float gr = sqrtf(gxr * gxr + gyr * gyr + gzr * gzr);
+  const float a = om / D.ph.vort_t, bb = gr / D.ph.grad_t;
+  return fmaxf(0.f, a < bb ? bb : a);
+}
+// max over the 8 lanes of a subblock group (lanes 8k..8k+7 of a warp)
+__device__ __forceinline__ float max8(float m) {
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  return m;
+}
+__device__ __forceinline__ void scores_fields_body(const Dev &D, unsigned bx, unsigned gx) {
+  const long long gid = (long long)bx * blockDim.x + threadIdx.x;
   const long long b = gid >> 6;
   if (b >= D.g.B) {
     if (gid == 64 * D.g.B) D.ss[8 * D.g.B] = 0.f;
@@ -126,43 +165,16 @@ __global__ void __launch_bounds__(256) k_scores_fields(Dev D) {
   const int c = (int)(gid & 63);
   const int4 bp = D.pos[b];
   const long long sb = (long long)b * 8 + (c >> 3);
-  const bool blocked = D.child[sb] != NONE || bp.w < 0 || (bp.w >= 0 && level_blocked(D, bp.w));
-  float m = 0.f;
-  if (!blocked) {
-    int lx, ly, lz;
-    local_xyz(c, lx, ly, lz);
-    const int ax = lx + 1, ay = ly + 1, az = lz + 1;
-    const int scale = 1 << bp.w;
-    const float alpha = 0.5f * D.ph.rdx / (float)scale;
-    const unsigned long long L = apron_cell(D, (uint32_t)b, bp, ax - 1, ay, az);
-    const unsigned long long R = apron_cell(D, (uint32_t)b, bp, ax + 1, ay, az);
-    const unsigned long long Dn = apron_cell(D, (uint32_t)b, bp, ax, ay - 1, az);
-    const unsigned long long U = apron_cell(D, (uint32_t)b, bp, ax, ay + 1, az);
-    const unsigned long long Bk = apron_cell(D, (uint32_t)b, bp, ax, ay, az - 1);
-    const unsigned long long F = apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1);
-    const float *W = D.w;
-    const float wl = W[L], wr = W[R], wd = W[Dn], wu = W[U], wb = W[Bk], wf = W[F];
-    const float *V0 = D.v[0], *V1 = D.v[1], *V2 = D.v[2];
-    const float ox = alpha * ((wu * V2[U] - wd * V2[Dn]) - (wf * V1[F] - wb * V1[Bk]));
-    const float oy = alpha * ((wf * V0[F] - wb * V0[Bk]) - (wr * V2[R] - wl * V2[L]));
-    const float oz = alpha * ((wr * V1[R] - wl * V1[L]) - (wu * V0[U] - wd * V0[Dn]));
-    const float gxr = alpha * (q_ld(D, 0, R) - q_ld(D, 0, L));
-    const float gyr = alpha * (q_ld(D, 0, U) - q_ld(D, 0, Dn));
-    const float gzr = alpha * (q_ld(D, 0, F) - q_ld(D, 0, Bk));
-    const float om = sqrtf(ox * ox + oy * oy + oz * oz);
-    const float gr = sqrtf(gxr * gxr + gyr * gyr + gzr * gzr);
-    const float a = om / D.ph.vort_t, bb = gr / D.ph.grad_t;
-    m = fmaxf(0.f, a < bb ? bb : a);
-  }
-#pragma unroll
-  for (int o = 1; o < 8; o <<= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  const bool blocked = subblock_blocked(D, sb, bp);
+  const float m = max8(blocked ? 0.f : field_cell_score(D, b, bp, c));
   if ((c & 7) == 0) D.ss[sb] = blocked ? -FLT_MAX : m;
 }
+__global__ void __launch_bounds__(256) k_scores_fields(Dev D) { scores_fields_body(D, blockIdx.x, gridDim.x); }
 
 // k_dcgrid_accumulate_subblock_scores (dcgrid_adaptation.cu:42-63); with
 // ref_compat the reference's ninth summand s[8] is included.
-__global__ void __launch_bounds__(256) k_block_scores(Dev D) {
-  const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void block_scores_body(const Dev &D, unsigned bx, unsigned gx) {
+  const long long b = (long long)bx * blockDim.x + threadIdx.x;
   if (b >= D.g.B) return;
   D.bs[b] = -FLT_MAX;
   const int level = D.pos[b].w;
@@ -175,10 +187,11 @@ __global__ void __launch_bounds__(256) k_block_scores(Dev D) {
     D.bs[b] = .125f * sum;
   }
 }
+__global__ void __launch_bounds__(256) k_block_scores(Dev D) { block_scores_body(D, blockIdx.x, gridDim.x); }
 
 // ------------------------------------------------------------------ moves
 // Move limit of one level (fluid_simulation_dcgrid.cu:376-385).
-__global__ void k_move_setup(Dev D, int L) {
+__device__ __forceinline__ void move_setup_body(const Dev &D, int L, unsigned bx, unsigned gx) {
   const long long d0 = D.g.budget[L], d1 = 8 * D.g.budget[L + 1];
   long long l = d0 < d1 ? d0 : d1;
   l = l < D.load[L] ? l : D.load[L];
@@ -190,22 +203,24 @@ __global__ void k_move_setup(Dev D, int L) {
   D.ctr[C_MOVE_BEGIN + L] = D.ctr[C_MOVES];
   D.ctr[C_MOVE_END + L] = D.ctr[C_MOVES];
 }
+__global__ void k_move_setup(Dev D, int L) { move_setup_body(D, L, blockIdx.x, gridDim.x); }
 
 // Sort keys: blocks ascending by score, negative scores last; subblocks
 // descending by score. The sort is stable over index-ordered input, so
 // equal keys stay in index order.
-__global__ void __launch_bounds__(256) k_keys_blocks(Dev D, int L, uint32_t *keys, uint32_t *vals) {
+__device__ __forceinline__ void keys_blocks_body(const Dev &D, int L, uint32_t *keys, uint32_t *vals, unsigned bx, unsigned gx) {
   if (D.ctr[C_MOVE_LIMIT] == 0) return;
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long i = (long long)bx * blockDim.x + threadIdx.x;
   if (i >= D.g.budget[L]) return;
   const long long b = D.g.off[L] + i;
   const float s = D.bs[b];
   keys[i] = s < 0.f ? 0xFFFFFFFFu : (__float_as_uint(s) & 0x7FFFFFFFu);
   vals[i] = (uint32_t)b;
 }
-__global__ void __launch_bounds__(256) k_keys_dests(Dev D, int L, uint32_t *keys, uint32_t *vals) {
+__global__ void __launch_bounds__(256) k_keys_blocks(Dev D, int L, uint32_t *keys, uint32_t *vals) { keys_blocks_body(D, L, keys, vals, blockIdx.x, gridDim.x); }
+__device__ __forceinline__ void keys_dests_body(const Dev &D, int L, uint32_t *keys, uint32_t *vals, unsigned bx, unsigned gx) {
   if (D.ctr[C_MOVE_LIMIT] == 0) return;
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long i = (long long)bx * blockDim.x + threadIdx.x;
   if (i >= 8 * D.g.budget[L + 1]) return;
   const long long sb = 8 * D.g.off[L + 1] + i;
   const float s = D.ss[sb];
@@ -214,26 +229,27 @@ __global__ void __launch_bounds__(256) k_keys_dests(Dev D, int L, uint32_t *keys
   keys[i] = ~u;                                      // descending
   vals[i] = (uint32_t)sb;
 }
+__global__ void __launch_bounds__(256) k_keys_dests(Dev D, int L, uint32_t *keys, uint32_t *vals) { keys_dests_body(D, L, keys, vals, blockIdx.x, gridDim.x); }
 // First pair that fails the reference's match condition (cu:410-418).
-__global__ void __launch_bounds__(256) k_match(Dev D, const uint32_t *blocks, const uint32_t *dests) {
+__device__ __forceinline__ void match_body(const Dev &D, const uint32_t *blocks, const uint32_t *dests, unsigned bx, unsigned gx) {
   const long long l = D.ctr[C_MOVE_LIMIT];
-  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < l; m += (long long)gridDim.x * blockDim.x) {
+  for (long long m = (long long)bx * blockDim.x + threadIdx.x; m < l; m += (long long)gx * blockDim.x) {
     const float sb = D.bs[blocks[m]], sd = D.ss[dests[m]];
     if (!(sb >= 0.f && sd >= 0.f && sb < sd)) atomicMin(&D.ctr[C_MATCHES], m);
   }
 }
+__global__ void __launch_bounds__(256) k_match(Dev D, const uint32_t *blocks, const uint32_t *dests) { match_body(D, blocks, dests, blockIdx.x, gridDim.x); }
 // Records the matched pairs and protects blocks from moving at the next
 // level: with ref_compat the block of the candidate *after* each match, as
 // the reference's loop does (cu:415-417); otherwise the destination's block.
-__global__ void __launch_bounds__(256) k_commit_moves(Dev D, int L, const uint32_t *blocks,
-                                                      const uint32_t *dests) {
+__device__ __forceinline__ void commit_moves_body(const Dev &D, int L, const uint32_t *blocks, const uint32_t *dests, unsigned bx, unsigned gx) {
   const long long l = D.ctr[C_MOVE_LIMIT];
   if (l == 0) return;
   const long long matches = D.ctr[C_MATCHES];
   const long long base = D.ctr[C_MOVE_BEGIN + L];
   const long long d1 = 8 * D.g.budget[L + 1];
-  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m <= matches;
-       m += (long long)gridDim.x * blockDim.x) {
+  for (long long m = (long long)bx * blockDim.x + threadIdx.x; m <= matches;
+       m += (long long)gx * blockDim.x) {
     if (m < matches) {
       D.moves[2 * (base + m)] = blocks[m];
       D.moves[2 * (base + m) + 1] = dests[m];
@@ -244,21 +260,23 @@ __global__ void __launch_bounds__(256) k_commit_moves(Dev D, int L, const uint32
       D.bs[dests[m] >> 3] = -FLT_MAX;
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (bx == 0 && threadIdx.x == 0) {
     D.move_limit[L] = (long long)(unsigned long long)((float)matches * 1.2f);
     D.ctr[C_MOVES] = base + matches;
     D.ctr[C_MOVE_END + L] = base + matches;
   }
 }
+__global__ void __launch_bounds__(256) k_commit_moves(Dev D, int L, const uint32_t *blocks, const uint32_t *dests) { commit_moves_body(D, L, blocks, dests, blockIdx.x, gridDim.x); }
 // k_dcgrid_move_blocks (dcgrid_adaptation.cu:65-90), one level at a time from
 // coarse to fine so a block moved into a block that itself moved takes its
 // parent's new position.
-__global__ void __launch_bounds__(256) k_apply_moves(Dev D, int L) {
+__device__ __forceinline__ void apply_moves_body(const Dev &D, int L, uint32_t *prevs, unsigned bx, unsigned gx) {
   const long long beg = D.ctr[C_MOVE_BEGIN + L], end = D.ctr[C_MOVE_END + L];
-  for (long long m = beg + (long long)blockIdx.x * blockDim.x + threadIdx.x; m < end;
-       m += (long long)gridDim.x * blockDim.x) {
+  for (long long m = beg + (long long)bx * blockDim.x + threadIdx.x; m < end;
+       m += (long long)gx * blockDim.x) {
     const uint32_t b = D.moves[2 * m], dest = D.moves[2 * m + 1];
     const uint32_t prev = D.parent[b];
+    prevs[m] = prev;
     if (prev != NONE) D.child[prev] = NONE;
     D.child[dest] = b;
     D.parent[b] = dest;
@@ -272,10 +290,50 @@ __global__ void __launch_bounds__(256) k_apply_moves(Dev D, int L) {
     D.touched[m] = b;
   }
 }
+__global__ void __launch_bounds__(256) k_apply_moves(Dev D, int L, uint32_t *prevs) { apply_moves_body(D, L, prevs, blockIdx.x, gridDim.x); }
+
+// Subblock scores after the moves (the reference recomputes every score,
+// fluid_simulation_dcgrid.cu:436). A score depends on its block's position,
+// its own child pointer, the level loads, the neighbour table and the field
+// values; moves change only the positions of moved blocks and the child
+// pointers of their previous and new parent subblocks. Recomputing those
+// subblocks (10 per move: the moved block's 8, the old and the new parent
+// subblock) gives exactly the scores of a full pass.
+__device__ __forceinline__ uint32_t rescore_target(const Dev &D, const uint32_t *prevs, long long t) {
+  const long long m = t / 10;
+  const int k = (int)(t - 10 * m);
+  if (k < 8) return 8u * D.moves[2 * m] + (uint32_t)k;
+  return k == 8 ? prevs[m] : D.moves[2 * m + 1];
+}
+__device__ __forceinline__ void rescore_body(const Dev &D, const uint32_t *prevs, unsigned bx, unsigned gx) {
+  const long long ntask = 10 * D.ctr[C_MOVES];
+  if (ntask == 0) return;
+  if (D.ph.criterion == 0) {
+    for (long long t = (long long)bx * blockDim.x + threadIdx.x; t < ntask; t += (long long)gx * blockDim.x) {
+      const uint32_t sb = rescore_target(D, prevs, t);
+      if (sb != NONE) D.ss[sb] = geo_score(D, sb);
+    }
+    return;
+  }
+  // field criterion: 8 lanes per subblock, 4 subblocks per warp pass
+  const int lane = threadIdx.x & 31;
+  const long long w0 = ((long long)bx * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gx * blockDim.x) >> 5;
+  for (long long tw = 4 * w0; tw < ntask; tw += 4 * nw) {
+    const long long t = tw + (lane >> 3);
+    const uint32_t sb = t < ntask ? rescore_target(D, prevs, t) : NONE;
+    const long long b = sb == NONE ? 0 : (long long)(sb >> 3);
+    const int4 bp = sb == NONE ? make_int4(0, 0, 0, -1) : D.pos[b];
+    const bool blocked = sb == NONE || subblock_blocked(D, sb, bp);
+    const float m = max8(blocked ? 0.f : field_cell_score(D, b, bp, (int)(8 * (sb & 7) + (lane & 7))));
+    if ((lane & 7) == 0 && sb != NONE) D.ss[sb] = blocked ? -FLT_MAX : m;
+  }
+}
+__global__ void __launch_bounds__(256) k_rescore(Dev D, const uint32_t *prevs) { rescore_body(D, prevs, blockIdx.x, gridDim.x); }
 
 // ------------------------------------------------------------ refinements
 // Refinement limit of one parent level (fluid_simulation_dcgrid.cu:449-453).
-__global__ void k_refine_setup(Dev D, int L) {
+__device__ __forceinline__ void refine_setup_body(const Dev &D, int L, unsigned bx, unsigned gx) {
   const unsigned long long a = (unsigned long long)(D.g.budget[L - 1] - D.load[L - 1]);
   const unsigned long long bb = (unsigned long long)(8 * D.load[L]) - (unsigned long long)D.load[L - 1];
   const long long limit = (long long)(a < bb ? a : bb);
@@ -285,6 +343,7 @@ __global__ void k_refine_setup(Dev D, int L) {
   D.ctr[C_LOAD0 + L - 1] = D.load[L - 1];
   D.ctr[C_NCAND] = 0;
 }
+__global__ void k_refine_setup(Dev D, int L) { refine_setup_body(D, L, blockIdx.x, gridDim.x); }
 
 constexpr int CMP_TILE = 2048;
 
@@ -294,10 +353,10 @@ __device__ inline bool cand_flag(const Dev &D, int L, long long i, const uint8_t
   if (sel) return sel[8 * D.g.off[L] + i] != 0;
   return D.ss[8 * D.g.off[L] + i] > D.ph.refine_threshold;
 }
-__global__ void __launch_bounds__(256) k_cmp_count(Dev D, int L, const uint8_t *sel, uint32_t *tile_sums) {
+__device__ __forceinline__ void cmp_count_body(const Dev &D, int L, const uint8_t *sel, uint32_t *tile_sums, unsigned bx, unsigned gx) {
   if (D.ctr[C_MOVE_LIMIT] == 0) return;
   const long long n = 8 * D.g.budget[L];
-  const long long base = (long long)blockIdx.x * CMP_TILE;
+  const long long base = (long long)bx * CMP_TILE;
   int cnt = 0;
   for (int r = 0; r < CMP_TILE / 256; r++) {
     const long long i = base + r * 256 + threadIdx.x;
@@ -310,10 +369,11 @@ __global__ void __launch_bounds__(256) k_cmp_count(Dev D, int L, const uint8_t *
   if (threadIdx.x == 0) {
     int t = 0;
     for (int w = 0; w < 8; w++) t += ws[w];
-    tile_sums[blockIdx.x] = (uint32_t)t;
+    tile_sums[bx] = (uint32_t)t;
   }
 }
-__global__ void __launch_bounds__(1024) k_cmp_scan(Dev D, uint32_t *tile_sums, long long ntiles) {
+__global__ void __launch_bounds__(256) k_cmp_count(Dev D, int L, const uint8_t *sel, uint32_t *tile_sums) { cmp_count_body(D, L, sel, tile_sums, blockIdx.x, gridDim.x); }
+__device__ __forceinline__ void cmp_scan_body(const Dev &D, uint32_t *tile_sums, long long ntiles, unsigned bx, unsigned gx) {
   if (D.ctr[C_MOVE_LIMIT] == 0) return;
   __shared__ uint32_t ws[32];
   __shared__ uint32_t carry_s;
@@ -348,14 +408,14 @@ __global__ void __launch_bounds__(1024) k_cmp_scan(Dev D, uint32_t *tile_sums, l
   }
   if (threadIdx.x == 0) D.ctr[C_NCAND] = carry_s;
 }
-__global__ void __launch_bounds__(256) k_cmp_scatter(Dev D, int L, const uint8_t *sel,
-                                                     const uint32_t *tile_sums, uint32_t *out) {
+__global__ void __launch_bounds__(1024) k_cmp_scan(Dev D, uint32_t *tile_sums, long long ntiles) { cmp_scan_body(D, tile_sums, ntiles, blockIdx.x, gridDim.x); }
+__device__ __forceinline__ void cmp_scatter_body(const Dev &D, int L, const uint8_t *sel, const uint32_t *tile_sums, uint32_t *out, unsigned bx, unsigned gx) {
   if (D.ctr[C_MOVE_LIMIT] == 0) return;
   __shared__ uint32_t ws[8];
   __shared__ uint32_t run_s;
   const long long n = 8 * D.g.budget[L];
-  const long long base = (long long)blockIdx.x * CMP_TILE;
-  if (threadIdx.x == 0) run_s = tile_sums[blockIdx.x];
+  const long long base = (long long)bx * CMP_TILE;
+  if (threadIdx.x == 0) run_s = tile_sums[bx];
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int r = 0; r < CMP_TILE / 256; r++) {
@@ -376,11 +436,11 @@ __global__ void __launch_bounds__(256) k_cmp_scatter(Dev D, int L, const uint8_t
     __syncthreads();
   }
 }
+__global__ void __launch_bounds__(256) k_cmp_scatter(Dev D, int L, const uint8_t *sel, const uint32_t *tile_sums, uint32_t *out) { cmp_scatter_body(D, L, sel, tile_sums, out, blockIdx.x, gridDim.x); }
 // Score-ordered selection (ref_compat off): keys of the compacted candidates.
-__global__ void __launch_bounds__(256) k_keys_cands(Dev D, const uint32_t *cand, uint32_t *keys,
-                                                    uint32_t *vals, long long nmax) {
+__device__ __forceinline__ void keys_cands_body(const Dev &D, const uint32_t *cand, uint32_t *keys, uint32_t *vals, long long nmax, unsigned bx, unsigned gx) {
   const long long n = D.ctr[C_NCAND];
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nmax; i += (long long)gridDim.x * blockDim.x) {
+  for (long long i = (long long)bx * blockDim.x + threadIdx.x; i < nmax; i += (long long)gx * blockDim.x) {
     if (i < n) {
       const float s = D.ss[cand[i]];
       uint32_t u = s == 0.f ? 0u : __float_as_uint(s);
@@ -393,17 +453,19 @@ __global__ void __launch_bounds__(256) k_keys_cands(Dev D, const uint32_t *cand,
     }
   }
 }
-__global__ void __launch_bounds__(256) k_mark_selected(Dev D, const uint32_t *sorted, uint8_t *sel) {
+__global__ void __launch_bounds__(256) k_keys_cands(Dev D, const uint32_t *cand, uint32_t *keys, uint32_t *vals, long long nmax) { keys_cands_body(D, cand, keys, vals, nmax, blockIdx.x, gridDim.x); }
+__device__ __forceinline__ void mark_selected_body(const Dev &D, const uint32_t *sorted, uint8_t *sel, unsigned bx, unsigned gx) {
   if (D.ctr[C_MOVE_LIMIT] == 0) return;
   const long long n = D.ctr[C_NCAND], limit = D.ctr[C_MOVE_LIMIT];
   const long long keep = n < limit ? n : limit;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < keep; i += (long long)gridDim.x * blockDim.x)
+  for (long long i = (long long)bx * blockDim.x + threadIdx.x; i < keep; i += (long long)gx * blockDim.x)
     sel[sorted[i]] = 1;
 }
+__global__ void __launch_bounds__(256) k_mark_selected(Dev D, const uint32_t *sorted, uint8_t *sel) { mark_selected_body(D, sorted, sel, blockIdx.x, gridDim.x); }
 // Records the kept candidates of one level and assigns new block indices in
 // ascending subblock order. ref_compat keeps the `limit` largest subblock
 // indices (the reference's nth_element over indices, cu:464-466).
-__global__ void __launch_bounds__(256) k_record_refines(Dev D, int L, const uint32_t *cand, int compat_tail) {
+__device__ __forceinline__ void record_refines_body(const Dev &D, int L, const uint32_t *cand, int compat_tail, unsigned bx, unsigned gx) {
   const long long limit = D.ctr[C_MOVE_LIMIT];
   if (limit == 0) return;
   const long long n = D.ctr[C_NCAND];
@@ -411,20 +473,21 @@ __global__ void __launch_bounds__(256) k_record_refines(Dev D, int L, const uint
   const long long first = compat_tail ? n - keep : 0;
   const long long base = D.ctr[C_REF_BEGIN + L - 1];
   const long long load0 = D.ctr[C_LOAD0 + L - 1];
-  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < keep; r += (long long)gridDim.x * blockDim.x) {
+  for (long long r = (long long)bx * blockDim.x + threadIdx.x; r < keep; r += (long long)gx * blockDim.x) {
     D.refines[2 * (base + r)] = cand[first + r];
     D.refines[2 * (base + r) + 1] = (uint32_t)(D.g.off[L - 1] + load0 + r);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (bx == 0 && threadIdx.x == 0) {
     D.ctr[C_REFINES] = base + keep;
     D.ctr[C_REF_END + L - 1] = base + keep;
   }
 }
+__global__ void __launch_bounds__(256) k_record_refines(Dev D, int L, const uint32_t *cand, int compat_tail) { record_refines_body(D, L, cand, compat_tail, blockIdx.x, gridDim.x); }
 // k_dcgrid_refine_subblocks + insertBlock (dcgrid_adaptation.cu:145-178,
 // dcgrid_utils.cuh:99-140) for every recorded refinement.
-__global__ void __launch_bounds__(256) k_apply_refines(Dev D) {
+__device__ __forceinline__ void apply_refines_body(const Dev &D, unsigned bx, unsigned gx) {
   const long long nr = D.ctr[C_REFINES], nm = D.ctr[C_MOVES];
-  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < nr; m += (long long)gridDim.x * blockDim.x) {
+  for (long long m = (long long)bx * blockDim.x + threadIdx.x; m < nr; m += (long long)gx * blockDim.x) {
     const uint32_t sb = D.refines[2 * m], cb = D.refines[2 * m + 1];
     const uint32_t pb = sb >> 3;
     const int4 pp = D.pos[pb];
@@ -443,20 +506,22 @@ __global__ void __launch_bounds__(256) k_apply_refines(Dev D) {
     D.touched[nm + m] = cb;
   }
 }
-__global__ void k_finish_refines(Dev D) {
+__global__ void __launch_bounds__(256) k_apply_refines(Dev D) { apply_refines_body(D, blockIdx.x, gridDim.x); }
+__device__ __forceinline__ void finish_refines_body(const Dev &D, unsigned bx, unsigned gx) {
   for (int L = 1; L < D.g.levels; L++) {
     const long long n = D.ctr[C_REF_END + L - 1] - D.ctr[C_REF_BEGIN + L - 1];
     D.load[L - 1] += n;
   }
   D.ctr[C_TOUCHED] = D.ctr[C_MOVES] + D.ctr[C_REFINES];
 }
+__global__ void k_finish_refines(Dev D) { finish_refines_body(D, blockIdx.x, gridDim.x); }
 
 // k_dcgrid_propagate_values (dcgrid_adaptation.cu:92-143): new or moved blocks
 // of one level take 27/9/3/1 interpolations of their parent's apron.
-__global__ void __launch_bounds__(256) k_propagate(Dev D, int level) {
+__device__ __forceinline__ void propagate_body(const Dev &D, int level, unsigned bx, unsigned gx) {
   const long long nt = D.ctr[C_TOUCHED];
   const int c = threadIdx.x & 63;
-  for (long long t = (long long)blockIdx.x * 4 + (threadIdx.x >> 6); t < nt; t += (long long)gridDim.x * 4) {
+  for (long long t = (long long)bx * 4 + (threadIdx.x >> 6); t < nt; t += (long long)gx * 4) {
     const uint32_t b = D.touched[t];
     if (b == NONE) continue;
     const int4 bp = D.pos[b];
@@ -497,6 +562,7 @@ __global__ void __launch_bounds__(256) k_propagate(Dev D, int level) {
     D.w[cell] = fluidity(D.g, D.ph, x, y, z, 1 << level);
   }
 }
+__global__ void __launch_bounds__(256) k_propagate(Dev D, int level) { propagate_body(D, level, blockIdx.x, gridDim.x); }
 
 static unsigned grid_for(long long n, int threads = 256) {
   return (unsigned)((n + threads - 1) / threads);
@@ -540,9 +606,9 @@ void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *
     k_match<<<gs, 256, 0, st>>>(D, vals, vals2);
     k_commit_moves<<<gs, 256, 0, st>>>(D, L, vals, vals2);
   }
-  for (int L = D.g.levels - 2; L >= 0; L--) k_apply_moves<<<gs, 256, 0, st>>>(D, L);
+  for (int L = D.g.levels - 2; L >= 0; L--) k_apply_moves<<<gs, 256, 0, st>>>(D, L, keys);
   // refineSubblocks
-  launch_scores(D, st);
+  k_rescore<<<gs, 256, 0, st>>>(D, keys);
   uint8_t *sel = reinterpret_cast<uint8_t *>(keys2);  // 8*B bytes, reused as selection flags
   for (int L = 1; L < D.g.levels; L++) {
     const long long n8 = 8 * D.g.budget[L];
@@ -569,6 +635,243 @@ void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *
   // neighbour tables + value propagation for touched blocks
   launch_build_nbr(D, true, st);
   for (int L = D.g.levels - 2; L >= 0; L--) k_propagate<<<gs, 256, 0, st>>>(D, L);
+}
+
+// ------------------------------------------------------- batched adaptation
+// launch_adapt's sequence for up to BMAX members, one launch per adaptation
+// kernel: a CTA picks its member from the cumulative CTA counts and runs the
+// single-simulation body with its member-local CTA index and grid size. A
+// member without the launch's level (or of the other selection mode) gets no
+// CTAs. The bodies are the single simulation's, so the results are too.
+enum : int {
+  A_CLEAR, A_SCORES, A_BLOCK_SCORES, A_MOVE_SETUP, A_KEYS, A_MATCH, A_COMMIT, A_APPLY_MOVES, A_REFINE_SETUP,
+  A_CMP_COUNT, A_CMP_SCAN, A_CMP_SCATTER, A_RECORD, A_KEYS_CANDS, A_CLEAR_SEL, A_MARK, A_APPLY_REFINES,
+  A_FINISH, A_NBR, A_PROPAGATE, A_RESCORE
+};
+struct AdaptBatchP {
+  int n, L;
+  long long end[BMAX];
+  uint32_t *p0[BMAX], *p1[BMAX], *p2[BMAX], *p3[BMAX];  // per-op buffers
+  long long nn[BMAX];
+  int arg[BMAX];
+  Dev d[BMAX];
+};
+static_assert(sizeof(AdaptBatchP) < 32000, "kernel parameter space");
+
+// clears the counters and the block flags of one member
+__device__ __forceinline__ void clear_body(const Dev &D, unsigned bx, unsigned gx) {
+  const long long n = D.g.B > C_COUNT ? D.g.B : C_COUNT;
+  for (long long i = (long long)bx * blockDim.x + threadIdx.x; i < n; i += (long long)gx * blockDim.x) {
+    if (i < C_COUNT) D.ctr[i] = 0;
+    if (i < D.g.B) D.flags[i] = 0;
+  }
+}
+
+template <int OP, int T> __global__ void __launch_bounds__(T) k_adapt_batch(const __grid_constant__ AdaptBatchP P) {
+  int s = 0;
+  while (s < P.n - 1 && blockIdx.x >= P.end[s]) s++;
+  const long long first = s ? P.end[s - 1] : 0;
+  const unsigned bx = (unsigned)(blockIdx.x - first), gx = (unsigned)(P.end[s] - first);
+  const Dev &D = P.d[s];
+  const int L = P.L;
+  if constexpr (OP == A_CLEAR) clear_body(D, bx, gx);
+  if constexpr (OP == A_SCORES) {
+    if (D.ph.criterion == 0)
+      scores_geo_body(D, bx, gx);
+    else
+      scores_fields_body(D, bx, gx);
+  }
+  if constexpr (OP == A_BLOCK_SCORES) block_scores_body(D, bx, gx);
+  if constexpr (OP == A_MOVE_SETUP) {
+    if (threadIdx.x == 0) move_setup_body(D, L, bx, gx);
+  }
+  if constexpr (OP == A_KEYS) {  // block keys of level L and destination keys of level L+1
+    const long long nb = (P.nn[s] + T - 1) / T;
+    if (bx < nb)
+      keys_blocks_body(D, L, P.p0[s], P.p1[s], bx, (unsigned)nb);
+    else
+      keys_dests_body(D, L, P.p2[s], P.p3[s], bx - (unsigned)nb, gx - (unsigned)nb);
+  }
+  if constexpr (OP == A_MATCH) match_body(D, P.p0[s], P.p1[s], bx, gx);
+  if constexpr (OP == A_COMMIT) commit_moves_body(D, L, P.p0[s], P.p1[s], bx, gx);
+  if constexpr (OP == A_APPLY_MOVES) apply_moves_body(D, L, P.p0[s], bx, gx);
+  if constexpr (OP == A_RESCORE) rescore_body(D, P.p0[s], bx, gx);
+  if constexpr (OP == A_REFINE_SETUP) {
+    if (threadIdx.x == 0) refine_setup_body(D, L, bx, gx);
+  }
+  if constexpr (OP == A_CMP_COUNT)
+    cmp_count_body(D, L, reinterpret_cast<const uint8_t *>(P.p0[s]), P.p1[s], bx, gx);
+  if constexpr (OP == A_CMP_SCAN) cmp_scan_body(D, P.p1[s], P.nn[s], bx, gx);
+  if constexpr (OP == A_CMP_SCATTER)
+    cmp_scatter_body(D, L, reinterpret_cast<const uint8_t *>(P.p0[s]), P.p1[s], P.p2[s], bx, gx);
+  if constexpr (OP == A_RECORD) record_refines_body(D, L, P.p0[s], P.arg[s], bx, gx);
+  if constexpr (OP == A_KEYS_CANDS) keys_cands_body(D, P.p0[s], P.p1[s], P.p2[s], P.nn[s], bx, gx);
+  if constexpr (OP == A_CLEAR_SEL) {
+    uint32_t *w = P.p0[s];
+    for (long long i = (long long)bx * T + threadIdx.x; i < P.nn[s]; i += (long long)gx * T) w[i] = 0;
+  }
+  if constexpr (OP == A_MARK) mark_selected_body(D, P.p0[s], reinterpret_cast<uint8_t *>(P.p1[s]), bx, gx);
+  if constexpr (OP == A_APPLY_REFINES) apply_refines_body(D, bx, gx);
+  if constexpr (OP == A_FINISH) {
+    if (threadIdx.x == 0) finish_refines_body(D, bx, gx);
+  }
+  if constexpr (OP == A_NBR) build_nbr_body(D, 1, bx, gx);
+  if constexpr (OP == A_PROPAGATE) propagate_body(D, L, bx, gx);
+}
+
+namespace {
+struct AdaptLauncher {
+  const AdaptMember *m;
+  int n;
+  unsigned gs;  // grid-stride CTAs per member
+  cudaStream_t st;
+  AdaptBatchP P{};
+
+  AdaptLauncher(const AdaptMember *mm, int nn, int sms, cudaStream_t s) : m(mm), n(nn), st(s) {
+    P.n = n;
+    for (int i = 0; i < n; i++) P.d[i] = m[i].D;
+    const int total = sms > 0 ? sms * 4 : 512;
+    gs = (unsigned)std::max(32, (total + n - 1) / n);
+  }
+  // CTA counts from ctas(i) (0 = member i sits the launch out); false when no CTA runs
+  template <typename F> bool counts(F ctas) {
+    long long e = 0;
+    for (int i = 0; i < n; i++) {
+      e += ctas(i);
+      P.end[i] = e;
+    }
+    return e > 0;
+  }
+  template <int OP, int T = 256, typename F> void go(F ctas) {
+    if (counts(ctas)) k_adapt_batch<OP, T><<<(unsigned)P.end[n - 1], T, 0, st>>>(P);
+  }
+  int levels(int i) const { return m[i].D.g.levels; }
+  long long B(int i) const { return m[i].D.g.B; }
+
+  void scores() {
+    go<A_SCORES>([&](int i) {
+      return (long long)grid_for(m[i].D.ph.criterion == 0 ? 8 * B(i) + 1 : 64 * B(i) + 1);
+    });
+  }
+  // compaction of level L's flagged subblocks (sel null: threshold test) into p2
+  void compact(int L, bool sel, const std::vector<bool> &in) {
+    auto nt = [&](int i) { return (8 * m[i].D.g.budget[L] + CMP_TILE - 1) / CMP_TILE; };
+    for (int i = 0; i < n; i++) {
+      P.p0[i] = sel ? m[i].keys2 : nullptr;
+      P.p1[i] = m[i].S.tile_sums;
+      P.p2[i] = m[i].vals;
+      P.nn[i] = nt(i);
+    }
+    go<A_CMP_COUNT>([&](int i) { return in[i] ? nt(i) : 0; });
+    go<A_CMP_SCAN, 1024>([&](int i) { return in[i] ? 1 : 0; });
+    go<A_CMP_SCATTER>([&](int i) { return in[i] ? nt(i) : 0; });
+  }
+
+  void run() {
+    int maxl = 0;
+    for (int i = 0; i < n; i++) maxl = std::max(maxl, levels(i));
+    go<A_CLEAR>([&](int i) { return (long long)std::min<long long>(gs, grid_for(std::max<long long>(B(i), C_COUNT))); });
+    // moveBlocks
+    scores();
+    go<A_BLOCK_SCORES>([&](int i) { return (long long)grid_for(B(i)); });
+    for (int L = 0; L < maxl - 1; L++) {
+      P.L = L;
+      auto has = [&](int i) { return L < levels(i) - 1; };
+      go<A_MOVE_SETUP, 32>([&](int i) { return has(i) ? 1 : 0; });
+      for (int i = 0; i < n; i++) {
+        P.p0[i] = m[i].keys;
+        P.p1[i] = m[i].vals;
+        P.p2[i] = m[i].keys2;
+        P.p3[i] = m[i].vals2;
+        P.nn[i] = m[i].D.g.budget[L];
+      }
+      go<A_KEYS>([&](int i) {
+        return has(i) ? (long long)grid_for(m[i].D.g.budget[L]) + grid_for(8 * m[i].D.g.budget[L + 1]) : 0;
+      });
+      SortSeg seg[SORT_SEGS];
+      int ns = 0;
+      for (int i = 0; i < n; i++) {
+        if (!has(i)) continue;
+        const long long *act = m[i].D.ctr + C_MOVE_LIMIT;
+        seg[ns++] = SortSeg{m[i].keys, m[i].vals, m[i].D.g.budget[L], act, m[i].S2};
+        seg[ns++] = SortSeg{m[i].keys2, m[i].vals2, 8 * m[i].D.g.budget[L + 1], act, m[i].S};
+      }
+      launch_radix_sort_batch(seg, ns, st);
+      for (int i = 0; i < n; i++) {
+        P.p0[i] = m[i].vals;
+        P.p1[i] = m[i].vals2;
+      }
+      go<A_MATCH>([&](int i) { return has(i) ? gs : 0u; });
+      go<A_COMMIT>([&](int i) { return has(i) ? gs : 0u; });
+    }
+    for (int i = 0; i < n; i++) P.p0[i] = m[i].keys;  // previous parents of the moved blocks
+    for (int L = maxl - 2; L >= 0; L--) {
+      P.L = L;
+      go<A_APPLY_MOVES>([&](int i) { return L < levels(i) - 1 ? gs : 0u; });
+    }
+    // refineSubblocks
+    go<A_RESCORE>([&](int i) { return gs; });
+    for (int L = 1; L < maxl; L++) {
+      P.L = L;
+      std::vector<bool> in(n), compat(n), score(n);
+      for (int i = 0; i < n; i++) {
+        in[i] = L < levels(i);
+        compat[i] = in[i] && m[i].D.g.ref_compat;
+        score[i] = in[i] && !m[i].D.g.ref_compat;
+      }
+      go<A_REFINE_SETUP, 32>([&](int i) { return in[i] ? 1 : 0; });
+      compact(L, false, in);
+      for (int i = 0; i < n; i++) {
+        P.p0[i] = m[i].vals;
+        P.arg[i] = 1;
+      }
+      go<A_RECORD>([&](int i) { return compat[i] ? gs : 0u; });
+      if (std::none_of(score.begin(), score.end(), [](bool b) { return b; })) continue;
+      for (int i = 0; i < n; i++) {
+        P.p0[i] = m[i].vals;
+        P.p1[i] = m[i].keys;
+        P.p2[i] = m[i].vals2;
+        P.nn[i] = 8 * m[i].D.g.budget[L];
+      }
+      go<A_KEYS_CANDS>([&](int i) { return score[i] ? gs : 0u; });
+      SortSeg seg[SORT_SEGS];
+      int ns = 0;
+      for (int i = 0; i < n; i++)
+        if (score[i])
+          seg[ns++] = SortSeg{m[i].keys, m[i].vals2, 8 * m[i].D.g.budget[L], m[i].D.ctr + C_MOVE_LIMIT, m[i].S};
+      launch_radix_sort_batch(seg, ns, st);
+      for (int i = 0; i < n; i++) {
+        P.p0[i] = m[i].keys2;
+        P.nn[i] = 2 * B(i);  // 8*B selection bytes as words
+      }
+      go<A_CLEAR_SEL>([&](int i) { return score[i] ? gs : 0u; });
+      for (int i = 0; i < n; i++) {
+        P.p0[i] = m[i].vals2;
+        P.p1[i] = m[i].keys2;
+      }
+      go<A_MARK>([&](int i) { return score[i] ? gs : 0u; });
+      compact(L, true, score);
+      for (int i = 0; i < n; i++) {
+        P.p0[i] = m[i].vals;
+        P.arg[i] = 0;
+      }
+      go<A_RECORD>([&](int i) { return score[i] ? gs : 0u; });
+    }
+    go<A_APPLY_REFINES>([&](int i) { return gs; });
+    go<A_FINISH, 32>([&](int i) { return 1; });
+    // neighbour tables + value propagation for touched blocks
+    go<A_NBR>([&](int i) { return (long long)grid_for(B(i) * 27); });
+    for (int L = maxl - 2; L >= 0; L--) {
+      P.L = L;
+      go<A_PROPAGATE>([&](int i) { return L < levels(i) - 1 ? gs : 0u; });
+    }
+  }
+};
+}  // namespace
+
+void launch_adapt_batch(const AdaptMember *m, int n, int sms, cudaStream_t st) {
+  if (n <= 0 || n > BMAX) return;
+  AdaptLauncher(m, n, sms, st).run();
 }
 
 // ------------------------------------------------------------------ stats
