@@ -500,6 +500,27 @@ int dcg_launches_per_step(dcg_sim *s, int64_t *n) {
   return DCG_OK;
 }
 
+int dcg_check_div6(uint64_t *mismatches, uint32_t *first) {
+  if (!mismatches || !first) return DCG_E_INVALID;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return DCG_E_CUDA;
+  unsigned long long *d = nullptr, h[2] = {0, 0xFFFFFFFFull};
+  if (cudaMalloc(&d, sizeof h) != cudaSuccess) return DCG_E_CUDA;
+  cudaError_t e = cudaMemcpy(d, h, sizeof h, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    launch_check_div6(d, sms, 0);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return DCG_E_CUDA;
+  *mismatches = h[0];
+  *first = (uint32_t)h[1];
+  return DCG_OK;
+}
+
 size_t dcg_sizeof_params(void) { return sizeof(dcg_params); }
 size_t dcg_sizeof_info(void) { return sizeof(dcg_info); }
 size_t dcg_sizeof_stats(void) { return sizeof(dcg_stats); }

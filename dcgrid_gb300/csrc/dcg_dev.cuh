@@ -233,6 +233,23 @@ __device__ inline uint32_t descend(const Dev &D, uint32_t b, int &l, int qx, int
   return b;
 }
 
+// x / 6, correctly rounded, by the method for divisors known in advance of
+// Brisebarre, Muller and Raina (IEEE Trans. Computers 53(8), 2004): q =
+// RN(x z) with z = RN(1/6), the remainder x - 6q exactly by one FMA, then
+// RN(q + r z). The method assumes no underflow: inputs below 2^-120 in
+// magnitude (subnormal quotients, signed zeros) take the IEEE division.
+// Infinite x gives a NaN remainder; q (= x / 6 for those) is returned then.
+// The library's self-check (dcg_check_div6) compares the result with the
+// IEEE division over every binary32 input.
+__device__ __forceinline__ float div6(float x) {
+  if (!(fabsf(x) >= 0x1p-120f) && x == x) return x / 6.f;
+  const float z = 0x1.555556p-3f;
+  const float q = __fmul_rn(x, z);
+  const float r = fmaf(-q, 6.f, x);
+  const float y = fmaf(r, z, q);
+  return r == r ? y : q;
+}
+
 __device__ inline int dir_of(int a) { return a == 0 ? 0 : (a == AW - 1 ? 2 : 1); }
 
 // Global cell index of apron cell (ax, ay, az) in [0,6)^3 of block b.
@@ -357,6 +374,18 @@ __device__ inline void vel_bc(const Geom &g, const Phys &P, float &vx, float &vy
     if (x * scale >= g.gx) return;
   }
   if (outside(g, x, y, z, scale)) vx = vy = vz = 0.f;
+}
+// component `comp` of vel_bc alone (each output component of vel_bc depends
+// only on its own input component)
+__device__ inline float vel_bc1(const Geom &g, const Phys &P, float v, int comp, int x, int y, int z,
+                                int scale) {
+  if (in_inlet(g, P, x, y, z, scale)) return comp == 1 ? P.v_emit : 0.f;
+  if (P.wind && yz_inside(g, y, z, scale)) {
+    if (x < 0) return P.wind_v[comp];
+    if (x * scale >= g.gx) return v;
+  }
+  if (outside(g, x, y, z, scale)) return 0.f;
+  return v;
 }
 // densityBndCond (sim_utils.cu:41-55) + wind extension; scalar k
 __device__ inline float q_bc(const Geom &g, const Phys &P, float q, int k, int x, int y, int z,
@@ -509,6 +538,14 @@ __device__ inline void corner_of(const Smp &s, int c, int &x, int &y, int &z) {
   z = (c & 1) ? s.z1 : s.z0;
 }
 
+// The sample's 2x2x2 corner box lies inside the domain: then no corner is in
+// the inlet (y < 0), left of a wind inflow (x < 0) or outside, and the
+// boundary conditions of every corner return the sampled values unchanged.
+__device__ __forceinline__ bool box_inside(const Geom &g, const Smp &s) {
+  return s.x0 >= 0 && s.y0 >= 0 && s.z0 >= 0 && s.x1 * s.scale < g.gx && s.y1 * s.scale < g.gy &&
+         s.z1 * s.scale < g.gz;
+}
+
 // Back-trace (dcgrid_fluid.cu:115-122): (pos + .5) * scale - v * dt * rdx.
 __device__ inline void back_trace(const Dev &D, int4 bp, int c, size_t cell, float &px, float &py,
                                   float &pz) {
@@ -525,37 +562,42 @@ __device__ inline void back_trace(const Dev &D, int4 bp, int c, size_t cell, flo
 // k_dcgrid_debug_stats (dcgrid_structure.cu:224-251) for one cell of block b,
 // plus mass and leaf counts, reduced per warp into D.red (every lane of the
 // warp calls this; a warp covers half of one block).
-// Warp totals of the statistics of k_dcgrid_debug_stats (dcgrid_structure.cu:224-251)
-// plus mass and leaf counts; every lane receives them. A warp covers half of
-// one block, so all its leaf cells share one level (lvl, cnt leaf cells).
+// Statistics of one cell: for a leaf cell, scale * |residual| with the FP32
+// arithmetic of k_dcgrid_debug_stats (dcgrid_structure.cu:224-251), and its
+// mass rho * w * scale^3 (extension); returns the cell's level, -1 when the
+// cell is not a leaf (both values 0 then).
+__device__ inline int stats_vals(const Dev &D, long long b, int c, float &res, float &mass) {
+  res = mass = 0.f;
+  if (b >= D.g.B) return -1;
+  const int4 bp = D.pos[b];
+  const size_t cell = (size_t)b * BV + c;
+  if (bp.w < 0 || D.child[cell >> 3] != NONE) return -1;
+  int lx, ly, lz;
+  local_xyz(c, lx, ly, lz);
+  const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+  const int scale = 1 << bp.w;
+  const float alpha = D.ph.rdx * D.ph.rdx / (float)(scale * scale);
+  const float *P = D.p;
+  const float pc = P[cell];
+  const float pl = P[apron_cell(D, (uint32_t)b, bp, ax - 1, ay, az)];
+  const float pr = P[apron_cell(D, (uint32_t)b, bp, ax + 1, ay, az)];
+  const float pd = P[apron_cell(D, (uint32_t)b, bp, ax, ay - 1, az)];
+  const float pu = P[apron_cell(D, (uint32_t)b, bp, ax, ay + 1, az)];
+  const float pb = P[apron_cell(D, (uint32_t)b, bp, ax, ay, az - 1)];
+  const float pf = P[apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1)];
+  const float r = D.div[cell] - (pl + pr + pd + pu + pb + pf - 6.f * pc) * alpha;
+  res = (float)scale * fabsf(r);
+  mass = q_ld(D, 0, cell) * D.w[cell] * (float)(scale * scale * scale);
+  return bp.w;
+}
+// Warp totals of stats_vals (FP64 sums); every lane receives them. A warp
+// covers half of one block, so all its leaf cells share one level (lvl, cnt
+// leaf cells).
 struct WarpStats {
   double res, mass;
   int lvl, cnt;
 };
-__device__ inline WarpStats stats_warp(const Dev &D, long long b, int c) {
-  double res = 0.0, mass = 0.0;
-  int lev = -1;
-  if (b < D.g.B) {
-    const int4 bp = D.pos[b];
-    const size_t cell = (size_t)b * BV + c;
-    if (bp.w >= 0 && D.child[cell >> 3] == NONE) {
-      lev = bp.w;
-      int lx, ly, lz;
-      local_xyz(c, lx, ly, lz);
-      const int ax = lx + 1, ay = ly + 1, az = lz + 1;
-      const int scale = 1 << bp.w;
-      const double alpha = (double)D.ph.rdx * (double)D.ph.rdx / (double)(scale * scale);
-      const float *P = D.p;
-      const double lap = (double)P[apron_cell(D, (uint32_t)b, bp, ax - 1, ay, az)] +
-                         P[apron_cell(D, (uint32_t)b, bp, ax + 1, ay, az)] +
-                         P[apron_cell(D, (uint32_t)b, bp, ax, ay - 1, az)] +
-                         P[apron_cell(D, (uint32_t)b, bp, ax, ay + 1, az)] +
-                         P[apron_cell(D, (uint32_t)b, bp, ax, ay, az - 1)] +
-                         P[apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1)] - 6.0 * P[cell];
-      res = (double)scale * fabs((double)D.div[cell] - lap * alpha);
-      mass = (double)q_ld(D, 0, cell) * (double)D.w[cell] * scale * scale * scale;
-    }
-  }
+__device__ inline WarpStats warp_sum_stats(double res, double mass, int lev) {
   for (int o = 16; o > 0; o >>= 1) {
     res += __shfl_xor_sync(0xffffffffu, res, o);
     mass += __shfl_xor_sync(0xffffffffu, mass, o);
@@ -567,6 +609,11 @@ __device__ inline WarpStats stats_warp(const Dev &D, long long b, int c) {
   w.cnt = __popc(leafmask);
   w.lvl = __shfl_sync(0xffffffffu, lev, leafmask ? __ffs(leafmask) - 1 : 0);
   return w;
+}
+__device__ inline WarpStats stats_warp(const Dev &D, long long b, int c) {
+  float r, m;
+  const int lev = stats_vals(D, b, c, r, m);
+  return warp_sum_stats((double)r, (double)m, lev);
 }
 // adds warp totals into the member's reduction slots (lane 0)
 __device__ inline void stats_flush(const Dev &D, double res, double mass, int lvl, double cnt) {

@@ -96,6 +96,9 @@ int batch_solve_grid(int sms, int cache, int ctas_per_sm);
 void launch_level_solve_batch(const SolveBatch &P, int round, int sweeps, int grid, int cache, int tree,
                               cudaStream_t st);
 
+// self-check of the solver's division by six: bad[0] += mismatches, bad[1] = min mismatching input
+void launch_check_div6(unsigned long long *bad, int sms, cudaStream_t st);
+
 // k_topology.cu
 void launch_init_blocks(const Dev &D, cudaStream_t st);
 void launch_activate_level(const Dev &D, int level, cudaStream_t st);

@@ -24,12 +24,13 @@ __device__ __forceinline__ void advect_velocity_cell(const Dev &D, long long b, 
     Smp s;
     sample_at(D, (uint32_t)b, bp, px, py, pz, s);
     if (!(s.wAcc < 1e-6f)) {
+      const bool inside = box_inside(D.g, s);
 #pragma unroll
       for (int k = 0; k < 8; k++) {
         int x, y, z;
         corner_of(s, k, x, y, z);
         float vx = D.v[0][s.idx[k]], vy = D.v[1][s.idx[k]], vz = D.v[2][s.idx[k]];
-        vel_bc(D.g, D.ph, vx, vy, vz, x, y, z, s.scale);
+        if (!inside) vel_bc(D.g, D.ph, vx, vy, vz, x, y, z, s.scale);
         if (k == 0) {
           o0 = vx * s.wt[0]; o1 = vy * s.wt[0]; o2 = vz * s.wt[0];
         } else {
@@ -87,11 +88,12 @@ __device__ __forceinline__ void advect_scalars_cell_t(const Dev &D, long long b,
     if (!(s.wAcc < 1e-6f)) {
       // per scalar the sum runs over the corners in order, as in
       // k_dcgrid_advect_density (dcgrid_fluid.cu:129-144)
+      const bool inside = box_inside(D.g, s);
 #pragma unroll
       for (int k = 0; k < 8; k++) {
         int x, y, z;
         corner_of(s, k, x, y, z);
-        const int mode = q_bc_mode(D.g, D.ph, x, y, z, s.scale);
+        const int mode = inside ? 0 : q_bc_mode(D.g, D.ph, x, y, z, s.scale);
 #pragma unroll
         for (int kq = 0; kq < NQ; kq++) {
           const float qc = mode == 0 ? q_ldm<MODE>(D, kq, s.idx[k]) : (mode == 1 && kq == 0 ? D.ph.d_emit : 0.f);
@@ -218,10 +220,10 @@ __device__ __forceinline__ void divergence_cell(const Dev &D, long long b, int c
       const unsigned long long nc = apron_cell(D, (uint32_t)b, bp, i, j, k);
       nbw[n] = D.w[nc];
       const int comp = n >> 1;
-      float vx = D.v[0][nc], vy = D.v[1][nc], vz = D.v[2][nc];
+      float v = D.v[comp][nc];
       if (i == 0 || i == AW - 1 || j == 0 || j == AW - 1 || k == 0 || k == AW - 1)
-        vel_bc(D.g, D.ph, vx, vy, vz, x + off[n][0], y + off[n][1], z + off[n][2], scale);
-      nbv[n] = comp == 0 ? vx : (comp == 1 ? vy : vz);
+        v = vel_bc1(D.g, D.ph, v, comp, x + off[n][0], y + off[n][1], z + off[n][2], scale);
+      nbv[n] = v;
     }
     dv = alpha * (nbw[1] * nbv[1] - nbw[0] * nbv[0] + nbw[3] * nbv[3] - nbw[2] * nbv[2] +
                   nbw[5] * nbv[5] - nbw[4] * nbv[4]);
@@ -251,7 +253,7 @@ __global__ void __launch_bounds__(256) k_jacobi(Dev D, int level, const float *_
   const float pb = src[apron_cell(D, (uint32_t)b, bp, ax, ay, az - 1)];
   const float pf = src[apron_cell(D, (uint32_t)b, bp, ax, ay, az + 1)];
   const size_t cell = (size_t)b * BV + c;
-  dst[cell] = (pl + pr + pd + pu + pb + pf - alpha * D.div[cell]) / 6.f;
+  dst[cell] = div6(pl + pr + pd + pu + pb + pf - alpha * D.div[cell]);
 }
 
 // k_dcgrid_prolongate (dcgrid_multigrid_solver.cu:43-76): 27/9/3/1 trilinear
@@ -332,8 +334,8 @@ __device__ inline Nb6 jacobi_neighbours(const Dev &D, long long cell) {
 // Loads go through L2 (__ldcg): inside one persistent launch the ping-pong
 // buffers are rewritten by other SMs, so no SM may serve them from its L1.
 __device__ inline float jacobi_update(const float *src, const Nb6 &n, float ad) {
-  return (__ldcg(src + n.i0) + __ldcg(src + n.i1) + __ldcg(src + n.i2) + __ldcg(src + n.i3) + __ldcg(src + n.i4) +
-          __ldcg(src + n.i5) - ad) / 6.f;
+  return div6(__ldcg(src + n.i0) + __ldcg(src + n.i1) + __ldcg(src + n.i2) + __ldcg(src + n.i3) +
+              __ldcg(src + n.i4) + __ldcg(src + n.i5) - ad);
 }
 
 __device__ inline uint32_t ld_acquire_u32(const uint32_t *p) {
@@ -653,10 +655,20 @@ __global__ void __launch_bounds__(64 * TB) k_cells_persist(const __grid_constant
   __syncthreads();
   const long long total = s_end[nseg - 1];
   const int c = threadIdx.x & 63;
-  // statistics: warp totals accumulate in registers while the member and
-  // level stay the same and are flushed with one atomic per quantity
-  double a_res = 0.0, a_mass = 0.0, a_cnt = 0.0;
-  int a_mem = -1, a_lvl = 0;
+  // statistics: every thread sums its cells' values in FP64 registers while
+  // the warp's member and level stay the same; a change (and the end) reduces
+  // the warp's sums and adds them with one atomic per quantity
+  double a_res = 0.0, a_mass = 0.0;
+  int a_cnt = 0, a_mem = -1, a_lvl = 0;
+  auto flush = [&]() {
+    double r = a_res, m = a_mass;
+    for (int o = 16; o > 0; o >>= 1) {
+      r += __shfl_xor_sync(0xffffffffu, r, o);
+      m += __shfl_xor_sync(0xffffffffu, m, o);
+    }
+    const int n = (int)__reduce_add_sync(0xffffffffu, (unsigned)a_cnt);
+    stats_flush(P.d[a_mem], r, m, a_lvl, (double)n);
+  };
   for (long long t = blockIdx.x; t < total; t += gridDim.x) {
     int lo = 0, hi = nseg - 1;
     while (lo < hi) {
@@ -675,22 +687,26 @@ __global__ void __launch_bounds__(64 * TB) k_cells_persist(const __grid_constant
     else if (STAGE == 2) divergence_cell(D, b, c);
     else if (STAGE == 3) apply_pressure_cell(D, b, c);
     else {
-      const WarpStats w = stats_warp(D, b, c);
-      const int mem = lo / MAXL;
-      if (w.cnt) {
-        if (mem != a_mem || w.lvl != a_lvl) {
-          if (a_mem >= 0) stats_flush(P.d[a_mem], a_res, a_mass, a_lvl, a_cnt);
+      float r, m;
+      const int lev = stats_vals(D, b, c, r, m);
+      const unsigned leaf = __ballot_sync(0xffffffffu, lev >= 0);
+      if (leaf) {  // warp-uniform: a warp covers half of one block
+        const int lvl = __shfl_sync(0xffffffffu, lev, __ffs(leaf) - 1);
+        const int mem = lo / MAXL;
+        if (mem != a_mem || lvl != a_lvl) {
+          if (a_mem >= 0) flush();
           a_mem = mem;
-          a_lvl = w.lvl;
-          a_res = a_mass = a_cnt = 0.0;
+          a_lvl = lvl;
+          a_res = a_mass = 0.0;
+          a_cnt = 0;
         }
-        a_res += w.res;
-        a_mass += w.mass;
-        a_cnt += (double)w.cnt;
+        a_res += (double)r;
+        a_mass += (double)m;
+        a_cnt += lev >= 0;
       }
     }
   }
-  if (STAGE == 4 && a_mem >= 0) stats_flush(P.d[a_mem], a_res, a_mass, a_lvl, a_cnt);
+  if (STAGE == 4 && a_mem >= 0) flush();
 }
 
 __global__ void __launch_bounds__(128) k_stats_zero(const __grid_constant__ CellBatch P) {
@@ -995,8 +1011,8 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
           const float a = cur.own_v[u].x, b = cur.own_v[u].y;
           const float adA = cur.alpha[u] * cur.dv[u].x, adB = cur.alpha[u] * cur.dv[u].y;
           float2 res;
-          res.x = (L.x + R.x + Dn.x + Up.x + Bk + b - adA) / 6.f;
-          res.y = (L.y + R.y + Dn.y + Up.y + a + Fw - adB) / 6.f;
+          res.x = div6(L.x + R.x + Dn.x + Up.x + Bk + b - adA);
+          res.y = div6(L.y + R.y + Dn.y + Up.y + a + Fw - adB);
           reinterpret_cast<float2 *>(dst + cur.own[u])[lane] = res;
         }
         __syncwarp();
@@ -1005,6 +1021,26 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
       if (it + 1 < sweeps) barrier();
     }
   }
+}
+
+// Self-check of div6: every binary32 bit pattern against the IEEE division
+// (NaN results compare equal whatever their payload).
+__global__ void __launch_bounds__(256) k_check_div6(unsigned long long *bad) {
+  unsigned long long n = 0;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long u = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; u < (1ull << 32);
+       u += stride) {
+    const float x = __uint_as_float((uint32_t)u);
+    const float a = x / 6.f, b = div6(x);
+    if (__float_as_uint(a) != __float_as_uint(b) && !(a != a && b != b)) {
+      n++;
+      atomicMin(bad + 1, u);
+    }
+  }
+  if (n) atomicAdd(bad, n);
+}
+void launch_check_div6(unsigned long long *bad, int sms, cudaStream_t st) {
+  k_check_div6<<<(unsigned)(sms > 0 ? sms * 8 : 1024), 256, 0, st>>>(bad);
 }
 
 template <int TB, int STAGE> static unsigned persist_grid() {

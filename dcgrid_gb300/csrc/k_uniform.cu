@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(256) k_u_jacobi(UDev U, int level, const float
   const size_t id = y > 0 ? idx - w : idx, iu = y < h - 1 ? idx + w : idx;
   const size_t ib = z > 0 ? idx - (size_t)w * h : idx, iff = z < d - 1 ? idx + (size_t)w * h : idx;
   const float alpha = U.ph.dx * U.ph.dx * (float)s * (float)s;
-  dst[idx] = (src[il] + src[ir] + src[id] + src[iu] + src[ib] + src[iff] - alpha * U.div[idx]) / 6.f;
+  dst[idx] = div6(src[il] + src[ir] + src[id] + src[iu] + src[ib] + src[iff] - alpha * U.div[idx]);
 }
 
 // k_uniform_prolongate (uniformgrid_fluid.cu:206-237)

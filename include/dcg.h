@@ -292,6 +292,13 @@ int dcg_time_kernel(dcg_sim *sim, int32_t which, int32_t level, int32_t reps,
 /* Number of kernel launches one dcg_step performs (kernel nodes of the
  * captured step graph; 0 before the first graph capture). */
 int dcg_launches_per_step(dcg_sim *sim, int64_t *n);
+/* Self-check of the solver arithmetic on the current device: the Jacobi
+ * update divides by six with a multiply and two FMAs (a correctly rounded
+ * method for a divisor known in advance) instead of the IEEE division. Runs
+ * both over every binary32 input; *mismatches = inputs whose results differ
+ * (NaNs compare equal), *first = the smallest such input's bit pattern
+ * (0xFFFFFFFF when none). */
+int dcg_check_div6(uint64_t *mismatches, uint32_t *first);
 /* ---- batches: many independent adaptive simulations stepped together -----
  * No reference counterpart: the reference runs one simulation per process
  * (one global __constant__ parameter set, src/utils/sim_utils.h:5-6). A batch

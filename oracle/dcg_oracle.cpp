@@ -1685,7 +1685,8 @@ template <typename R> struct DC : Base {
       i->offset[l] = off[l];
     }
   }
-  // k_dcgrid_debug_stats (dcgrid_structure.cu:224-251) + leaf counts and mass.
+  // k_dcgrid_debug_stats (dcgrid_structure.cu:224-251) in the precision R
+  // (its FP32 arithmetic for R = float) + leaf counts and mass; FP64 sums.
   int stats(dcg_stats *st) override {
     std::memset(st, 0, sizeof(*st));
     double res = 0, mass = 0;
@@ -1693,7 +1694,7 @@ template <typename R> struct DC : Base {
     for (int64_t b = 0; b < B; b++) {
       if (lvl[b] == FREE) continue;
       const int scale = 1 << lvl[b];
-      const double alpha = (double)rdx_f * (double)rdx_f / (double)(scale * scale);
+      const R alpha = (R)rdx_f * (R)rdx_f / (R)(scale * scale);
       for (int c = 0; c < BV; c++) {
         const size_t cell = (size_t)b * BV + c;
         if (!leaf(cell)) continue;
@@ -1701,11 +1702,12 @@ template <typename R> struct DC : Base {
         int lx, ly, lz;
         local_xyz(c, lx, ly, lz);
         const int ax = lx + 1, ay = ly + 1, az = lz + 1;
-        const double lap = (double)p[apr(b, ax - 1, ay, az)] + p[apr(b, ax + 1, ay, az)] +
-                           p[apr(b, ax, ay - 1, az)] + p[apr(b, ax, ay + 1, az)] +
-                           p[apr(b, ax, ay, az - 1)] + p[apr(b, ax, ay, az + 1)] - 6.0 * p[cell];
-        res += scale * std::fabs((double)dv[cell] - lap * alpha);
-        mass += (double)q[0][cell] * (double)w[cell] * scale * scale * scale;
+        const R lap = p[apr(b, ax - 1, ay, az)] + p[apr(b, ax + 1, ay, az)] + p[apr(b, ax, ay - 1, az)] +
+                      p[apr(b, ax, ay + 1, az)] + p[apr(b, ax, ay, az - 1)] + p[apr(b, ax, ay, az + 1)] -
+                      (R)6 * p[cell];
+        const R r = dv[cell] - lap * alpha;
+        res += (double)((R)scale * std::fabs(r));
+        mass += (double)(q[0][cell] * w[cell] * (R)(scale * scale * scale));
       }
     }
     for (int l = 0; l < levels; l++) {

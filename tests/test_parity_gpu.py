@@ -266,3 +266,15 @@ def test_defect_residuals_match_the_oracle():
     a, b = g.stats().defect_rel_residual, o.stats().defect_rel_residual
     assert a[1] < a[0]
     assert list(a) == pytest.approx(list(b), rel=1e-6)
+
+
+def test_division_by_six_matches_ieee_for_every_input():
+    """The Jacobi update divides by six with a multiply and two FMAs; over all
+    2^32 binary32 inputs it must give the IEEE quotient (NaN payloads aside)."""
+    import ctypes as C
+    from dcgrid_gb300.sim import lib
+    L = lib()
+    L.dcg_check_div6.argtypes = [C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]
+    bad, first = C.c_uint64(), C.c_uint32()
+    assert L.dcg_check_div6(C.byref(bad), C.byref(first)) == capi.DCG_OK
+    assert bad.value == 0, f"{bad.value} mismatches, first input bits {first.value:#010x}"
