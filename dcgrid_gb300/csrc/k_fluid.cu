@@ -793,6 +793,36 @@ __device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long 
 #define DCG_TILE_SY 8
 #endif
 
+// Lane layout of the staged block kernels (one warp per block of 64 cells):
+// lane owns the z-adjacent cells c = 2*lane, 2*lane+1, the first at tile
+// offset oA of a 6^3 tile with strides SX, SY, 1 (and +1 so that the pair is
+// 8-byte aligned). Halo slot q = 0..2 of the lane is halo cell h = lane + 32q
+// of the block's 96 face-halo cells, face f = h >> 4 (-x, +x, -y, +y, -z,
+// +z, so slot q covers the two faces of axis q). hpk: tile position (9 bits)
+// | cell in a same-level neighbour << 9 | clamped own cell << 15 | compat-
+// quirk own cell << 21; hax: apron coordinates ax | ay << 4 | az << 8 | f << 12.
+template <int SX, int SY>
+__device__ __forceinline__ void halo_slots(int lane, int &oA, uint32_t hpk[3], uint32_t hax[3]) {
+  {
+    int x, y, z;
+    local_xyz(2 * lane, x, y, z);
+    oA = (x + 1) * SX + (y + 1) * SY + (z + 1) + 1;
+  }
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    const int h = lane + 32 * q;
+    const int f = h >> 4, i = 1 + ((h >> 2) & 3), j = 1 + (h & 3);
+    const int side = (f & 1) ? AW - 1 : 0;
+    const int ax = f < 2 ? side : i, ay = f < 2 ? i : (f < 4 ? side : j), az = f < 4 ? j : side;
+    const int same = local_of((ax - 1) & 3, (ay - 1) & 3, (az - 1) & 3);
+    const int self = local_of(clampi(ax, 1, BW) - 1, clampi(ay, 1, BW) - 1, clampi(az, 1, BW) - 1);
+    const int quirk = local_of(clampi(ax, 1, BW) & 3, clampi(ay, 1, BW) & 3, clampi(az, 1, BW) & 3);
+    hpk[q] = (uint32_t)(ax * SX + ay * SY + az + 1) | ((uint32_t)same << 9) | ((uint32_t)self << 15) |
+             ((uint32_t)quirk << 21);
+    hax[q] = (uint32_t)ax | ((uint32_t)ay << 4) | ((uint32_t)az << 8) | ((uint32_t)f << 12);
+  }
+}
+
 // One round of the batched cascade: level maxtop - round of every member that
 // has it, optional prolongation from the member's parent level, then `sweeps`
 // Jacobi sweeps over the concatenated cells of all members, separated by grid
@@ -888,27 +918,8 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
     __shared__ uint32_t s_scratch[W][U][BI_WORDS];
     const int w = t >> 5, lane = t & 31;
     int oA;
-    {
-      int x, y, z;
-      local_xyz(2 * lane, x, y, z);
-      oA = (x + 1) * SX + (y + 1) * SY + (z + 1) + 1;
-    }
-    // halo slots h = lane + 32q: tile position, cell in a same-level
-    // neighbour, clamped own cell, compat-quirk own cell; apron coords + face
     uint32_t hpk[3], hax[3];
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-      const int h = lane + 32 * q;
-      const int f = h >> 4, i = 1 + ((h >> 2) & 3), j = 1 + (h & 3);
-      const int side = (f & 1) ? AW - 1 : 0;
-      const int ax = f < 2 ? side : i, ay = f < 2 ? i : (f < 4 ? side : j), az = f < 4 ? j : side;
-      const int same = local_of((ax - 1) & 3, (ay - 1) & 3, (az - 1) & 3);
-      const int self = local_of(clampi(ax, 1, BW) - 1, clampi(ay, 1, BW) - 1, clampi(az, 1, BW) - 1);
-      const int quirk = local_of(clampi(ax, 1, BW) & 3, clampi(ay, 1, BW) & 3, clampi(az, 1, BW) & 3);
-      hpk[q] = (uint32_t)(ax * SX + ay * SY + az + 1) | ((uint32_t)same << 9) | ((uint32_t)self << 15) |
-               ((uint32_t)quirk << 21);
-      hax[q] = (uint32_t)ax | ((uint32_t)ay << 4) | ((uint32_t)az << 8) | ((uint32_t)f << 12);
-    }
+    halo_slots<SX, SY>(lane, oA, hpk, hax);
     const long long nblocks = total >> 6;
     const int rounds_b = (int)((nblocks + (long long)W * nctas - 1) / ((long long)W * nctas));
     // block descriptions: in shared memory when they fit, else built once
@@ -1023,6 +1034,174 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
   }
 }
 
+// ------------------------------------------------------ staged cell stages
+// Divergence (STAGE 2) and pressure application (STAGE 3) one warp per
+// block: lanes 0-5 read the block's six face entries of the neighbour table
+// once, every lane resolves its three halo cells from them (apron_cell for a
+// known face), and the block's values and face halo go through a shared 6^3
+// tile, so a cell's six neighbours are tile reads instead of six neighbour
+// resolutions. The arithmetic of divergence_cell / apply_pressure_cell is
+// kept operation for operation (identical results). Persistent: warps walk
+// the allocated blocks of every (member, level) segment.
+__device__ __forceinline__ size_t halo_cell(const Dev &D, uint32_t b, int4 bp, uint32_t e, uint32_t pk,
+                                            uint32_t ga) {
+  if (e == OUT) {
+    const uint32_t li = (D.g.ref_compat && bp.w < D.g.sparse) ? (pk >> 21) & 63u : (pk >> 15) & 63u;
+    return (size_t)b * BV + li;
+  }
+  const int k = (int)(e >> 28);
+  uint32_t li = (pk >> 9) & 63u;
+  if (k > 0) {
+    const int cx = bp.x + (int)(ga & 15u) - 1, cy = bp.y + (int)((ga >> 4) & 15u) - 1,
+              cz = bp.z + (int)((ga >> 8) & 15u) - 1;
+    li = (uint32_t)local_of((cx >> k) & 3, (cy >> k) & 3, (cz >> k) & 3);
+  }
+  return (size_t)(e & NBR_MASK) * BV + li;
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(256) k_cells_staged(const __grid_constant__ CellBatch P) {
+  constexpr int W = 8, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 8;
+  constexpr int NT = STAGE == 2 ? 3 : 2;
+  __shared__ long long s_end[BMAX * MAXL];
+  __shared__ __align__(16) float s_tile[W][NT][TILE];
+  const int nseg = P.n * MAXL;
+  for (int i = threadIdx.x; i < nseg; i += blockDim.x) {
+    const Dev &D = P.d[i / MAXL];
+    const int l = i % MAXL;
+    s_end[i] = l < D.g.levels ? __ldcg(D.load + l) : 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int i = 1; i < nseg; i++) s_end[i] += s_end[i - 1];
+  __syncthreads();
+  const long long total = s_end[nseg - 1];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int oA;
+  uint32_t hpk[3], hax[3];
+  halo_slots<SX, SY>(lane, oA, hpk, hax);
+  const unsigned full = 0xffffffffu;
+  int seg = 0;
+  for (long long t = (long long)blockIdx.x * W + w; t < total; t += (long long)gridDim.x * W) {
+    while (t >= s_end[seg]) seg++;  // t grows: the segment only moves forward
+    const Dev &D = P.d[seg / MAXL];
+    const int l = seg % MAXL;
+    const uint32_t b = (uint32_t)(D.g.off[l] + (t - (seg ? s_end[seg - 1] : 0)));
+    const int4 bp = D.pos[b];
+    const size_t own = (size_t)b * BV;
+    uint32_t e = OUT;
+    if (lane < 6) e = D.nbr[27u * b + (lane == 0 ? 4 : lane == 1 ? 22 : lane == 2 ? 10 : lane == 3 ? 16 : lane == 4 ? 12 : 14)];
+    size_t hc[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) hc[q] = halo_cell(D, b, bp, __shfl_sync(full, e, (int)(hax[q] >> 12)), hpk[q], hax[q]);
+    const bool leaf = D.child[8u * b + (lane >> 2)] == NONE;
+    const int scale = 1 << bp.w;
+    const float alpha = 0.5f * D.ph.rdx / (float)scale;
+    float *T0 = s_tile[w][0], *T1 = s_tile[w][1];
+    if constexpr (STAGE == 2) {
+      float *T2 = s_tile[w][2];
+      const float2 w2 = reinterpret_cast<const float2 *>(D.w + own)[lane];
+      const float2 vx = reinterpret_cast<const float2 *>(D.v[0] + own)[lane];
+      const float2 vy = reinterpret_cast<const float2 *>(D.v[1] + own)[lane];
+      const float2 vz = reinterpret_cast<const float2 *>(D.v[2] + own)[lane];
+      float hp[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        float v = D.v[q][hc[q]];
+        const uint32_t ga = hax[q];
+        const int x = bp.x + (int)(ga & 15u) - 1, y = bp.y + (int)((ga >> 4) & 15u) - 1,
+                  z = bp.z + (int)((ga >> 8) & 15u) - 1;
+        if (outside(D.g, x, y, z, scale)) v = vel_bc1(D.g, D.ph, v, q, x, y, z, scale);
+        hp[q] = D.w[hc[q]] * v;
+      }
+      *reinterpret_cast<float2 *>(T0 + oA) = make_float2(w2.x * vx.x, w2.y * vx.y);
+      *reinterpret_cast<float2 *>(T1 + oA) = make_float2(w2.x * vy.x, w2.y * vy.y);
+      const float zA = w2.x * vz.x, zB = w2.y * vz.y;
+      *reinterpret_cast<float2 *>(T2 + oA) = make_float2(zA, zB);
+      T0[hpk[0] & 511u] = hp[0];
+      T1[hpk[1] & 511u] = hp[1];
+      T2[hpk[2] & 511u] = hp[2];
+      __syncwarp();
+      float2 dv = make_float2(0.f, 0.f);
+      if (leaf) {
+        const float2 L = *reinterpret_cast<const float2 *>(T0 + oA - SX);
+        const float2 R = *reinterpret_cast<const float2 *>(T0 + oA + SX);
+        const float2 Dn = *reinterpret_cast<const float2 *>(T1 + oA - SY);
+        const float2 U = *reinterpret_cast<const float2 *>(T1 + oA + SY);
+        const float Bk = T2[oA - 1], Fw = T2[oA + 2];
+        dv.x = alpha * (R.x - L.x + U.x - Dn.x + zB - Bk);
+        dv.y = alpha * (R.y - L.y + U.y - Dn.y + Fw - zA);
+      }
+      __syncwarp();
+      reinterpret_cast<float2 *>(D.p + own)[lane] = make_float2(0.f, 0.f);
+      reinterpret_cast<float2 *>(D.pt + own)[lane] = make_float2(0.f, 0.f);
+      reinterpret_cast<float2 *>(D.div + own)[lane] = dv;
+    } else {
+      const float2 p2 = reinterpret_cast<const float2 *>(D.p + own)[lane];
+      const float2 w2 = reinterpret_cast<const float2 *>(D.w + own)[lane];
+      float hp[3], hw[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        hp[q] = D.p[hc[q]];
+        hw[q] = D.w[hc[q]];
+      }
+      *reinterpret_cast<float2 *>(T0 + oA) = p2;
+      *reinterpret_cast<float2 *>(T1 + oA) = w2;
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        T0[hpk[q] & 511u] = hp[q];
+        T1[hpk[q] & 511u] = hw[q];
+      }
+      __syncwarp();
+      if (leaf) {
+        float2 *V0 = reinterpret_cast<float2 *>(D.v[0] + own) + lane;
+        float2 *V1 = reinterpret_cast<float2 *>(D.v[1] + own) + lane;
+        float2 *V2 = reinterpret_cast<float2 *>(D.v[2] + own) + lane;
+        const float2 v0 = *V0, v1 = *V1, v2 = *V2;
+        const float2 PL = *reinterpret_cast<const float2 *>(T0 + oA - SX);
+        const float2 PR = *reinterpret_cast<const float2 *>(T0 + oA + SX);
+        const float2 PD = *reinterpret_cast<const float2 *>(T0 + oA - SY);
+        const float2 PU = *reinterpret_cast<const float2 *>(T0 + oA + SY);
+        const float2 WL = *reinterpret_cast<const float2 *>(T1 + oA - SX);
+        const float2 WR = *reinterpret_cast<const float2 *>(T1 + oA + SX);
+        const float2 WD = *reinterpret_cast<const float2 *>(T1 + oA - SY);
+        const float2 WU = *reinterpret_cast<const float2 *>(T1 + oA + SY);
+        const float PB = T0[oA - 1], PF = T0[oA + 2], WB = T1[oA - 1], WF = T1[oA + 2];
+        float2 o0, o1, o2;
+        {
+          const float pc = p2.x;
+          o0.x = v0.x - alpha * (WR.x * (PR.x - pc) + WL.x * (pc - PL.x));
+          o1.x = v1.x - alpha * (WU.x * (PU.x - pc) + WD.x * (pc - PD.x));
+          o2.x = v2.x - alpha * (w2.y * (p2.y - pc) + WB * (pc - PB));
+        }
+        {
+          const float pc = p2.y;
+          o0.y = v0.y - alpha * (WR.y * (PR.y - pc) + WL.y * (pc - PL.y));
+          o1.y = v1.y - alpha * (WU.y * (PU.y - pc) + WD.y * (pc - PD.y));
+          o2.y = v2.y - alpha * (WF * (PF - pc) + w2.x * (pc - p2.x));
+        }
+        *V0 = o0;
+        *V1 = o1;
+        *V2 = o2;
+      }
+      __syncwarp();
+    }
+  }
+}
+static unsigned staged_grid(int stage) {
+  static unsigned g[2] = {0, 0};
+  const int i = stage == 2 ? 0 : 1;
+  if (!g[i]) {
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (stage == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cells_staged<2>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cells_staged<3>, 256, 0);
+    g[i] = (unsigned)(sms * (occ > 0 ? occ : 1));
+  }
+  return g[i];
+}
+
 // Self-check of div6: every binary32 bit pattern against the IEEE division
 // (NaN results compare equal whatever their payload).
 __global__ void __launch_bounds__(256) k_check_div6(unsigned long long *bad) {
@@ -1075,6 +1254,11 @@ static void cells_batch_tb(int stage, const CellBatch &P, unsigned grid, cudaStr
   }
 }
 void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st, bool persistent) {
+  if (tile == 1 && (stage == 2 || stage == 3)) {  // staged, one warp per block
+    if (stage == 2) k_cells_staged<2><<<staged_grid(2), 256, 0, st>>>(P);
+    else k_cells_staged<3><<<staged_grid(3), 256, 0, st>>>(P);
+    return;
+  }
   if (tile != 2 && tile != 8) tile = 4;
   if (persistent) {
     if (tile == 2) cells_persist_tb<2>(stage, P, st);

@@ -81,8 +81,10 @@ def test_results_do_not_depend_on_tuning():
     rounds = tuning(4, 4, 0, 1, 1)
     rounds.round_ctas_per_sm[0], rounds.round_cache[0], rounds.round_barrier[0] = 1, 0, 1
     rounds.round_ctas_per_sm[1], rounds.round_cache[1], rounds.round_barrier[1] = 2, 3, 0
+    staged = tuning(4, 4, 0, 1, 1)
+    staged.tile[2] = staged.tile[3] = 1
     for t in [tuning(2, 0, 1, 0), tuning(8, 8, 2, 1, 1), tuning(2, 8, 1, 0, 1), tuning(8, 0, 0, 1),
-              tuning(4, 3, 0, 0, 1), rounds]:
+              tuning(4, 3, 0, 0, 1), rounds, staged]:
         b = batch_run(params, 5, t)
         for i, p in enumerate(params):
             compare(b[i], ref[i], p, f"tiles {list(t.tile)} cache {t.solve_cache} member {i}")
@@ -100,7 +102,7 @@ def test_autotune_resets_and_keeps_results():
     params = small_batch(4, 17)
     b = Batch(params)
     t = b.autotune(spinup_steps=3, reps=2)
-    assert all(x in (2, 4, 8) for x in t["tile"])
+    assert all(x in (2, 4, 8) for x in t["tile"][:2]) and all(x in (1, 2, 4, 8) for x in t["tile"][2:])
     assert t["solve_cache"] in (0, 3, 4, 8) and t["solve_barrier"] in (0, 1)
     assert t["solve_ms"] > 0
     fresh = Batch(params)
