@@ -784,44 +784,6 @@ __device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long 
 #ifndef DCG_SOLVE_MINB
 #define DCG_SOLVE_MINB 4
 #endif
-// block+halo tile strides: 52 (x) and 8 (y) put the 32 cells of either half
-// of a block, and each of their six neighbour sets, in 32 distinct banks
-#ifndef DCG_TILE_SX
-#define DCG_TILE_SX 52
-#endif
-#ifndef DCG_TILE_SY
-#define DCG_TILE_SY 8
-#endif
-
-// Lane layout of the staged block kernels (one warp per block of 64 cells):
-// lane owns the z-adjacent cells c = 2*lane, 2*lane+1, the first at tile
-// offset oA of a 6^3 tile with strides SX, SY, 1 (and +1 so that the pair is
-// 8-byte aligned). Halo slot q = 0..2 of the lane is halo cell h = lane + 32q
-// of the block's 96 face-halo cells, face f = h >> 4 (-x, +x, -y, +y, -z,
-// +z, so slot q covers the two faces of axis q). hpk: tile position (9 bits)
-// | cell in a same-level neighbour << 9 | clamped own cell << 15 | compat-
-// quirk own cell << 21; hax: apron coordinates ax | ay << 4 | az << 8 | f << 12.
-template <int SX, int SY>
-__device__ __forceinline__ void halo_slots(int lane, int &oA, uint32_t hpk[3], uint32_t hax[3]) {
-  {
-    int x, y, z;
-    local_xyz(2 * lane, x, y, z);
-    oA = (x + 1) * SX + (y + 1) * SY + (z + 1) + 1;
-  }
-#pragma unroll
-  for (int q = 0; q < 3; q++) {
-    const int h = lane + 32 * q;
-    const int f = h >> 4, i = 1 + ((h >> 2) & 3), j = 1 + (h & 3);
-    const int side = (f & 1) ? AW - 1 : 0;
-    const int ax = f < 2 ? side : i, ay = f < 2 ? i : (f < 4 ? side : j), az = f < 4 ? j : side;
-    const int same = local_of((ax - 1) & 3, (ay - 1) & 3, (az - 1) & 3);
-    const int self = local_of(clampi(ax, 1, BW) - 1, clampi(ay, 1, BW) - 1, clampi(az, 1, BW) - 1);
-    const int quirk = local_of(clampi(ax, 1, BW) & 3, clampi(ay, 1, BW) & 3, clampi(az, 1, BW) & 3);
-    hpk[q] = (uint32_t)(ax * SX + ay * SY + az + 1) | ((uint32_t)same << 9) | ((uint32_t)self << 15) |
-             ((uint32_t)quirk << 21);
-    hax[q] = (uint32_t)ax | ((uint32_t)ay << 4) | ((uint32_t)az << 8) | ((uint32_t)f << 12);
-  }
-}
 
 // One round of the batched cascade: level maxtop - round of every member that
 // has it, optional prolongation from the member's parent level, then `sweeps`
@@ -1043,22 +1005,6 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
 // resolutions. The arithmetic of divergence_cell / apply_pressure_cell is
 // kept operation for operation (identical results). Persistent: warps walk
 // the allocated blocks of every (member, level) segment.
-__device__ __forceinline__ size_t halo_cell(const Dev &D, uint32_t b, int4 bp, uint32_t e, uint32_t pk,
-                                            uint32_t ga) {
-  if (e == OUT) {
-    const uint32_t li = (D.g.ref_compat && bp.w < D.g.sparse) ? (pk >> 21) & 63u : (pk >> 15) & 63u;
-    return (size_t)b * BV + li;
-  }
-  const int k = (int)(e >> 28);
-  uint32_t li = (pk >> 9) & 63u;
-  if (k > 0) {
-    const int cx = bp.x + (int)(ga & 15u) - 1, cy = bp.y + (int)((ga >> 4) & 15u) - 1,
-              cz = bp.z + (int)((ga >> 8) & 15u) - 1;
-    li = (uint32_t)local_of((cx >> k) & 3, (cy >> k) & 3, (cz >> k) & 3);
-  }
-  return (size_t)(e & NBR_MASK) * BV + li;
-}
-
 template <int STAGE>
 __global__ void __launch_bounds__(256) k_cells_staged(const __grid_constant__ CellBatch P) {
   constexpr int W = 8, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 8;

@@ -579,11 +579,12 @@ void launch_build_nbr(const Dev &D, bool only_if_touched, cudaStream_t st) {
   k_build_nbr<<<grid_for(D.g.B * 27), 256, 0, st>>>(D, only_if_touched ? 1 : 0);
 }
 
+static void launch_scores_staged(const Dev *d, int n, cudaStream_t st);
 static void launch_scores(const Dev &D, cudaStream_t st) {
   if (D.ph.criterion == 0)
     k_scores_geo<<<grid_for(8 * D.g.B + 1), 256, 0, st>>>(D);
   else
-    k_scores_fields<<<grid_for(64 * D.g.B + 1), 256, 0, st>>>(D);
+    launch_scores_staged(&D, 1, st);
 }
 
 // FluidSimulationDCGrid::adaptTopology (fluid_simulation_dcgrid.cu:320-346)
@@ -635,6 +636,144 @@ void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *
   // neighbour tables + value propagation for touched blocks
   launch_build_nbr(D, true, st);
   for (int L = D.g.levels - 2; L >= 0; L--) k_propagate<<<gs, 256, 0, st>>>(D, L);
+}
+
+// Field-criterion scores one warp per block (used for every simulation whose
+// refine criterion is the field one): lanes 0-5 resolve the block's faces,
+// the products w*v0, w*v1, w*v2 and the density of the block and its face
+// halo go through shared tiles, then each lane computes field_cell_score's
+// arithmetic for its two cells from the tiles and the four lanes of a
+// subblock reduce the maximum. Blocks of every level's budget range are
+// visited (unallocated ones get the blocked score). Results equal
+// scores_fields_body.
+__device__ __forceinline__ float2 q_ld2(const Dev &D, size_t own, int lane) {
+  if (D.g.mixed) {
+    const uint32_t u = reinterpret_cast<const uint32_t *>(D.qh[0] + own)[lane];
+    return make_float2(h16_to_f((uint16_t)(u & 0xFFFFu), D.g.mixed), h16_to_f((uint16_t)(u >> 16), D.g.mixed));
+  }
+  return reinterpret_cast<const float2 *>(D.q[0] + own)[lane];
+}
+struct StagedScoreOut {
+  float ox, oy, oz, gx, gy, gz;
+};
+__device__ __forceinline__ float field_score_of(const Dev &D, float alpha, float wv2U, float wv2D, float wv1F,
+                                                float wv1B, float wv0F, float wv0B, float wv2R, float wv2L,
+                                                float wv1R, float wv1L, float wv0U, float wv0D, float qR, float qL,
+                                                float qU, float qD, float qF, float qB) {
+  const float ox = alpha * ((wv2U - wv2D) - (wv1F - wv1B));
+  const float oy = alpha * ((wv0F - wv0B) - (wv2R - wv2L));
+  const float oz = alpha * ((wv1R - wv1L) - (wv0U - wv0D));
+  const float gxr = alpha * (qR - qL);
+  const float gyr = alpha * (qU - qD);
+  const float gzr = alpha * (qF - qB);
+  const float om = sqrtf(ox * ox + oy * oy + oz * oz);
+  const float gr = sqrtf(gxr * gxr + gyr * gyr + gzr * gzr);
+  const float a = om / D.ph.vort_t, bb = gr / D.ph.grad_t;
+  return fmaxf(0.f, a < bb ? bb : a);
+}
+struct ScoreBatchP {
+  int n, pad;
+  long long end[BMAX];  // cumulative block counts (0 for members without the field criterion)
+  Dev d[BMAX];
+};
+__global__ void __launch_bounds__(256) k_scores_staged(const __grid_constant__ ScoreBatchP P) {
+  constexpr int W = 8, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 8;
+  __shared__ __align__(16) float s_tile[W][4][TILE];
+  if (blockIdx.x == 0 && threadIdx.x < P.n) {
+    const long long cnt = P.end[threadIdx.x] - (threadIdx.x ? P.end[threadIdx.x - 1] : 0);
+    if (cnt > 0) P.d[threadIdx.x].ss[8 * P.d[threadIdx.x].g.B] = 0.f;
+  }
+  const long long total = P.end[P.n - 1];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int oA;
+  uint32_t hpk[3], hax[3];
+  halo_slots<SX, SY>(lane, oA, hpk, hax);
+  const unsigned full = 0xffffffffu;
+  int m = 0;
+  for (long long t = (long long)blockIdx.x * W + w; t < total; t += (long long)gridDim.x * W) {
+    while (t >= P.end[m]) m++;
+    const Dev &D = P.d[m];
+    const uint32_t b = (uint32_t)(t - (m ? P.end[m - 1] : 0));
+    const int4 bp = D.pos[b];
+    const uint32_t sb = 8u * b + (uint32_t)(lane >> 2);
+    if (bp.w < 0 || level_blocked(D, bp.w)) {  // warp-uniform
+      if ((lane & 3) == 0) D.ss[sb] = -FLT_MAX;
+      continue;
+    }
+    const bool blocked = D.child[sb] != NONE;
+    const size_t own = (size_t)b * BV;
+    uint32_t e = OUT;
+    if (lane < 6) e = D.nbr[27u * b + (lane == 0 ? 4 : lane == 1 ? 22 : lane == 2 ? 10 : lane == 3 ? 16 : lane == 4 ? 12 : 14)];
+    size_t hc[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) hc[q] = halo_cell(D, b, bp, __shfl_sync(full, e, (int)(hax[q] >> 12)), hpk[q], hax[q]);
+    float *T0 = s_tile[w][0], *T1 = s_tile[w][1], *T2 = s_tile[w][2], *TQ = s_tile[w][3];
+    const float2 w2 = reinterpret_cast<const float2 *>(D.w + own)[lane];
+    const float2 v0 = reinterpret_cast<const float2 *>(D.v[0] + own)[lane];
+    const float2 v1 = reinterpret_cast<const float2 *>(D.v[1] + own)[lane];
+    const float2 v2 = reinterpret_cast<const float2 *>(D.v[2] + own)[lane];
+    const float2 q2 = q_ld2(D, own, lane);
+    const float2 p0 = make_float2(w2.x * v0.x, w2.y * v0.y), p1 = make_float2(w2.x * v1.x, w2.y * v1.y),
+                 p2 = make_float2(w2.x * v2.x, w2.y * v2.y);
+    *reinterpret_cast<float2 *>(T0 + oA) = p0;
+    *reinterpret_cast<float2 *>(T1 + oA) = p1;
+    *reinterpret_cast<float2 *>(T2 + oA) = p2;
+    *reinterpret_cast<float2 *>(TQ + oA) = q2;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {  // slot q lies on the faces of axis q
+      const size_t c = hc[q];
+      const float hw = D.w[c];
+      const uint32_t at = hpk[q] & 511u;
+      if (q != 0) T0[at] = hw * D.v[0][c];
+      if (q != 1) T1[at] = hw * D.v[1][c];
+      if (q != 2) T2[at] = hw * D.v[2][c];
+      TQ[at] = q_ld(D, 0, c);
+    }
+    __syncwarp();
+    const int scale = 1 << bp.w;
+    const float alpha = 0.5f * D.ph.rdx / (float)scale;
+    const float2 w0U = *reinterpret_cast<const float2 *>(T0 + oA + SY), w0D = *reinterpret_cast<const float2 *>(T0 + oA - SY);
+    const float2 w1R = *reinterpret_cast<const float2 *>(T1 + oA + SX), w1L = *reinterpret_cast<const float2 *>(T1 + oA - SX);
+    const float2 w2U = *reinterpret_cast<const float2 *>(T2 + oA + SY), w2D = *reinterpret_cast<const float2 *>(T2 + oA - SY);
+    const float2 w2R = *reinterpret_cast<const float2 *>(T2 + oA + SX), w2L = *reinterpret_cast<const float2 *>(T2 + oA - SX);
+    const float2 qR = *reinterpret_cast<const float2 *>(TQ + oA + SX), qL = *reinterpret_cast<const float2 *>(TQ + oA - SX);
+    const float2 qU = *reinterpret_cast<const float2 *>(TQ + oA + SY), qD = *reinterpret_cast<const float2 *>(TQ + oA - SY);
+    const float w0B = T0[oA - 1], w0F = T0[oA + 2], w1B = T1[oA - 1], w1F = T1[oA + 2], qB = TQ[oA - 1],
+                qF = TQ[oA + 2];
+    __syncwarp();
+    // cell A (z even): +z neighbour is cell B; cell B: -z neighbour is cell A
+    const float mA = field_score_of(D, alpha, w2U.x, w2D.x, p1.y, w1B, p0.y, w0B, w2R.x, w2L.x, w1R.x, w1L.x, w0U.x,
+                                    w0D.x, qR.x, qL.x, qU.x, qD.x, q2.y, qB);
+    const float mB = field_score_of(D, alpha, w2U.y, w2D.y, w1F, p1.x, w0F, p0.x, w2R.y, w2L.y, w1R.y, w1L.y, w0U.y,
+                                    w0D.y, qR.y, qL.y, qU.y, qD.y, qF, q2.x);
+    float mm = blocked ? 0.f : fmaxf(mA, mB);
+    mm = fmaxf(mm, __shfl_xor_sync(full, mm, 1));
+    mm = fmaxf(mm, __shfl_xor_sync(full, mm, 2));
+    if ((lane & 3) == 0) D.ss[sb] = blocked ? -FLT_MAX : mm;
+  }
+}
+static unsigned scores_staged_grid() {
+  static unsigned g = 0;
+  if (!g) {
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_scores_staged, 256, 0);
+    g = (unsigned)(sms * (occ > 0 ? occ : 1));
+  }
+  return g;
+}
+// field-criterion scores of the members with that criterion (in one launch)
+static void launch_scores_staged(const Dev *d, int n, cudaStream_t st) {
+  ScoreBatchP P{};
+  P.n = n;
+  long long e = 0;
+  for (int i = 0; i < n; i++) {
+    P.d[i] = d[i];
+    if (d[i].ph.criterion != 0) e += d[i].g.B;
+    P.end[i] = e;
+  }
+  if (e > 0) k_scores_staged<<<scores_staged_grid(), 256, 0, st>>>(P);
 }
 
 // ------------------------------------------------------- batched adaptation
@@ -749,9 +888,10 @@ struct AdaptLauncher {
   long long B(int i) const { return m[i].D.g.B; }
 
   void scores() {
-    go<A_SCORES>([&](int i) {
-      return (long long)grid_for(m[i].D.ph.criterion == 0 ? 8 * B(i) + 1 : 64 * B(i) + 1);
-    });
+    go<A_SCORES>([&](int i) { return m[i].D.ph.criterion == 0 ? (long long)grid_for(8 * B(i) + 1) : 0ll; });
+    Dev d[BMAX];
+    for (int i = 0; i < n; i++) d[i] = m[i].D;
+    launch_scores_staged(d, n, st);
   }
   // compaction of level L's flagged subblocks (sel null: threshold test) into p2
   void compact(int L, bool sel, const std::vector<bool> &in) {
