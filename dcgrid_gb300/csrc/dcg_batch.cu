@@ -78,8 +78,8 @@ struct dcg_batch {
     if (tune.solve_cache != 0 && tune.solve_cache != 3 && tune.solve_cache != 4 && tune.solve_cache != 8)
       return fail(DCG_E_INVALID, "solve_cache must be 0, 3, 4 or 8");
     for (int k = 0; k < 4; k++)
-      if (tune.tile[k] != 2 && tune.tile[k] != 4 && tune.tile[k] != 8 && !(tune.tile[k] == 1 && k >= 2))
-        return fail(DCG_E_INVALID, "tiles must be 2, 4 or 8 blocks (1: staged, stages 2 and 3)");
+      if (tune.tile[k] != 1 && tune.tile[k] != 2 && tune.tile[k] != 4 && tune.tile[k] != 8)
+        return fail(DCG_E_INVALID, "tiles must be 1 (staged), 2, 4 or 8 blocks");
     solve_grid = batch_solve_grid(sms, tune.solve_cache, tune.solve_ctas_per_sm);
     if (solve_grid <= 0) return fail(DCG_E_CUDA, "cooperative level solve cannot be resident");
     for (int r = 0; r < 4; r++) {
@@ -299,8 +299,8 @@ struct dcg_batch {
     if ((rc = step(spinup))) return rc;
     if ((rc = sync())) return rc;
     // cell stages: every tile of each stage, launched one CTA per block or
-    // persistent; the launch form that gives the lower total is kept. Tile 1
-    // (divergence, pressure application): one warp per block, staged
+    // persistent; the launch form that gives the lower total is kept. Tile 1:
+    // one warp per block through shared tiles (staged)
     const int tiles[4] = {1, 2, 4, 8};
     dcg_tuning best = tune;
     float total[2] = {0.f, 0.f};
@@ -311,7 +311,6 @@ struct dcg_batch {
       for (int stage = 0; stage < 4; stage++) {
         float best_ms = 1e30f;
         for (int tile : tiles) {
-          if (tile == 1 && stage < 2) continue;
           tune.tile[stage] = tile;
           const float ms = time_ms(reps, [&] { cells(stage); });
           if (ms < best_ms) {

@@ -563,7 +563,7 @@ __device__ inline void sample_at(const Dev &D, uint32_t b0, int4 bp0, float pxw,
   if (b == NONE) b = locate(D, ix, iy, iz, 0, lev);
   const int4 bp = (b == b0) ? bp0 : D.pos[b];
   s.scale = 1 << lev;
-  const float scaleInv = 1.f / (float)s.scale;
+  const float scaleInv = __int_as_float((127 - lev) << 23);  // 1 / 2^lev, exact
   const float x = pxw * scaleInv - 0.5f, y = pyw * scaleInv - 0.5f, z = pzw * scaleInv - 0.5f;
   const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
   const float dx = x - xf, dy = y - yf, dz = z - zf;

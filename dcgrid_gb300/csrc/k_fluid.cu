@@ -1134,6 +1134,332 @@ __global__ void __launch_bounds__(256) k_cells_staged(const __grid_constant__ Ce
     }
   }
 }
+// ------------------------------------------------------ staged advection
+// Advection one warp per block: the block's 64 cells and its 152 apron cells
+// (faces, edges and corners, resolved once per block from the block's 26
+// neighbour-table entries as apron_cell does) of the sampled fields go into
+// shared 6^3 tiles. A leaf cell whose back-traced sample lies in its own block
+// (no finer block there: sample_at then takes the own block) reads its eight
+// stencil corners and their fluidities from the tiles; any other leaf cell
+// runs the per-cell body (advect_velocity_cell / advect_scalars_cell_t).
+// The arithmetic is sample_at's and the per-cell bodies' operation for
+// operation, so the results are identical.
+struct AdvSlots {  // the lane's apron slots a = lane + 32 r, r < 5 (152 slots)
+  uint32_t pk[5], ga[5];
+  int n;
+};
+template <int SX, int SY> __device__ __forceinline__ void apron_slots(int lane, AdvSlots &S) {
+  S.n = 0;
+#pragma unroll
+  for (int r = 0; r < 5; r++) S.pk[r] = S.ga[r] = 0;
+  int cnt = 0;
+  for (int idx = 0; idx < AW * AW * AW; idx++) {
+    const int ax = idx / 36, ay = (idx / 6) % 6, az = idx % 6;
+    if (ax > 0 && ax < AW - 1 && ay > 0 && ay < AW - 1 && az > 0 && az < AW - 1) continue;
+    if ((cnt & 31) == lane) {
+      const int same = local_of((ax - 1) & 3, (ay - 1) & 3, (az - 1) & 3);
+      const int self = local_of(clampi(ax, 1, BW) - 1, clampi(ay, 1, BW) - 1, clampi(az, 1, BW) - 1);
+      const int quirk = local_of(clampi(ax, 1, BW) & 3, clampi(ay, 1, BW) & 3, clampi(az, 1, BW) & 3);
+      const int d = dir_of(ax) * 9 + dir_of(ay) * 3 + dir_of(az);
+      S.pk[S.n] = (uint32_t)(ax * SX + ay * SY + az + 1) | ((uint32_t)same << 9) | ((uint32_t)self << 15) |
+                  ((uint32_t)quirk << 21);
+      S.ga[S.n] = (uint32_t)ax | ((uint32_t)ay << 4) | ((uint32_t)az << 8) | ((uint32_t)d << 12);
+      S.n++;
+    }
+    cnt++;
+  }
+}
+// The back-traced point of a cell of the block at bp0 lies in that block
+// (sample_at's block offset is 0); sub = the point's subblock. sample_at then
+// keeps the block unless that subblock has a child (a descent, level > 0).
+__device__ __forceinline__ bool sample_in_own(const Dev &D, int4 bp0, float pxw, float pyw, float pzw, int &sub) {
+  const int ix = clampi((int)floorf(pxw), 0, D.g.gx - 1);
+  const int iy = clampi((int)floorf(pyw), 0, D.g.gy - 1);
+  const int iz = clampi((int)floorf(pzw), 0, D.g.gz - 1);
+  const int L0 = bp0.w;
+  const int lx = (ix >> L0) - bp0.x, ly = (iy >> L0) - bp0.y, lz = (iz >> L0) - bp0.z;
+  sub = (((lx >> 1) & 1) << 2) | (((ly >> 1) & 1) << 1) | ((lz >> 1) & 1);
+  return ((((ix >> L0) >> 2) - (bp0.x >> 2)) | (((iy >> L0) >> 2) - (bp0.y >> 2)) |
+          (((iz >> L0) >> 2) - (bp0.z >> 2))) == 0;
+}
+template <int SX, int SY> __device__ __forceinline__ constexpr int tile_delta(int c) {
+  return ((c >> 2) & 1) * SX + ((c >> 1) & 1) * SY + (c & 1);
+}
+// sample_at's weights for a sample in the block at bp (level lev) with the
+// corner fluidities read from the tile Wt; off[c] = tile offset of corner c.
+struct SmpT {
+  int base;  // tile offset of corner 0; corner c at base + tile_delta<SX, SY>(c)
+  float wt[8];
+  float wAcc;
+  int x0, y0, z0, x1, y1, z1, scale;
+};
+template <int SX, int SY>
+__device__ __forceinline__ void sample_tile(int4 bp, int lev, float pxw, float pyw, float pzw, const float *Wt,
+                                            SmpT &s) {
+  s.scale = 1 << lev;
+  const float scaleInv = __int_as_float((127 - lev) << 23);  // 1 / 2^lev, exact
+  const float x = pxw * scaleInv - 0.5f, y = pyw * scaleInv - 0.5f, z = pzw * scaleInv - 0.5f;
+  const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+  const float dx = x - xf, dy = y - yf, dz = z - zf;
+  s.x0 = (int)xf; s.y0 = (int)yf; s.z0 = (int)zf;
+  s.x1 = s.x0 + 1; s.y1 = s.y0 + 1; s.z1 = s.z0 + 1;
+  const int i = clampi(s.x1 - bp.x, 0, AW - 2);
+  const int j = clampi(s.y1 - bp.y, 0, AW - 2);
+  const int k = clampi(s.z1 - bp.z, 0, AW - 2);
+  s.base = i * SX + j * SY + k + 1;
+  const float *Wc = Wt + s.base;
+  const float Dx = 1.f - dx, Dy = 1.f - dy, Dz = 1.f - dz;
+  s.wt[0] = Wc[tile_delta<SX, SY>(0)] * Dx * Dy * Dz;
+  s.wt[1] = Wc[tile_delta<SX, SY>(1)] * Dx * Dy * dz;
+  s.wt[2] = Wc[tile_delta<SX, SY>(2)] * Dx * dy * Dz;
+  s.wt[3] = Wc[tile_delta<SX, SY>(3)] * Dx * dy * dz;
+  s.wt[4] = Wc[tile_delta<SX, SY>(4)] * dx * Dy * Dz;
+  s.wt[5] = Wc[tile_delta<SX, SY>(5)] * dx * Dy * dz;
+  s.wt[6] = Wc[tile_delta<SX, SY>(6)] * dx * dy * Dz;
+  s.wt[7] = Wc[tile_delta<SX, SY>(7)] * dx * dy * dz;
+  s.wAcc = s.wt[0] + s.wt[1] + s.wt[2] + s.wt[3] + s.wt[4] + s.wt[5] + s.wt[6] + s.wt[7];
+  const float wInv = 1.f / s.wAcc;
+#pragma unroll
+  for (int c = 0; c < 8; c++) s.wt[c] = s.wt[c] * wInv;
+}
+__device__ __forceinline__ bool box_inside_t(const Geom &g, const SmpT &s) {
+  return s.x0 >= 0 && s.y0 >= 0 && s.z0 >= 0 && s.x1 * s.scale < g.gx && s.y1 * s.scale < g.gy &&
+         s.z1 * s.scale < g.gz;
+}
+
+// resident CTAs per SM the staged advection's register allocation targets
+#ifndef DCG_ADV_MINB
+#define DCG_ADV_MINB 2
+#endif
+// per-cell fallbacks, out of line so that the staged kernel keeps few registers
+__device__ __noinline__ void advect_velocity_cell_ool(const Dev &D, long long b, int c) { advect_velocity_cell(D, b, c); }
+template <int MODE, int NQ> __device__ __noinline__ void advect_scalars_cell_ool(const Dev &D, long long b, int c) {
+  advect_scalars_cell_t<MODE, NQ>(D, b, c);
+}
+
+// STAGE 0: velocity (MODE, NQ unused); STAGE 1: scalars of members with
+// storage format MODE and NQ scalars (other members have no blocks here)
+template <int STAGE, int MODE, int NQ>
+__global__ void __launch_bounds__(256, DCG_ADV_MINB) k_advect_staged(const __grid_constant__ CellBatch P) {
+  constexpr int W = 8, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 8;
+  constexpr int NF = STAGE == 0 ? 4 : 1 + NQ;  // tile 0: fluidity
+  __shared__ long long s_end[BMAX * MAXL];
+  __shared__ __align__(16) float s_tile[W][NF][TILE];
+  const int nseg = P.n * MAXL;
+  for (int i = threadIdx.x; i < nseg; i += blockDim.x) {
+    const Dev &D = P.d[i / MAXL];
+    const int l = i % MAXL;
+    const bool mine = STAGE == 0 || (D.g.mixed == MODE && D.g.nq == NQ);
+    s_end[i] = (mine && l < D.g.levels) ? __ldcg(D.load + l) : 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int i = 1; i < nseg; i++) s_end[i] += s_end[i - 1];
+  __syncthreads();
+  const long long total = s_end[nseg - 1];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int oA;
+  {
+    int x, y, z;
+    local_xyz(2 * lane, x, y, z);
+    oA = (x + 1) * SX + (y + 1) * SY + (z + 1) + 1;
+  }
+  // the lanes' apron slots, the same for every warp: in shared memory
+  __shared__ uint32_t s_slot[2][5][32];
+  if (w == 0) {
+    AdvSlots S;
+    apron_slots<SX, SY>(lane, S);
+#pragma unroll
+    for (int r = 0; r < 5; r++) {
+      s_slot[0][r][lane] = r < S.n ? S.pk[r] : 0xFFFFFFFFu;
+      s_slot[1][r][lane] = S.ga[r];
+    }
+  }
+  __syncthreads();
+  const unsigned full = 0xffffffffu;
+  int seg = 0;
+  for (long long t = (long long)blockIdx.x * W + w; t < total; t += (long long)gridDim.x * W) {
+    while (t >= s_end[seg]) seg++;
+    const Dev &D = P.d[seg / MAXL];
+    const int l = seg % MAXL;
+    const uint32_t b = (uint32_t)(D.g.off[l] + (t - (seg ? s_end[seg - 1] : 0)));
+    const int4 bp = D.pos[b];
+    const size_t own = (size_t)b * BV;
+    const uint32_t e = lane < 27 ? D.nbr[27u * b + lane] : OUT;
+    const uint32_t ch = lane < 8 ? D.child[8u * b + lane] : NONE;  // the block's subblock children
+    float *Wt = s_tile[w][0];
+    float2 qa = make_float2(0.f, 0.f), qb = qa;  // own density / temperature pairs (buoyancy)
+    if (STAGE == 0 && (D.ph.buoy_a != 0.f || D.ph.buoy_b != 0.f)) {
+      qa = make_float2(q_ld(D, 0, own + 2 * lane), q_ld(D, 0, own + 2 * lane + 1));
+      if (D.g.nq > 1) qb = make_float2(q_ld(D, 1, own + 2 * lane), q_ld(D, 1, own + 2 * lane + 1));
+    }
+    // own cells
+    const float2 wo = reinterpret_cast<const float2 *>(D.w + own)[lane];
+    *reinterpret_cast<float2 *>(Wt + oA) = wo;
+    const float2 va = reinterpret_cast<const float2 *>(D.v[0] + own)[lane];
+    const float2 vb = reinterpret_cast<const float2 *>(D.v[1] + own)[lane];
+    const float2 vc = reinterpret_cast<const float2 *>(D.v[2] + own)[lane];
+    if constexpr (STAGE == 0) {
+      *reinterpret_cast<float2 *>(s_tile[w][1] + oA) = va;
+      *reinterpret_cast<float2 *>(s_tile[w][2] + oA) = vb;
+      *reinterpret_cast<float2 *>(s_tile[w][3] + oA) = vc;
+    } else {
+#pragma unroll
+      for (int kq = 0; kq < NQ; kq++) {
+        float2 q2;
+        if (MODE == 0) {
+          q2 = reinterpret_cast<const float2 *>(D.q[kq] + own)[lane];
+        } else {
+          const uint32_t u = reinterpret_cast<const uint32_t *>(D.qh[kq] + own)[lane];
+          q2 = make_float2(h16_to_f((uint16_t)(u & 0xFFFFu), MODE), h16_to_f((uint16_t)(u >> 16), MODE));
+        }
+        *reinterpret_cast<float2 *>(s_tile[w][1 + kq] + oA) = q2;
+      }
+    }
+    // apron cells
+#pragma unroll
+    for (int r = 0; r < 5; r++) {
+      const uint32_t pk = s_slot[0][r][lane], ga = s_slot[1][r][lane];
+      const uint32_t ed = __shfl_sync(full, e, (int)((ga >> 12) & 31u));
+      if (pk != 0xFFFFFFFFu) {
+        const size_t c = halo_cell(D, b, bp, ed, pk, ga);
+        const uint32_t at = pk & 511u;
+        Wt[at] = D.w[c];
+        if constexpr (STAGE == 0) {
+          s_tile[w][1][at] = D.v[0][c];
+          s_tile[w][2][at] = D.v[1][c];
+          s_tile[w][3][at] = D.v[2][c];
+        } else {
+#pragma unroll
+          for (int kq = 0; kq < NQ; kq++) s_tile[w][1 + kq][at] = q_ldm<MODE>(D, kq, c);
+        }
+      }
+    }
+    __syncwarp();
+    const bool leaf = __shfl_sync(full, ch, lane >> 2) == NONE;
+#pragma unroll 1
+    for (int h = 0; h < 2; h++) {
+      const int c = 2 * lane + h;
+      const size_t cell = own + c;
+      float px = 0.f, py = 0.f, pz = 0.f;
+      bool fast = false;
+      int sub = 0;
+      if (leaf) {
+        int lx, ly, lz;
+        local_xyz(c, lx, ly, lz);
+        const float scale = (float)(1 << bp.w);
+        const float alpha = D.ph.dt * D.ph.rdx;
+        px = ((float)(bp.x + lx) + 0.5f) * scale - (h ? va.y : va.x) * alpha;
+        py = ((float)(bp.y + ly) + 0.5f) * scale - (h ? vb.y : vb.x) * alpha;
+        pz = ((float)(bp.z + lz) + 0.5f) * scale - (h ? vc.y : vc.x) * alpha;
+        fast = sample_in_own(D, bp, px, py, pz, sub);
+      }
+      // the sample's subblock must have no child (else sample_at descends)
+      const bool sub_leaf = __shfl_sync(full, ch, sub) == NONE;
+      fast = fast && (bp.w == 0 || sub_leaf);
+      if constexpr (STAGE == 0) {
+        if (leaf && !fast) {
+          advect_velocity_cell_ool(D, b, c);
+          continue;
+        }
+        float o0 = 0.f, o1 = 0.f, o2 = 0.f;
+        if (leaf) {
+          SmpT s;
+          sample_tile<SX, SY>(bp, bp.w, px, py, pz, Wt, s);
+          if (!(s.wAcc < 1e-6f)) {
+            const bool inside = box_inside_t(D.g, s);
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+              const int o = s.base + tile_delta<SX, SY>(k);
+              float vx = s_tile[w][1][o], vy = s_tile[w][2][o], vz = s_tile[w][3][o];
+              if (!inside) {
+                const int x = (k & 4) ? s.x1 : s.x0, y = (k & 2) ? s.y1 : s.y0, z = (k & 1) ? s.z1 : s.z0;
+                vel_bc(D.g, D.ph, vx, vy, vz, x, y, z, s.scale);
+              }
+              if (k == 0) {
+                o0 = vx * s.wt[0]; o1 = vy * s.wt[0]; o2 = vz * s.wt[0];
+              } else {
+                o0 = o0 + vx * s.wt[k]; o1 = o1 + vy * s.wt[k]; o2 = o2 + vz * s.wt[k];
+              }
+            }
+          }
+          if (D.ph.buoy_a != 0.f || D.ph.buoy_b != 0.f) {
+            float f = -D.ph.buoy_a * (h ? qa.y : qa.x);
+            if (D.g.nq > 1) f = f + D.ph.buoy_b * ((h ? qb.y : qb.x) - D.ph.t_amb);
+            o1 = o1 + D.ph.dt * f;
+          }
+        }
+        D.tv[0][cell] = o0;
+        D.tv[1][cell] = o1;
+        D.tv[2][cell] = o2;
+      } else {
+        if (leaf && !fast) {
+          advect_scalars_cell_ool<MODE, NQ>(D, b, c);
+          continue;
+        }
+        float o[NQ];
+#pragma unroll
+        for (int kq = 0; kq < NQ; kq++) o[kq] = 0.f;
+        if (leaf) {
+          SmpT s;
+          sample_tile<SX, SY>(bp, bp.w, px, py, pz, Wt, s);
+          if (!(s.wAcc < 1e-6f)) {
+            const bool inside = box_inside_t(D.g, s);
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+              const int x = (k & 4) ? s.x1 : s.x0, y = (k & 2) ? s.y1 : s.y0, z = (k & 1) ? s.z1 : s.z0;
+              const int mode = inside ? 0 : q_bc_mode(D.g, D.ph, x, y, z, s.scale);
+#pragma unroll
+              for (int kq = 0; kq < NQ; kq++) {
+                const float qc = mode == 0 ? s_tile[w][1 + kq][s.base + tile_delta<SX, SY>(k)]
+                                           : (mode == 1 && kq == 0 ? D.ph.d_emit : 0.f);
+                o[kq] = (k == 0) ? qc * s.wt[0] : o[kq] + qc * s.wt[k];
+              }
+            }
+          }
+          int lx, ly, lz;
+          local_xyz(c, lx, ly, lz);
+          if (D.ph.em_n > 0)
+            o[0] = o[0] + D.ph.dt * emission_at(D.g, D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w);
+          if (D.ph.src) {
+            if (in_source(D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w))
+#pragma unroll
+              for (int kq = 0; kq < NQ; kq++) o[kq] = src_value_at(D.ph, kq, bp.x + lx, bp.y + ly, bp.z + lz, bp.w);
+          }
+        }
+#pragma unroll
+        for (int kq = 0; kq < NQ; kq++) tq_stm<MODE>(D, kq, cell, o[kq]);
+      }
+    }
+    __syncwarp();
+  }
+}
+template <int STAGE, int MODE, int NQ> static unsigned advect_grid() {
+  static unsigned g = 0;
+  if (!g) {
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_advect_staged<STAGE, MODE, NQ>, 256, 0);
+    g = (unsigned)(sms * (occ > 0 ? occ : 1));
+  }
+  return g;
+}
+static void launch_advect_staged(int stage, const CellBatch &P, cudaStream_t st) {
+  if (stage == 0) {
+    k_advect_staged<0, 0, 1><<<advect_grid<0, 0, 1>(), 256, 0, st>>>(P);
+    return;
+  }
+  bool has[3][2] = {};
+  for (int i = 0; i < P.n; i++) has[P.d[i].g.mixed][P.d[i].g.nq == 3 ? 1 : 0] = true;
+  if (has[0][0]) k_advect_staged<1, 0, 1><<<advect_grid<1, 0, 1>(), 256, 0, st>>>(P);
+  if (has[0][1]) k_advect_staged<1, 0, 3><<<advect_grid<1, 0, 3>(), 256, 0, st>>>(P);
+  if (has[1][0]) k_advect_staged<1, 1, 1><<<advect_grid<1, 1, 1>(), 256, 0, st>>>(P);
+  if (has[1][1]) k_advect_staged<1, 1, 3><<<advect_grid<1, 1, 3>(), 256, 0, st>>>(P);
+  if (has[2][0]) k_advect_staged<1, 2, 1><<<advect_grid<1, 2, 1>(), 256, 0, st>>>(P);
+  if (has[2][1]) k_advect_staged<1, 2, 3><<<advect_grid<1, 2, 3>(), 256, 0, st>>>(P);
+}
+
 static unsigned staged_grid(int stage) {
   static unsigned g[2] = {0, 0};
   const int i = stage == 2 ? 0 : 1;
@@ -1200,8 +1526,9 @@ static void cells_batch_tb(int stage, const CellBatch &P, unsigned grid, cudaStr
   }
 }
 void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st, bool persistent) {
-  if (tile == 1 && (stage == 2 || stage == 3)) {  // staged, one warp per block
-    if (stage == 2) k_cells_staged<2><<<staged_grid(2), 256, 0, st>>>(P);
+  if (tile == 1 && stage < 4) {  // staged, one warp per block
+    if (stage < 2) launch_advect_staged(stage, P, st);
+    else if (stage == 2) k_cells_staged<2><<<staged_grid(2), 256, 0, st>>>(P);
     else k_cells_staged<3><<<staged_grid(3), 256, 0, st>>>(P);
     return;
   }

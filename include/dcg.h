@@ -313,9 +313,8 @@ int dcg_check_div6(uint64_t *mismatches, uint32_t *first);
 typedef struct dcg_batch dcg_batch;
 typedef struct {
   int32_t tile[4];           /* blocks of 64 cells per CTA (2, 4 or 8) for advect velocity,
-                                advect scalars, divergence, apply pressure; 1 (divergence
-                                and apply pressure only): one warp per block through a
-                                shared tile of the block and its face halo                 */
+                                advect scalars, divergence, apply pressure; 1: one warp per
+                                block through shared tiles of the block and its apron      */
   int32_t solve_cache;       /* cells per thread whose stencil the level solve keeps in
                                 shared memory: 0, 3, 4 or 8 (8 KB of shared memory each)    */
   int32_t solve_ctas_per_sm; /* CTAs per SM of the cooperative solve (0 = occupancy limit) */

@@ -46,12 +46,15 @@ def test_batch_members_equal_standalone(prec):
         compare(b[i], standalone(p, 6), p, f"member {i}")
 
 
-def test_batch_mixed_precisions_and_levels_in_one_batch():
-    params = small_batch(4, 5)
+@pytest.mark.parametrize("staged", [False, True], ids=["tiled", "staged"])
+def test_batch_mixed_precisions_and_levels_in_one_batch(staged):
+    params = small_batch(5, 5)
     params[1].precision = capi.PRECISION_MIXED_FP16
     params[2].precision = capi.PRECISION_MIXED
     params[3].levels = 3 if params[3].levels == 2 else 2
-    b = batch_run(params, 4)
+    params[4].n_scalars = 1  # density only: another scalar-advection kernel
+    params[4].precision = capi.PRECISION_MIXED_FP16
+    b = batch_run(params, 4, tuning(1, 4, 0, 1, 1) if staged else None)
     for i, p in enumerate(params):
         compare(b[i], standalone(p, 4), p, f"member {i}")
 
@@ -81,10 +84,11 @@ def test_results_do_not_depend_on_tuning():
     rounds = tuning(4, 4, 0, 1, 1)
     rounds.round_ctas_per_sm[0], rounds.round_cache[0], rounds.round_barrier[0] = 1, 0, 1
     rounds.round_ctas_per_sm[1], rounds.round_cache[1], rounds.round_barrier[1] = 2, 3, 0
-    staged = tuning(4, 4, 0, 1, 1)
-    staged.tile[2] = staged.tile[3] = 1
+    staged = tuning(1, 4, 0, 1, 1)
+    mixed_tiles = tuning(4, 4, 0, 1, 0)
+    mixed_tiles.tile[0], mixed_tiles.tile[3] = 1, 1
     for t in [tuning(2, 0, 1, 0), tuning(8, 8, 2, 1, 1), tuning(2, 8, 1, 0, 1), tuning(8, 0, 0, 1),
-              tuning(4, 3, 0, 0, 1), rounds, staged]:
+              tuning(4, 3, 0, 0, 1), rounds, staged, mixed_tiles]:
         b = batch_run(params, 5, t)
         for i, p in enumerate(params):
             compare(b[i], ref[i], p, f"tiles {list(t.tile)} cache {t.solve_cache} member {i}")
@@ -102,7 +106,7 @@ def test_autotune_resets_and_keeps_results():
     params = small_batch(4, 17)
     b = Batch(params)
     t = b.autotune(spinup_steps=3, reps=2)
-    assert all(x in (2, 4, 8) for x in t["tile"][:2]) and all(x in (1, 2, 4, 8) for x in t["tile"][2:])
+    assert all(x in (1, 2, 4, 8) for x in t["tile"])
     assert t["solve_cache"] in (0, 3, 4, 8) and t["solve_barrier"] in (0, 1)
     assert t["solve_ms"] > 0
     fresh = Batch(params)
