@@ -75,8 +75,8 @@ struct dcg_batch {
   int groups() const { return (n() + BMAX - 1) / BMAX; }
 
   int set_solve_config() {
-    if (tune.solve_cache != 0 && tune.solve_cache != 3 && tune.solve_cache != 4 && tune.solve_cache != 8)
-      return fail(DCG_E_INVALID, "solve_cache must be 0, 3, 4 or 8");
+    if (!solve_variant_valid(tune.solve_cache))
+      return fail(DCG_E_INVALID, "solve_cache must be 0, 3, 4, 8 or a pipelined variant 16, 18, 19, 32, 34, 35");
     for (int k = 0; k < 4; k++)
       if (tune.tile[k] != 1 && tune.tile[k] != 2 && tune.tile[k] != 4 && tune.tile[k] != 8)
         return fail(DCG_E_INVALID, "tiles must be 1 (staged), 2, 4 or 8 blocks");
@@ -85,8 +85,8 @@ struct dcg_batch {
     for (int r = 0; r < 4; r++) {
       if (tune.round_ctas_per_sm[r] <= 0) continue;
       const int c = tune.round_cache[r];
-      if ((c != 0 && c != 3 && c != 4 && c != 8) || (tune.round_barrier[r] != 0 && tune.round_barrier[r] != 1))
-        return fail(DCG_E_INVALID, "round schedule: cache 0, 3, 4 or 8 and barrier 0 or 1");
+      if (!solve_variant_valid(c) || (tune.round_barrier[r] != 0 && tune.round_barrier[r] != 1))
+        return fail(DCG_E_INVALID, "round schedule: a valid solve variant and barrier 0 or 1");
       if (batch_solve_grid(sms, c, tune.round_ctas_per_sm[r]) <= 0)
         return fail(DCG_E_CUDA, "round schedule cannot be resident");
     }
@@ -332,7 +332,7 @@ struct dcg_batch {
     }
     // level solve: cache depth x CTAs per SM x barrier kind
     float best_solve = 1e30f;
-    for (int cache : {0, 3, 4, 8}) {
+    for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35}) {
       const int occ = batch_solve_grid(sms, cache, 0) / std::max(1, sms);
       for (int k = 1; k <= occ; k++)
         for (int tree = 0; tree < 2; tree++) {
@@ -355,7 +355,7 @@ struct dcg_batch {
       });
       float bms = base;
       best.round_ctas_per_sm[r] = 0;
-      for (int cache : {0, 3, 4, 8}) {
+      for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35}) {
         const int occ = batch_solve_grid(sms, cache, 0) / std::max(1, sms);
         for (int k = 1; k <= occ; k++)
           for (int tree = 0; tree < 2; tree++) {

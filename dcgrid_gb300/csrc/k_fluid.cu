@@ -784,6 +784,152 @@ __device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long 
 #ifndef DCG_SOLVE_MINB
 #define DCG_SOLVE_MINB 4
 #endif
+#ifndef DCG_PIPE_MINB
+#define DCG_PIPE_MINB 4
+#endif
+
+// ---- pipelined staged sweeps
+// Asynchronous copies (cp.async, Ampere+ LDGSTS) of 4 and 8 bytes from global
+// memory into shared memory: the data goes to the tile without passing
+// through registers, so a warp keeps the loads of the next NB-1 blocks in
+// flight while it computes the current one.
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Staged sweeps as in the per-pass form below, pipelined: each warp walks its
+// blocks (round r: level block ((r * nctas + blockIdx.x) * 8 + warp)) with NB
+// tile buffers; the copies of block r + NB - 1 (own cells, three halo cells
+// per lane, divergence) are issued before block r is computed from its tile.
+// The copies read the previous sweep's results written by other SMs; the grid
+// barrier's fences order them. Block descriptions come from the launch's
+// shared cache when they fit, else from the global table, through shuffles.
+template <int CACHE, int NB>
+__device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long long *s_end, const int *s_lev,
+                                                uint32_t *s_cache, long long total, unsigned nctas, int sweeps,
+                                                int tree) {
+  constexpr int W = 8, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 8;
+  __shared__ __align__(16) float s_pt[W][NB][TILE];
+  __shared__ __align__(16) float s_pd[W][NB][64];
+  const unsigned full = 0xffffffffu;
+  const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+  int oA;
+  uint32_t hpk[3], hax[3];
+  halo_slots<SX, SY>(lane, oA, hpk, hax);
+  const long long nblocks = total >> 6;
+  const int rounds_b = (int)((nblocks + (long long)W * nctas - 1) / ((long long)W * nctas));
+  const bool cached = rounds_b <= CACHE * 2048 / (W * BI_WORDS);
+  for (int r = 0; r < rounds_b; r++) {
+    const long long gb = ((long long)r * nctas + blockIdx.x) * W + w;
+    if (gb >= nblocks) continue;
+    if (cached) {
+      fill_block_info(P, s_end, s_lev, gb, s_cache + (r * W + w) * BI_WORDS, lane);
+    } else {
+      __shared__ uint32_t s_one[W][BI_WORDS];
+      fill_block_info(P, s_end, s_lev, gb, s_one[w], lane);
+      __syncwarp();
+      if (lane < BI_WORDS) P.binfo[gb * BI_WORDS + lane] = s_one[w][lane];
+      __syncwarp();
+    }
+  }
+  __syncwarp();
+  if (!cached) __threadfence_block();
+  auto barrier = [&]() {
+    if (tree) grid_barrier_tree(P.bar, P.err, nctas);
+    else grid_barrier(P.bar, P.err, nctas);
+  };
+  // per buffer: arena index of the block's first cell and alpha (bits); own = ~0u: no block
+  uint32_t b_own[NB], b_alpha[NB];
+  for (int it = 0; it < sweeps; it++) {
+    const float *src = (it & 1) ? P.pt : P.p;
+    float *dst = (it & 1) ? P.p : P.pt;
+    auto issue = [&](int r, int buf) {
+      const long long gb = ((long long)r * nctas + blockIdx.x) * W + w;
+      const bool act = r < rounds_b && gb < nblocks;  // warp-uniform
+      uint32_t biw = 0;
+      if (act && lane < BI_WORDS)
+        biw = cached ? s_cache[(r * W + w) * BI_WORDS + lane] : __ldcg(P.binfo + gb * BI_WORDS + lane);
+      const uint32_t own = __shfl_sync(full, biw, 0);
+      const uint32_t alpha = __shfl_sync(full, biw, 1);
+      const uint32_t c11 = __shfl_sync(full, biw, 11), c12 = __shfl_sync(full, biw, 12);
+      uint32_t fb[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) fb[q] = __shfl_sync(full, biw, 5 + (int)(hax[q] >> 12));
+      uint32_t addr[3];
+      if (c11 == 0u && (c12 & 0xFFFFu) == 0u) {  // all six faces border same-level blocks
+#pragma unroll
+        for (int q = 0; q < 3; q++) addr[q] = fb[q] + ((hpk[q] >> 9) & 63u);
+      } else {
+        const int bx = (int)__shfl_sync(full, biw, 2), by = (int)__shfl_sync(full, biw, 3),
+                  bz = (int)__shfl_sync(full, biw, 4);
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const uint32_t pk = hpk[q], ga = hax[q];
+          const int f = (int)(ga >> 12);
+          const int code = (int)(((f < 4 ? c11 : c12) >> (8 * (f & 3))) & 0xFFu);
+          uint32_t li = code == 0 ? (pk >> 9) & 63u : code == 16 ? (pk >> 15) & 63u : (pk >> 21) & 63u;
+          if (code > 0 && code < 16) {  // coarser by `code` levels: injection
+            const int cx = bx + (int)(ga & 15u) - 1, cy = by + (int)((ga >> 4) & 15u) - 1,
+                      cz = bz + (int)((ga >> 8) & 15u) - 1;
+            li = (uint32_t)local_of((cx >> code) & 3, (cy >> code) & 3, (cz >> code) & 3);
+          }
+          addr[q] = fb[q] + li;
+        }
+      }
+      b_own[buf] = act ? own : ~0u;
+      b_alpha[buf] = alpha;
+      if (act) {
+        float *T = s_pt[w][buf];
+        cp_async8(T + oA, src + own + 2 * lane);
+#pragma unroll
+        for (int q = 0; q < 3; q++) cp_async4(T + (hpk[q] & 511u), src + addr[q]);
+        cp_async8(s_pd[w][buf] + 2 * lane, P.div + own + 2 * lane);
+      }
+      cp_async_commit();
+    };
+#pragma unroll
+    for (int k = 0; k < NB - 1; k++) issue(k, k);
+    for (int r0 = 0; r0 < rounds_b; r0 += NB)
+#pragma unroll
+    for (int buf = 0; buf < NB; buf++) {  // round r0 + buf uses buffer buf (compile-time index)
+      const int r = r0 + buf;
+      issue(r + NB - 1, (buf + NB - 1) % NB);
+      cp_async_wait<NB - 1>();  // the copies of block r are complete
+      __syncwarp();
+      const uint32_t own = b_own[buf];
+      if (own != ~0u) {
+        const float *T = s_pt[w][buf];
+        const float2 ab = *reinterpret_cast<const float2 *>(T + oA);
+        const float2 L = *reinterpret_cast<const float2 *>(T + oA - SX);
+        const float2 R = *reinterpret_cast<const float2 *>(T + oA + SX);
+        const float2 Dn = *reinterpret_cast<const float2 *>(T + oA - SY);
+        const float2 Up = *reinterpret_cast<const float2 *>(T + oA + SY);
+        const float Bk = T[oA - 1], Fw = T[oA + 2];
+        const float2 dv = *reinterpret_cast<const float2 *>(s_pd[w][buf] + 2 * lane);
+        const float al = __uint_as_float(b_alpha[buf]);
+        const float adA = al * dv.x, adB = al * dv.y;
+        float2 res;
+        res.x = div6(L.x + R.x + Dn.x + Up.x + Bk + ab.y - adA);
+        res.y = div6(L.y + R.y + Dn.y + Up.y + ab.x + Fw - adB);
+        reinterpret_cast<float2 *>(dst + own)[lane] = res;
+      }
+      __syncwarp();  // buffer `buf` may be refilled by the next issue
+    }
+    cp_async_wait<0>();
+    if (it + 1 < sweeps) barrier();
+  }
+}
 
 // One round of the batched cascade: level maxtop - round of every member that
 // has it, optional prolongation from the member's parent level, then `sweeps`
@@ -796,9 +942,9 @@ __device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long 
 // store per cell. Larger levels are swept one block per warp through a 6^3
 // shared-memory tile holding the block and its face halo. Arithmetic is that
 // of k_jacobi (identical results).
-template <int CACHE>
-__global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const __grid_constant__ SolveBatch P, int round, int sweeps,
-                                                           int tree) {
+template <int CACHE, int NB = 0>
+__global__ void __launch_bounds__(256, NB ? DCG_PIPE_MINB : DCG_SOLVE_MINB)
+    k_level_solve_batch(const __grid_constant__ SolveBatch P, int round, int sweeps, int tree) {
   __shared__ long long s_end[BMAX];
   __shared__ int s_lev[BMAX];
   extern __shared__ uint32_t s_cache[];
@@ -865,6 +1011,8 @@ __global__ void __launch_bounds__(256, DCG_SOLVE_MINB) k_level_solve_batch(const
       }
       if (it + 1 < sweeps) barrier();
     }
+  } else if constexpr (NB > 0) {
+    solve_pipelined<CACHE, NB>(P, s_end, s_lev, s_cache, total, nctas, sweeps, tree);
   } else {
     // staged sweeps, one warp per block: per round each of the CTA's 8 warps
     // takes one block; its 64 cells and 96 face-halo cells go into a 6^3 tile
@@ -1558,20 +1706,42 @@ void launch_restrict_batch(RestrictBatch &P, cudaStream_t st) {
   if (acc > 0) k_restrict_batch<<<(unsigned)acc, 256, 0, st>>>(P);
 }
 
-template <int C>
+template <int C, int NB>
 static int solve_batch_occupancy() {
   // static + dynamic shared memory above 48 KB needs the opt-in
   const int smem = C * 8 * 256 * 4;
-  if (smem > 0 &&
-      cudaFuncSetAttribute(k_level_solve_batch<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+  if (smem > 0 && cudaFuncSetAttribute(k_level_solve_batch<C, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       smem) != cudaSuccess)
     return 0;
   int a = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_level_solve_batch<C>, 256, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_level_solve_batch<C, NB>, 256, smem) != cudaSuccess)
+    return 0;
   return a;
 }
+// solve variants: cache depth 0, 3, 4 or 8 (cells per thread of the small-level
+// path; 8 KB of dynamic shared memory each); + SOLVE_PIPE (16): pipelined
+// staged sweeps with two tile buffers per warp, + 2 * SOLVE_PIPE: three
+static int solve_occupancy(int cache) {
+  switch (cache) {
+    case 8: return solve_batch_occupancy<8, 0>();
+    case 4: return solve_batch_occupancy<4, 0>();
+    case 3: return solve_batch_occupancy<3, 0>();
+    case 0: return solve_batch_occupancy<0, 0>();
+    case 16: return solve_batch_occupancy<0, 2>();
+    case 32: return solve_batch_occupancy<0, 3>();
+    case 16 + 2: return solve_batch_occupancy<2, 2>();
+    case 16 + 3: return solve_batch_occupancy<3, 2>();
+    case 32 + 2: return solve_batch_occupancy<2, 3>();
+    case 32 + 3: return solve_batch_occupancy<3, 3>();
+    default: return 0;
+  }
+}
+bool solve_variant_valid(int cache) {
+  return cache == 0 || cache == 3 || cache == 4 || cache == 8 || cache == 16 || cache == 18 || cache == 19 ||
+         cache == 32 || cache == 34 || cache == 35;
+}
 int batch_solve_grid(int sms, int cache, int ctas_per_sm) {
-  const int occ = cache == 8 ? solve_batch_occupancy<8>() : cache == 4 ? solve_batch_occupancy<4>()
-                  : cache == 3 ? solve_batch_occupancy<3>() : solve_batch_occupancy<0>();
+  const int occ = solve_occupancy(cache);
   const int k = (ctas_per_sm > 0 && ctas_per_sm < occ) ? ctas_per_sm : occ;
   return k * sms;
 }
@@ -1580,18 +1750,26 @@ void launch_level_solve_batch(const SolveBatch &P, int round, int sweeps, int gr
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(256);
-  if (cache != 8 && cache != 4 && cache != 3) cache = 0;
-  cfg.dynamicSmemBytes = (size_t)cache * 8 * 256 * 4;
+  if (!solve_variant_valid(cache)) cache = 0;
+  cfg.dynamicSmemBytes = (size_t)(cache & 15) * 8 * 256 * 4;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (cache == 8) cudaLaunchKernelEx(&cfg, k_level_solve_batch<8>, P, round, sweeps, tree);
-  else if (cache == 4) cudaLaunchKernelEx(&cfg, k_level_solve_batch<4>, P, round, sweeps, tree);
-  else if (cache == 3) cudaLaunchKernelEx(&cfg, k_level_solve_batch<3>, P, round, sweeps, tree);
-  else cudaLaunchKernelEx(&cfg, k_level_solve_batch<0>, P, round, sweeps, tree);
+  switch (cache) {
+    case 8: cudaLaunchKernelEx(&cfg, k_level_solve_batch<8, 0>, P, round, sweeps, tree); break;
+    case 4: cudaLaunchKernelEx(&cfg, k_level_solve_batch<4, 0>, P, round, sweeps, tree); break;
+    case 3: cudaLaunchKernelEx(&cfg, k_level_solve_batch<3, 0>, P, round, sweeps, tree); break;
+    case 16: cudaLaunchKernelEx(&cfg, k_level_solve_batch<0, 2>, P, round, sweeps, tree); break;
+    case 32: cudaLaunchKernelEx(&cfg, k_level_solve_batch<0, 3>, P, round, sweeps, tree); break;
+    case 18: cudaLaunchKernelEx(&cfg, k_level_solve_batch<2, 2>, P, round, sweeps, tree); break;
+    case 19: cudaLaunchKernelEx(&cfg, k_level_solve_batch<3, 2>, P, round, sweeps, tree); break;
+    case 34: cudaLaunchKernelEx(&cfg, k_level_solve_batch<2, 3>, P, round, sweeps, tree); break;
+    case 35: cudaLaunchKernelEx(&cfg, k_level_solve_batch<3, 3>, P, round, sweeps, tree); break;
+    default: cudaLaunchKernelEx(&cfg, k_level_solve_batch<0, 0>, P, round, sweeps, tree); break;
+  }
 }
 
 }  // namespace dcg

@@ -316,7 +316,9 @@ typedef struct {
                                 advect scalars, divergence, apply pressure; 1: one warp per
                                 block through shared tiles of the block and its apron      */
   int32_t solve_cache;       /* cells per thread whose stencil the level solve keeps in
-                                shared memory: 0, 3, 4 or 8 (8 KB of shared memory each)    */
+                                shared memory: 0, 3, 4 or 8 (8 KB of shared memory each);
+                                16 + c (c = 0, 2, 3): pipelined staged sweeps, asynchronous
+                                copies into two tile buffers per warp; 32 + c: three     */
   int32_t solve_ctas_per_sm; /* CTAs per SM of the cooperative solve (0 = occupancy limit) */
   int32_t solve_barrier;     /* grid barrier between sweeps: 0 flat, 1 two-level            */
   int32_t persistent;        /* cell stages as persistent kernels over the allocated blocks */

@@ -85,10 +85,17 @@ def test_results_do_not_depend_on_tuning():
     rounds.round_ctas_per_sm[0], rounds.round_cache[0], rounds.round_barrier[0] = 1, 0, 1
     rounds.round_ctas_per_sm[1], rounds.round_cache[1], rounds.round_barrier[1] = 2, 3, 0
     staged = tuning(1, 4, 0, 1, 1)
+    # one CTA per SM makes the levels large enough for the staged sweeps;
+    # variants 16 / 32 read block descriptions from the global table
+    piped2, piped3 = tuning(4, 18, 1, 0, 1), tuning(1, 35, 1, 1, 1)
+    piped_global2, piped_global3 = tuning(4, 16, 1, 1, 1), tuning(2, 32, 2, 0, 0)
+    piped_rounds = tuning(4, 4, 0, 1, 1)
+    piped_rounds.round_ctas_per_sm[1], piped_rounds.round_cache[1], piped_rounds.round_barrier[1] = 2, 34, 0
     mixed_tiles = tuning(4, 4, 0, 1, 0)
     mixed_tiles.tile[0], mixed_tiles.tile[3] = 1, 1
     for t in [tuning(2, 0, 1, 0), tuning(8, 8, 2, 1, 1), tuning(2, 8, 1, 0, 1), tuning(8, 0, 0, 1),
-              tuning(4, 3, 0, 0, 1), rounds, staged, mixed_tiles]:
+              tuning(4, 3, 0, 0, 1), rounds, staged, mixed_tiles, piped2, piped3, piped_rounds, piped_global2,
+              piped_global3]:
         b = batch_run(params, 5, t)
         for i, p in enumerate(params):
             compare(b[i], ref[i], p, f"tiles {list(t.tile)} cache {t.solve_cache} member {i}")
@@ -107,7 +114,7 @@ def test_autotune_resets_and_keeps_results():
     b = Batch(params)
     t = b.autotune(spinup_steps=3, reps=2)
     assert all(x in (1, 2, 4, 8) for x in t["tile"])
-    assert t["solve_cache"] in (0, 3, 4, 8) and t["solve_barrier"] in (0, 1)
+    assert t["solve_cache"] in (0, 3, 4, 8, 16, 18, 19, 32, 34, 35) and t["solve_barrier"] in (0, 1)
     assert t["solve_ms"] > 0
     fresh = Batch(params)
     for i, p in enumerate(params):
