@@ -66,6 +66,9 @@ struct dcg_sim {
   // barrier, 1 neighbour epochs, 2 two-level barrier
   int ls_epoch = 3;
   int ls_grid_staged = 0;  // CTAs of the staged solve
+  // level solve of single simulations: pipelined staged sweeps, two tile buffers,
+  // block descriptions cached in 3 x 8 KB of shared memory when they fit
+  static constexpr int kSolveVariant = 19;
   // batch members: p and p~ are slices of the batch's arenas, and the batch
   // steps the member (its own step and stage entry points are refused)
   float *ext_p = nullptr, *ext_pt = nullptr, *ext_div = nullptr;
@@ -280,7 +283,7 @@ struct dcg_sim {
     if (const char *m = std::getenv("DCG_SOLVE_SYNC"))
       ls_epoch = std::strcmp(m, "epoch") == 0 ? 1 : std::strcmp(m, "barrier") == 0 ? 0
                  : std::strcmp(m, "tree") == 0 ? 2 : 3;
-    ls_grid_staged = batch_solve_grid(sms, 4, 0);
+    ls_grid_staged = batch_solve_grid(sms, kSolveVariant, 0);
     if (ls_grid_staged <= 0 && ls_epoch == 3) ls_epoch = 2;
     if (P.emission_n > 0) {
       const size_t ne = (size_t)P.emission_n * P.emission_n * P.emission_n;
@@ -377,15 +380,23 @@ struct dcg_sim {
   }
 
   // stages (fluid_simulation_dcgrid.cu:263-346)
+  // the cell stages through the batched launchers as a batch of one: staged
+  // (one warp per block) except velocity advection (persistent, 2 blocks per CTA)
+  void cells(int stage, int tile) {
+    CellBatch C{};
+    C.n = 1;
+    C.d[0] = D;
+    launch_cells_batch(stage, C, tile, stream, true);
+  }
   void a_advect_velocity() {
-    launch_advect_velocity(D, stream);
+    cells(0, 2);
     vpar ^= 1;
     bind_parity();
     restrict_v();
   }
   void a_adapt() { launch_adapt(D, S, keys, vals, keys2, vals2, sms, stream); }
   void a_project(bool local) {
-    launch_divergence(D, stream);
+    cells(2, 1);
     restrict_div();
     const int top = D.g.levels - 1;
     if (ls_grid > 0) {
@@ -420,7 +431,7 @@ struct dcg_sim {
         }
       }
     }
-    launch_apply_pressure(D, stream);
+    cells(3, 1);
     restrict_v();
   }
   // ---------------------------------------------------------------- state I/O
@@ -484,10 +495,10 @@ struct dcg_sim {
       SB.d[0].pt = ppt;
       SB.d[0].div = pdiv;
     }
-    launch_level_solve_batch(SB, SB.maxtop - level, sweeps, ls_grid_staged, 4, 1, stream);
+    launch_level_solve_batch(SB, SB.maxtop - level, sweeps, ls_grid_staged, kSolveVariant, 1, stream);
   }
   void a_advect_scalars() {
-    launch_advect_scalars(D, stream);
+    cells(1, 1);
     qpar ^= 1;
     bind_parity();
     restrict_q();
