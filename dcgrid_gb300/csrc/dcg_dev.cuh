@@ -100,6 +100,42 @@ struct Dev {
   double *dnorm;           // defect correction: FP64 ||r||^2, ||div||^2 per pass
 };
 
+// Scoped atomics of the grid barriers (PTX memory model): arrivals are
+// acquire-release read-modify-writes, the release of the waiting CTAs a
+// release add on the generation word, the wait an acquire load of it. Before
+// the arrival, __syncthreads orders the CTA's writes before thread 0's release;
+// after the wait, __syncthreads orders thread 0's acquire before the CTA's
+// reads; so every write before the barrier is visible to every read after it.
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned *p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ void red_add_release(unsigned *p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(unsigned *p, unsigned v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// Bounded wait for the generation word to leave g: after 2^22 polls the CTA
+// records DCG_DEVERR_TIMEOUT (8) in the error word and gives up.
+__device__ __forceinline__ void barrier_wait(const unsigned *gen, unsigned g, uint32_t *errw) {
+  volatile unsigned *err = errw;
+  unsigned spins = 0;
+  while (ld_acquire(gen) == g) {
+    __nanosleep(32);
+    if (++spins > (1u << 22) || (*err & 8u)) {
+      atomicOr(errw, 8u);
+      break;
+    }
+  }
+}
+
 // Two-level grid barrier: CTAs arrive on one of 16 group counters (separate
 // 128-byte lines); the last of each group arrives on the top counter, and the
 // last there releases everyone through the generation word. Same bounded wait
@@ -109,36 +145,24 @@ __device__ inline void grid_barrier_tree(uint32_t *bar, uint32_t *errw, unsigned
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned *tb = bar + 64;
-    volatile unsigned *gen = tb;
     volatile unsigned *err = errw;
     if ((*err & 8u) == 0) {
-      const unsigned g = *gen;
+      const unsigned g = ld_acquire(tb);
       const unsigned grp = blockIdx.x & 15u;
       const unsigned members = (nctas >> 4) + ((grp < (nctas & 15u)) ? 1u : 0u);
       const unsigned groups = nctas < 16u ? nctas : 16u;
-      __threadfence();
       bool release = false;
-      if (atomicAdd(tb + 32 * (1 + grp), 1u) == members - 1) {
-        atomicExch(tb + 32 * (1 + grp), 0u);
-        if (atomicAdd(tb + 32 * 17, 1u) == groups - 1) {
-          atomicExch(tb + 32 * 17, 0u);
+      if (atom_add_acq_rel(tb + 32 * (1 + grp), 1u) == members - 1) {
+        st_relaxed(tb + 32 * (1 + grp), 0u);
+        if (atom_add_acq_rel(tb + 32 * 17, 1u) == groups - 1) {
+          st_relaxed(tb + 32 * 17, 0u);
           release = true;
         }
       }
-      if (release) {
-        __threadfence();
-        atomicAdd(tb, 1u);
-      } else {
-        unsigned spins = 0;
-        while (*gen == g) {
-          __nanosleep(32);
-          if (++spins > (1u << 22) || (*err & 8u)) {
-            atomicOr(errw, 8u);
-            break;
-          }
-        }
-      }
-      __threadfence();
+      if (release)
+        red_add_release(tb, 1u);
+      else
+        barrier_wait(tb, g, errw);
     }
   }
   __syncthreads();
@@ -152,26 +176,15 @@ __device__ inline void grid_barrier_tree(const Dev &D, unsigned nctas) { grid_ba
 __device__ inline void grid_barrier(uint32_t *bar, uint32_t *errw, unsigned nctas) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned *gen = bar + 1;
     volatile unsigned *err = errw;
     if ((*err & 8u) == 0) {
-      const unsigned g = *gen;
-      __threadfence();
-      if (atomicAdd(bar, 1u) == nctas - 1) {
-        atomicExch(bar, 0u);
-        __threadfence();
-        atomicAdd(bar + 1, 1u);
+      const unsigned g = ld_acquire(bar + 1);
+      if (atom_add_acq_rel(bar, 1u) == nctas - 1) {
+        st_relaxed(bar, 0u);
+        red_add_release(bar + 1, 1u);
       } else {
-        unsigned spins = 0;
-        while (*gen == g) {
-          __nanosleep(32);
-          if (++spins > (1u << 22) || (*err & 8u)) {
-            atomicOr(errw, 8u);
-            break;
-          }
-        }
+        barrier_wait(bar + 1, g, errw);
       }
-      __threadfence();
     }
   }
   __syncthreads();
