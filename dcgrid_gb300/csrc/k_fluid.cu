@@ -808,10 +808,12 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// Staged sweeps as in the per-pass form below, pipelined: each warp walks its
-// blocks (round r: level block ((r * nctas + blockIdx.x) * 8 + warp)) with NB
-// tile buffers; the copies of block r + NB - 1 (own cells, three halo cells
-// per lane, divergence) are issued before block r is computed from its tile.
+// Staged sweeps as in the per-pass form below, pipelined: the warps of a CTA
+// claim the CTA's blocks (level blocks ((r * nctas + blockIdx.x) * 8 + w'))
+// from a shared counter, so faster warps take more of them, and each warp
+// cycles its blocks through NB tile buffers: the copies of its next NB - 1
+// blocks (own cells, three halo cells per lane, divergence) are in flight
+// while a block is computed from its tile.
 // The copies read the previous sweep's results written by other SMs; the grid
 // barrier's fences order them. Block descriptions come from the launch's
 // shared cache when they fit, else from the global table, through shuffles.
@@ -843,8 +845,17 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
       __syncwarp();
     }
   }
-  __syncwarp();
-  if (!cached) __threadfence_block();
+  // blocks are claimed dynamically inside the CTA: CTA-local block k = r * W +
+  // w' is level block ((r * nctas + blockIdx.x) * W + w'), valid for k < kcount
+  __shared__ unsigned s_next[2];
+  if (t == 0) s_next[0] = s_next[1] = 0u;
+  __syncthreads();  // block descriptions filled by every warp, counters zeroed
+  int kcount = 0;
+  for (int r = 0; r < rounds_b; r++) {
+    const long long g0 = ((long long)r * nctas + blockIdx.x) * W;
+    const long long left = nblocks - g0;
+    kcount += left <= 0 ? 0 : (left >= W ? W : (int)left);
+  }
   auto barrier = [&]() {
     if (tree) grid_barrier_tree(P.bar, P.err, nctas);
     else grid_barrier(P.bar, P.err, nctas);
@@ -854,12 +865,17 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
   for (int it = 0; it < sweeps; it++) {
     const float *src = (it & 1) ? P.pt : P.p;
     float *dst = (it & 1) ? P.p : P.pt;
-    auto issue = [&](int r, int buf) {
-      const long long gb = ((long long)r * nctas + blockIdx.x) * W + w;
-      const bool act = r < rounds_b && gb < nblocks;  // warp-uniform
+    if (t == 0) s_next[(it + 1) & 1] = 0u;  // the next sweep's counter; its last use ended before the barrier
+    unsigned *cnt = &s_next[it & 1];
+    auto issue = [&](int buf) {
+      unsigned kk = 0;
+      if (lane == 0) kk = atomicAdd(cnt, 1u);
+      const int k = (int)__shfl_sync(full, kk, 0);
+      const bool act = k < kcount;  // warp-uniform; a warp's claims only grow
+      const long long gb = ((long long)(k >> 3) * nctas + blockIdx.x) * W + (k & 7);
       uint32_t biw = 0;
       if (act && lane < BI_WORDS)
-        biw = cached ? s_cache[(r * W + w) * BI_WORDS + lane] : __ldcg(P.binfo + gb * BI_WORDS + lane);
+        biw = cached ? s_cache[k * BI_WORDS + lane] : __ldcg(P.binfo + gb * BI_WORDS + lane);
       const uint32_t own = __shfl_sync(full, biw, 0);
       const uint32_t alpha = __shfl_sync(full, biw, 1);
       const uint32_t c11 = __shfl_sync(full, biw, 11), c12 = __shfl_sync(full, biw, 12);
@@ -899,15 +915,17 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
       cp_async_commit();
     };
 #pragma unroll
-    for (int k = 0; k < NB - 1; k++) issue(k, k);
-    for (int r0 = 0; r0 < rounds_b; r0 += NB)
+    for (int k = 0; k < NB - 1; k++) issue(k);
+    bool done = false;
+    while (!done)
 #pragma unroll
-    for (int buf = 0; buf < NB; buf++) {  // round r0 + buf uses buffer buf (compile-time index)
-      const int r = r0 + buf;
-      issue(r + NB - 1, (buf + NB - 1) % NB);
-      cp_async_wait<NB - 1>();  // the copies of block r are complete
+    for (int buf = 0; buf < NB; buf++) {  // the warp's blocks cycle through the buffers in claim order
+      if (done) break;
+      issue((buf + NB - 1) % NB);
+      cp_async_wait<NB - 1>();  // the copies of the block in `buf` are complete
       __syncwarp();
       const uint32_t own = b_own[buf];
+      done = own == ~0u;  // no block claimed: every later claim of this warp is empty too
       if (own != ~0u) {
         const float *T = s_pt[w][buf];
         const float2 ab = *reinterpret_cast<const float2 *>(T + oA);
