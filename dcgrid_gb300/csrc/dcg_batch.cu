@@ -391,7 +391,7 @@ struct dcg_batch {
       P.n = std::min(BMAX, n() - g * BMAX);
       for (int i = 0; i < P.n; i++) P.d[i] = m[g * BMAX + i]->D;
       launch_stats_zero(P, stream);
-      launch_cells_batch(4, P, 4, stream, tune.persistent != 0);
+      launch_cells_batch(4, P, 1, stream, true);  // staged statistics
       launch_stats_gather(P, stage_dev + g * BMAX, stream);
     }
     cudaMemcpyAsync(stage, stage_dev, sizeof(StatRecord) * n(), cudaMemcpyDeviceToHost, stream);

@@ -1174,9 +1174,22 @@ __global__ void __launch_bounds__(256, NB ? DCG_PIPE_MINB : DCG_SOLVE_MINB)
 template <int STAGE>
 __global__ void __launch_bounds__(256) k_cells_staged(const __grid_constant__ CellBatch P) {
   constexpr int W = 8, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 8;
-  constexpr int NT = STAGE == 2 ? 3 : 2;
+  constexpr int NT = STAGE == 2 ? 3 : STAGE == 3 ? 2 : 1;
   __shared__ long long s_end[BMAX * MAXL];
   __shared__ __align__(16) float s_tile[W][NT][TILE];
+  // statistics (STAGE 4): per-lane FP64 sums while the warp's member and level
+  // stay the same, reduced and added with one atomic per quantity on a change
+  double a_res = 0.0, a_mass = 0.0;
+  int a_cnt = 0, a_mem = -1, a_lvl = 0;
+  auto flush = [&]() {
+    double r = a_res, m = a_mass;
+    for (int o = 16; o > 0; o >>= 1) {
+      r += __shfl_xor_sync(0xffffffffu, r, o);
+      m += __shfl_xor_sync(0xffffffffu, m, o);
+    }
+    const int n = (int)__reduce_add_sync(0xffffffffu, (unsigned)a_cnt);
+    stats_flush(P.d[a_mem], r, m, a_lvl, (double)n);
+  };
   const int nseg = P.n * MAXL;
   for (int i = threadIdx.x; i < nseg; i += blockDim.x) {
     const Dev &D = P.d[i / MAXL];
@@ -1209,8 +1222,48 @@ __global__ void __launch_bounds__(256) k_cells_staged(const __grid_constant__ Ce
     const bool leaf = D.child[8u * b + (lane >> 2)] == NONE;
     const int scale = 1 << bp.w;
     const float alpha = 0.5f * D.ph.rdx / (float)scale;
-    float *T0 = s_tile[w][0], *T1 = s_tile[w][1];
-    if constexpr (STAGE == 2) {
+    float *T0 = s_tile[w][0], *T1 = s_tile[w][NT > 1 ? 1 : 0];
+    if constexpr (STAGE == 4) {
+      // stats_vals for the lane's two cells: pressure tile, FP32 residual and mass
+      const float2 p2 = reinterpret_cast<const float2 *>(D.p + own)[lane];
+      float hp[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) hp[q] = D.p[hc[q]];
+      *reinterpret_cast<float2 *>(T0 + oA) = p2;
+#pragma unroll
+      for (int q = 0; q < 3; q++) T0[hpk[q] & 511u] = hp[q];
+      __syncwarp();
+      const unsigned leafmask = __ballot_sync(full, leaf);
+      if (leafmask) {  // warp-uniform
+        if (seg / MAXL != a_mem || bp.w != a_lvl) {
+          if (a_mem >= 0) flush();
+          a_mem = seg / MAXL;
+          a_lvl = bp.w;
+          a_res = a_mass = 0.0;
+          a_cnt = 0;
+        }
+        if (leaf) {
+          const float2 dv = reinterpret_cast<const float2 *>(D.div + own)[lane];
+          const float2 w2 = reinterpret_cast<const float2 *>(D.w + own)[lane];
+          const float qa = q_ld(D, 0, own + 2 * lane), qb = q_ld(D, 0, own + 2 * lane + 1);
+          const float2 L = *reinterpret_cast<const float2 *>(T0 + oA - SX);
+          const float2 R = *reinterpret_cast<const float2 *>(T0 + oA + SX);
+          const float2 Dn = *reinterpret_cast<const float2 *>(T0 + oA - SY);
+          const float2 U = *reinterpret_cast<const float2 *>(T0 + oA + SY);
+          const float Bk = T0[oA - 1], Fw = T0[oA + 2];
+          const float as = D.ph.rdx * D.ph.rdx / (float)(scale * scale);
+          const float rA = dv.x - (L.x + R.x + Dn.x + U.x + Bk + p2.y - 6.f * p2.x) * as;
+          const float rB = dv.y - (L.y + R.y + Dn.y + U.y + p2.x + Fw - 6.f * p2.y) * as;
+          const float s3 = (float)(scale * scale * scale);
+          a_res += (double)((float)scale * fabsf(rA));
+          a_res += (double)((float)scale * fabsf(rB));
+          a_mass += (double)(qa * w2.x * s3);
+          a_mass += (double)(qb * w2.y * s3);
+          a_cnt += 2;
+        }
+      }
+      __syncwarp();
+    } else if constexpr (STAGE == 2) {
       float *T2 = s_tile[w][2];
       const float2 w2 = reinterpret_cast<const float2 *>(D.w + own)[lane];
       const float2 vx = reinterpret_cast<const float2 *>(D.v[0] + own)[lane];
@@ -1299,6 +1352,7 @@ __global__ void __launch_bounds__(256) k_cells_staged(const __grid_constant__ Ce
       __syncwarp();
     }
   }
+  if (STAGE == 4 && a_mem >= 0) flush();
 }
 // ------------------------------------------------------ staged advection
 // Advection one warp per block: the block's 64 cells and its 152 apron cells
@@ -1627,14 +1681,15 @@ static void launch_advect_staged(int stage, const CellBatch &P, cudaStream_t st)
 }
 
 static unsigned staged_grid(int stage) {
-  static unsigned g[2] = {0, 0};
-  const int i = stage == 2 ? 0 : 1;
+  static unsigned g[3] = {0, 0, 0};
+  const int i = stage == 2 ? 0 : stage == 3 ? 1 : 2;
   if (!g[i]) {
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (stage == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cells_staged<2>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cells_staged<3>, 256, 0);
+    else if (stage == 3) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cells_staged<3>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cells_staged<4>, 256, 0);
     g[i] = (unsigned)(sms * (occ > 0 ? occ : 1));
   }
   return g[i];
@@ -1692,10 +1747,11 @@ static void cells_batch_tb(int stage, const CellBatch &P, unsigned grid, cudaStr
   }
 }
 void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st, bool persistent) {
-  if (tile == 1 && stage < 4) {  // staged, one warp per block
+  if (tile == 1) {  // staged, one warp per block
     if (stage < 2) launch_advect_staged(stage, P, st);
     else if (stage == 2) k_cells_staged<2><<<staged_grid(2), 256, 0, st>>>(P);
-    else k_cells_staged<3><<<staged_grid(3), 256, 0, st>>>(P);
+    else if (stage == 3) k_cells_staged<3><<<staged_grid(3), 256, 0, st>>>(P);
+    else k_cells_staged<4><<<staged_grid(4), 256, 0, st>>>(P);
     return;
   }
   if (tile != 2 && tile != 8) tile = 4;
