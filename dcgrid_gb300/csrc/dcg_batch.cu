@@ -83,7 +83,7 @@ struct dcg_batch {
     solve_grid = batch_solve_grid(sms, tune.solve_cache, tune.solve_ctas_per_sm);
     if (solve_grid <= 0) return fail(DCG_E_CUDA, "cooperative level solve cannot be resident");
     for (int r = 0; r < 4; r++) {
-      if (tune.round_ctas_per_sm[r] <= 0) continue;
+      if (tune.round_ctas_per_sm[r] == 0) continue;
       const int c = tune.round_cache[r];
       if (!solve_variant_valid(c) || (tune.round_barrier[r] != 0 && tune.round_barrier[r] != 1))
         return fail(DCG_E_INVALID, "round schedule: a valid solve variant and barrier 0 or 1");
@@ -135,7 +135,7 @@ struct dcg_batch {
   // the cascade with the tuned schedule of each round
   void solve_tuned() {
     for (int round = 0; round <= maxtop; round++) {
-      if (round < 4 && tune.round_ctas_per_sm[round] > 0)
+      if (round < 4 && tune.round_ctas_per_sm[round] != 0)
         solve_round(round, batch_solve_grid(sms, tune.round_cache[round], tune.round_ctas_per_sm[round]),
                     tune.round_cache[round], tune.round_barrier[round]);
       else
@@ -357,7 +357,9 @@ struct dcg_batch {
       best.round_ctas_per_sm[r] = 0;
       for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35}) {
         const int occ = batch_solve_grid(sms, cache, 0) / std::max(1, sms);
-        for (int k = 1; k <= occ; k++)
+        std::vector<int> ks = {-8, -4, -2};  // k < 0: one CTA per -k SMs (small rounds)
+        for (int k = 1; k <= occ; k++) ks.push_back(k);
+        for (int k : ks)
           for (int tree = 0; tree < 2; tree++) {
             const int grid = batch_solve_grid(sms, cache, k);
             const float ms = time_ms(reps, [&] { solve_round(r, grid, cache, tree); });

@@ -6,6 +6,8 @@
 // warp covers half a block (4 subblocks, 32 contiguous floats = 128 B), so
 // every field plane is read and written in full 128-byte lines.
 #include "dcg_dev.cuh"
+#include <algorithm>
+
 #include "dcg_kernels.h"
 
 namespace dcg {
@@ -1816,6 +1818,8 @@ bool solve_variant_valid(int cache) {
 }
 int batch_solve_grid(int sms, int cache, int ctas_per_sm) {
   const int occ = solve_occupancy(cache);
+  if (occ <= 0) return 0;
+  if (ctas_per_sm < 0) return std::max(1, sms / -ctas_per_sm);  // one CTA per -ctas_per_sm SMs
   const int k = (ctas_per_sm > 0 && ctas_per_sm < occ) ? ctas_per_sm : occ;
   return k * sms;
 }

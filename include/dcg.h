@@ -322,8 +322,9 @@ typedef struct {
   int32_t solve_ctas_per_sm; /* CTAs per SM of the cooperative solve (0 = occupancy limit) */
   int32_t solve_barrier;     /* grid barrier between sweeps: 0 flat, 1 two-level            */
   int32_t persistent;        /* cell stages as persistent kernels over the allocated blocks */
-  /* per cascade round r < 4: its own schedule when round_ctas_per_sm[r] > 0
-   * (CTAs per SM, cache depth, barrier), else the solve_* fields above */
+  /* per cascade round r < 4: its own schedule when round_ctas_per_sm[r] != 0
+   * (CTAs per SM, or -k: one CTA per k SMs; cache depth; barrier), else the
+   * solve_* fields above */
   int16_t round_ctas_per_sm[4];
   int8_t round_cache[4];
   int8_t round_barrier[4];

@@ -91,6 +91,7 @@ def test_results_do_not_depend_on_tuning():
     piped_global2, piped_global3 = tuning(4, 16, 1, 1, 1), tuning(2, 32, 2, 0, 0)
     piped_rounds = tuning(4, 4, 0, 1, 1)
     piped_rounds.round_ctas_per_sm[1], piped_rounds.round_cache[1], piped_rounds.round_barrier[1] = 2, 34, 0
+    piped_rounds.round_ctas_per_sm[0], piped_rounds.round_cache[0], piped_rounds.round_barrier[0] = -4, 18, 1
     mixed_tiles = tuning(4, 4, 0, 1, 0)
     mixed_tiles.tile[0], mixed_tiles.tile[3] = 1, 1
     for t in [tuning(2, 0, 1, 0), tuning(8, 8, 2, 1, 1), tuning(2, 8, 1, 0, 1), tuning(8, 0, 0, 1),
