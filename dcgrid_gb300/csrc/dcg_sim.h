@@ -380,8 +380,8 @@ struct dcg_sim {
   }
 
   // stages (fluid_simulation_dcgrid.cu:263-346)
-  // the cell stages through the batched launchers as a batch of one: staged
-  // (one warp per block) except velocity advection (persistent, 2 blocks per CTA)
+  // the cell stages through the batched launchers as a batch of one, staged
+  // (one warp, or for the advections two warps, per block through shared tiles)
   void cells(int stage, int tile) {
     CellBatch C{};
     C.n = 1;
@@ -389,7 +389,7 @@ struct dcg_sim {
     launch_cells_batch(stage, C, tile, stream, true);
   }
   void a_advect_velocity() {
-    cells(0, 2);
+    cells(0, 1);
     vpar ^= 1;
     bind_parity();
     restrict_v();

@@ -1366,31 +1366,6 @@ __global__ void __launch_bounds__(256) k_cells_staged(const __grid_constant__ Ce
 // runs the per-cell body (advect_velocity_cell / advect_scalars_cell_t).
 // The arithmetic is sample_at's and the per-cell bodies' operation for
 // operation, so the results are identical.
-struct AdvSlots {  // the lane's apron slots a = lane + 32 r, r < 5 (152 slots)
-  uint32_t pk[5], ga[5];
-  int n;
-};
-template <int SX, int SY> __device__ __forceinline__ void apron_slots(int lane, AdvSlots &S) {
-  S.n = 0;
-#pragma unroll
-  for (int r = 0; r < 5; r++) S.pk[r] = S.ga[r] = 0;
-  int cnt = 0;
-  for (int idx = 0; idx < AW * AW * AW; idx++) {
-    const int ax = idx / 36, ay = (idx / 6) % 6, az = idx % 6;
-    if (ax > 0 && ax < AW - 1 && ay > 0 && ay < AW - 1 && az > 0 && az < AW - 1) continue;
-    if ((cnt & 31) == lane) {
-      const int same = local_of((ax - 1) & 3, (ay - 1) & 3, (az - 1) & 3);
-      const int self = local_of(clampi(ax, 1, BW) - 1, clampi(ay, 1, BW) - 1, clampi(az, 1, BW) - 1);
-      const int quirk = local_of(clampi(ax, 1, BW) & 3, clampi(ay, 1, BW) & 3, clampi(az, 1, BW) & 3);
-      const int d = dir_of(ax) * 9 + dir_of(ay) * 3 + dir_of(az);
-      S.pk[S.n] = (uint32_t)(ax * SX + ay * SY + az + 1) | ((uint32_t)same << 9) | ((uint32_t)self << 15) |
-                  ((uint32_t)quirk << 21);
-      S.ga[S.n] = (uint32_t)ax | ((uint32_t)ay << 4) | ((uint32_t)az << 8) | ((uint32_t)d << 12);
-      S.n++;
-    }
-    cnt++;
-  }
-}
 // The back-traced point of a cell of the block at bp0 lies in that block
 // (sample_at's block offset is 0); sub = the point's subblock. sample_at then
 // keeps the block unless that subblock has a child (a descent, level > 0).
@@ -1449,9 +1424,10 @@ __device__ __forceinline__ bool box_inside_t(const Geom &g, const SmpT &s) {
          s.z1 * s.scale < g.gz;
 }
 
-// resident CTAs per SM the staged advection's register allocation targets
+// resident CTAs per SM the staged advection's register allocation targets (4:
+// 64 registers; measured faster than 3 at 80 registers or 2 at 96)
 #ifndef DCG_ADV_MINB
-#define DCG_ADV_MINB 2
+#define DCG_ADV_MINB 4
 #endif
 // per-cell fallbacks, out of line so that the staged kernel keeps few registers
 __device__ __noinline__ void advect_velocity_cell_ool(const Dev &D, long long b, int c) { advect_velocity_cell(D, b, c); }
@@ -1460,13 +1436,16 @@ template <int MODE, int NQ> __device__ __noinline__ void advect_scalars_cell_ool
 }
 
 // STAGE 0: velocity (MODE, NQ unused); STAGE 1: scalars of members with
-// storage format MODE and NQ scalars (other members have no blocks here)
+// storage format MODE and NQ scalars (other members have no blocks here).
+// Four blocks per CTA pass, 64 threads (two warps) per block, one cell per
+// thread; the two warps of a block share its tiles through a named barrier.
 template <int STAGE, int MODE, int NQ>
 __global__ void __launch_bounds__(256, DCG_ADV_MINB) k_advect_staged(const __grid_constant__ CellBatch P) {
-  constexpr int W = 8, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 8;
+  constexpr int NBK = 4, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 8;
   constexpr int NF = STAGE == 0 ? 4 : 1 + NQ;  // tile 0: fluidity
   __shared__ long long s_end[BMAX * MAXL];
-  __shared__ __align__(16) float s_tile[W][NF][TILE];
+  __shared__ __align__(16) float s_tile[NBK][NF][TILE];
+  __shared__ uint32_t s_slot[2][3][64];  // apron slots a = c + 64 r of thread c (pk ~0u: none)
   const int nseg = P.n * MAXL;
   for (int i = threadIdx.x; i < nseg; i += blockDim.x) {
     const Dev &D = P.d[i / MAXL];
@@ -1474,116 +1453,103 @@ __global__ void __launch_bounds__(256, DCG_ADV_MINB) k_advect_staged(const __gri
     const bool mine = STAGE == 0 || (D.g.mixed == MODE && D.g.nq == NQ);
     s_end[i] = (mine && l < D.g.levels) ? __ldcg(D.load + l) : 0;
   }
+  if (threadIdx.x < 64) {
+    const int c = threadIdx.x;
+#pragma unroll 1
+    for (int r = 0; r < 3; r++) s_slot[0][r][c] = ~0u, s_slot[1][r][c] = 0u;
+    int cnt = 0;
+    for (int idx = 0; idx < AW * AW * AW; idx++) {
+      const int ax = idx / 36, ay = (idx / 6) % 6, az = idx % 6;
+      if (ax > 0 && ax < AW - 1 && ay > 0 && ay < AW - 1 && az > 0 && az < AW - 1) continue;
+      if ((cnt & 63) == c) {
+        const int same = local_of((ax - 1) & 3, (ay - 1) & 3, (az - 1) & 3);
+        const int self = local_of(clampi(ax, 1, BW) - 1, clampi(ay, 1, BW) - 1, clampi(az, 1, BW) - 1);
+        const int quirk = local_of(clampi(ax, 1, BW) & 3, clampi(ay, 1, BW) & 3, clampi(az, 1, BW) & 3);
+        const int d = dir_of(ax) * 9 + dir_of(ay) * 3 + dir_of(az);
+        s_slot[0][cnt >> 6][c] = (uint32_t)(ax * SX + ay * SY + az + 1) | ((uint32_t)same << 9) |
+                                 ((uint32_t)self << 15) | ((uint32_t)quirk << 21);
+        s_slot[1][cnt >> 6][c] = (uint32_t)ax | ((uint32_t)ay << 4) | ((uint32_t)az << 8) | ((uint32_t)d << 12);
+      }
+      cnt++;
+    }
+  }
   __syncthreads();
   if (threadIdx.x == 0)
     for (int i = 1; i < nseg; i++) s_end[i] += s_end[i - 1];
   __syncthreads();
   const long long total = s_end[nseg - 1];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int oA;
-  {
-    int x, y, z;
-    local_xyz(2 * lane, x, y, z);
-    oA = (x + 1) * SX + (y + 1) * SY + (z + 1) + 1;
-  }
-  // the lanes' apron slots, the same for every warp: in shared memory
-  __shared__ uint32_t s_slot[2][5][32];
-  if (w == 0) {
-    AdvSlots S;
-    apron_slots<SX, SY>(lane, S);
-#pragma unroll
-    for (int r = 0; r < 5; r++) {
-      s_slot[0][r][lane] = r < S.n ? S.pk[r] : 0xFFFFFFFFu;
-      s_slot[1][r][lane] = S.ga[r];
-    }
-  }
-  __syncthreads();
+  const int k = threadIdx.x >> 6, c = threadIdx.x & 63, lane = threadIdx.x & 31;
+  int oC, lx, ly, lz;
+  local_xyz(c, lx, ly, lz);
+  oC = (lx + 1) * SX + (ly + 1) * SY + (lz + 1) + 1;
   const unsigned full = 0xffffffffu;
+  auto pair_sync = [&]() { asm volatile("bar.sync %0, 64;" ::"r"(1 + k) : "memory"); };
   int seg = 0;
-  for (long long t = (long long)blockIdx.x * W + w; t < total; t += (long long)gridDim.x * W) {
+  for (long long t = (long long)blockIdx.x * NBK + k; t < total; t += (long long)gridDim.x * NBK) {
     while (t >= s_end[seg]) seg++;
     const Dev &D = P.d[seg / MAXL];
     const int l = seg % MAXL;
     const uint32_t b = (uint32_t)(D.g.off[l] + (t - (seg ? s_end[seg - 1] : 0)));
     const int4 bp = D.pos[b];
     const size_t own = (size_t)b * BV;
-    const uint32_t e = lane < 27 ? D.nbr[27u * b + lane] : OUT;
+    const size_t cell = own + c;
+    const uint32_t e = lane < 27 ? D.nbr[27u * b + lane] : OUT;   // each warp keeps a copy
     const uint32_t ch = lane < 8 ? D.child[8u * b + lane] : NONE;  // the block's subblock children
-    float *Wt = s_tile[w][0];
-    float2 qa = make_float2(0.f, 0.f), qb = qa;  // own density / temperature pairs (buoyancy)
-    if (STAGE == 0 && (D.ph.buoy_a != 0.f || D.ph.buoy_b != 0.f)) {
-      qa = make_float2(q_ld(D, 0, own + 2 * lane), q_ld(D, 0, own + 2 * lane + 1));
-      if (D.g.nq > 1) qb = make_float2(q_ld(D, 1, own + 2 * lane), q_ld(D, 1, own + 2 * lane + 1));
-    }
-    // own cells
-    const float2 wo = reinterpret_cast<const float2 *>(D.w + own)[lane];
-    *reinterpret_cast<float2 *>(Wt + oA) = wo;
-    const float2 va = reinterpret_cast<const float2 *>(D.v[0] + own)[lane];
-    const float2 vb = reinterpret_cast<const float2 *>(D.v[1] + own)[lane];
-    const float2 vc = reinterpret_cast<const float2 *>(D.v[2] + own)[lane];
+    float *Wt = s_tile[k][0];
+    const float wo = D.w[cell];
+    const float va = D.v[0][cell], vb = D.v[1][cell], vc = D.v[2][cell];
+    Wt[oC] = wo;
+    float qa = 0.f, qb = 0.f;  // own density / temperature (buoyancy)
     if constexpr (STAGE == 0) {
-      *reinterpret_cast<float2 *>(s_tile[w][1] + oA) = va;
-      *reinterpret_cast<float2 *>(s_tile[w][2] + oA) = vb;
-      *reinterpret_cast<float2 *>(s_tile[w][3] + oA) = vc;
+      s_tile[k][1][oC] = va;
+      s_tile[k][2][oC] = vb;
+      s_tile[k][3][oC] = vc;
+      if (D.ph.buoy_a != 0.f || D.ph.buoy_b != 0.f) {
+        qa = q_ld(D, 0, cell);
+        if (D.g.nq > 1) qb = q_ld(D, 1, cell);
+      }
     } else {
 #pragma unroll
-      for (int kq = 0; kq < NQ; kq++) {
-        float2 q2;
-        if (MODE == 0) {
-          q2 = reinterpret_cast<const float2 *>(D.q[kq] + own)[lane];
-        } else {
-          const uint32_t u = reinterpret_cast<const uint32_t *>(D.qh[kq] + own)[lane];
-          q2 = make_float2(h16_to_f((uint16_t)(u & 0xFFFFu), MODE), h16_to_f((uint16_t)(u >> 16), MODE));
-        }
-        *reinterpret_cast<float2 *>(s_tile[w][1 + kq] + oA) = q2;
-      }
+      for (int kq = 0; kq < NQ; kq++) s_tile[k][1 + kq][oC] = q_ldm<MODE>(D, kq, cell);
     }
-    // apron cells
 #pragma unroll
-    for (int r = 0; r < 5; r++) {
-      const uint32_t pk = s_slot[0][r][lane], ga = s_slot[1][r][lane];
+    for (int r = 0; r < 3; r++) {
+      const uint32_t pk = s_slot[0][r][c], ga = s_slot[1][r][c];
       const uint32_t ed = __shfl_sync(full, e, (int)((ga >> 12) & 31u));
-      if (pk != 0xFFFFFFFFu) {
-        const size_t c = halo_cell(D, b, bp, ed, pk, ga);
+      if (pk != ~0u) {
+        const size_t ac = halo_cell(D, b, bp, ed, pk, ga);
         const uint32_t at = pk & 511u;
-        Wt[at] = D.w[c];
+        Wt[at] = D.w[ac];
         if constexpr (STAGE == 0) {
-          s_tile[w][1][at] = D.v[0][c];
-          s_tile[w][2][at] = D.v[1][c];
-          s_tile[w][3][at] = D.v[2][c];
+          s_tile[k][1][at] = D.v[0][ac];
+          s_tile[k][2][at] = D.v[1][ac];
+          s_tile[k][3][at] = D.v[2][ac];
         } else {
 #pragma unroll
-          for (int kq = 0; kq < NQ; kq++) s_tile[w][1 + kq][at] = q_ldm<MODE>(D, kq, c);
+          for (int kq = 0; kq < NQ; kq++) s_tile[k][1 + kq][at] = q_ldm<MODE>(D, kq, ac);
         }
       }
     }
-    __syncwarp();
-    const bool leaf = __shfl_sync(full, ch, lane >> 2) == NONE;
-#pragma unroll 1
-    for (int h = 0; h < 2; h++) {
-      const int c = 2 * lane + h;
-      const size_t cell = own + c;
-      float px = 0.f, py = 0.f, pz = 0.f;
-      bool fast = false;
-      int sub = 0;
-      if (leaf) {
-        int lx, ly, lz;
-        local_xyz(c, lx, ly, lz);
-        const float scale = (float)(1 << bp.w);
-        const float alpha = D.ph.dt * D.ph.rdx;
-        px = ((float)(bp.x + lx) + 0.5f) * scale - (h ? va.y : va.x) * alpha;
-        py = ((float)(bp.y + ly) + 0.5f) * scale - (h ? vb.y : vb.x) * alpha;
-        pz = ((float)(bp.z + lz) + 0.5f) * scale - (h ? vc.y : vc.x) * alpha;
-        fast = sample_in_own(D, bp, px, py, pz, sub);
-      }
-      // the sample's subblock must have no child (else sample_at descends)
-      const bool sub_leaf = __shfl_sync(full, ch, sub) == NONE;
-      fast = fast && (bp.w == 0 || sub_leaf);
-      if constexpr (STAGE == 0) {
-        if (leaf && !fast) {
-          advect_velocity_cell_ool(D, b, c);
-          continue;
-        }
+    pair_sync();
+    const bool leaf = __shfl_sync(full, ch, c >> 3) == NONE;
+    float px = 0.f, py = 0.f, pz = 0.f;
+    bool fast = false;
+    int sub = 0;
+    if (leaf) {
+      const float scale = (float)(1 << bp.w);
+      const float alpha = D.ph.dt * D.ph.rdx;
+      px = ((float)(bp.x + lx) + 0.5f) * scale - va * alpha;
+      py = ((float)(bp.y + ly) + 0.5f) * scale - vb * alpha;
+      pz = ((float)(bp.z + lz) + 0.5f) * scale - vc * alpha;
+      fast = sample_in_own(D, bp, px, py, pz, sub);
+    }
+    // the sample's subblock must have no child (else sample_at descends)
+    const bool sub_leaf = __shfl_sync(full, ch, sub) == NONE;
+    fast = fast && (bp.w == 0 || sub_leaf);
+    if constexpr (STAGE == 0) {
+      if (leaf && !fast) {
+        advect_velocity_cell_ool(D, b, c);
+      } else {
         float o0 = 0.f, o1 = 0.f, o2 = 0.f;
         if (leaf) {
           SmpT s;
@@ -1591,34 +1557,34 @@ __global__ void __launch_bounds__(256, DCG_ADV_MINB) k_advect_staged(const __gri
           if (!(s.wAcc < 1e-6f)) {
             const bool inside = box_inside_t(D.g, s);
 #pragma unroll
-            for (int k = 0; k < 8; k++) {
-              const int o = s.base + tile_delta<SX, SY>(k);
-              float vx = s_tile[w][1][o], vy = s_tile[w][2][o], vz = s_tile[w][3][o];
+            for (int kk = 0; kk < 8; kk++) {
+              const int o = s.base + tile_delta<SX, SY>(kk);
+              float vx = s_tile[k][1][o], vy = s_tile[k][2][o], vz = s_tile[k][3][o];
               if (!inside) {
-                const int x = (k & 4) ? s.x1 : s.x0, y = (k & 2) ? s.y1 : s.y0, z = (k & 1) ? s.z1 : s.z0;
+                const int x = (kk & 4) ? s.x1 : s.x0, y = (kk & 2) ? s.y1 : s.y0, z = (kk & 1) ? s.z1 : s.z0;
                 vel_bc(D.g, D.ph, vx, vy, vz, x, y, z, s.scale);
               }
-              if (k == 0) {
+              if (kk == 0) {
                 o0 = vx * s.wt[0]; o1 = vy * s.wt[0]; o2 = vz * s.wt[0];
               } else {
-                o0 = o0 + vx * s.wt[k]; o1 = o1 + vy * s.wt[k]; o2 = o2 + vz * s.wt[k];
+                o0 = o0 + vx * s.wt[kk]; o1 = o1 + vy * s.wt[kk]; o2 = o2 + vz * s.wt[kk];
               }
             }
           }
           if (D.ph.buoy_a != 0.f || D.ph.buoy_b != 0.f) {
-            float f = -D.ph.buoy_a * (h ? qa.y : qa.x);
-            if (D.g.nq > 1) f = f + D.ph.buoy_b * ((h ? qb.y : qb.x) - D.ph.t_amb);
+            float f = -D.ph.buoy_a * qa;
+            if (D.g.nq > 1) f = f + D.ph.buoy_b * (qb - D.ph.t_amb);
             o1 = o1 + D.ph.dt * f;
           }
         }
         D.tv[0][cell] = o0;
         D.tv[1][cell] = o1;
         D.tv[2][cell] = o2;
+      }
+    } else {
+      if (leaf && !fast) {
+        advect_scalars_cell_ool<MODE, NQ>(D, b, c);
       } else {
-        if (leaf && !fast) {
-          advect_scalars_cell_ool<MODE, NQ>(D, b, c);
-          continue;
-        }
         float o[NQ];
 #pragma unroll
         for (int kq = 0; kq < NQ; kq++) o[kq] = 0.f;
@@ -1628,19 +1594,17 @@ __global__ void __launch_bounds__(256, DCG_ADV_MINB) k_advect_staged(const __gri
           if (!(s.wAcc < 1e-6f)) {
             const bool inside = box_inside_t(D.g, s);
 #pragma unroll
-            for (int k = 0; k < 8; k++) {
-              const int x = (k & 4) ? s.x1 : s.x0, y = (k & 2) ? s.y1 : s.y0, z = (k & 1) ? s.z1 : s.z0;
+            for (int kk = 0; kk < 8; kk++) {
+              const int x = (kk & 4) ? s.x1 : s.x0, y = (kk & 2) ? s.y1 : s.y0, z = (kk & 1) ? s.z1 : s.z0;
               const int mode = inside ? 0 : q_bc_mode(D.g, D.ph, x, y, z, s.scale);
 #pragma unroll
               for (int kq = 0; kq < NQ; kq++) {
-                const float qc = mode == 0 ? s_tile[w][1 + kq][s.base + tile_delta<SX, SY>(k)]
+                const float qc = mode == 0 ? s_tile[k][1 + kq][s.base + tile_delta<SX, SY>(kk)]
                                            : (mode == 1 && kq == 0 ? D.ph.d_emit : 0.f);
-                o[kq] = (k == 0) ? qc * s.wt[0] : o[kq] + qc * s.wt[k];
+                o[kq] = (kk == 0) ? qc * s.wt[0] : o[kq] + qc * s.wt[kk];
               }
             }
           }
-          int lx, ly, lz;
-          local_xyz(c, lx, ly, lz);
           if (D.ph.em_n > 0)
             o[0] = o[0] + D.ph.dt * emission_at(D.g, D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w);
           if (D.ph.src) {
@@ -1653,7 +1617,7 @@ __global__ void __launch_bounds__(256, DCG_ADV_MINB) k_advect_staged(const __gri
         for (int kq = 0; kq < NQ; kq++) tq_stm<MODE>(D, kq, cell, o[kq]);
       }
     }
-    __syncwarp();
+    pair_sync();  // the tiles are refilled for the next block
   }
 }
 template <int STAGE, int MODE, int NQ> static unsigned advect_grid() {
