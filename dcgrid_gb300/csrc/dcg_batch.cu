@@ -75,6 +75,8 @@ struct dcg_batch {
   int groups() const { return (n() + BMAX - 1) / BMAX; }
 
   int set_solve_config() {
+    if (tune.solve_barrier < 0 || tune.solve_barrier > 3)
+      return fail(DCG_E_INVALID, "solve_barrier must be 0..3 (bit 0 two-level barrier, bit 1 coarsest-aligned rounds)");
     if (!solve_variant_valid(tune.solve_cache))
       return fail(DCG_E_INVALID, "solve_cache must be 0, 3, 4, 8 or a pipelined variant 16, 18, 19, 32, 34, 35");
     for (int k = 0; k < 4; k++)
@@ -139,13 +141,15 @@ struct dcg_batch {
         solve_round(round, batch_solve_grid(sms, tune.round_cache[round], tune.round_ctas_per_sm[round]),
                     tune.round_cache[round], tune.round_barrier[round]);
       else
-        solve_round(round, solve_grid, tune.solve_cache, tune.solve_barrier);
+        solve_round(round, solve_grid, tune.solve_cache, tune.solve_barrier & 1);
     }
   }
   void solve(int grid, int cache, int tree) {
     for (int round = 0; round <= maxtop; round++) solve_round(round, grid, cache, tree);
   }
+  // tree: two-level barrier; the round alignment comes from tune.solve_barrier's bit 1
   void solve_round(int round, int grid, int cache, int tree) {
+    tree = (tree & 1) | (tune.solve_barrier & 2);
     {
       for (int g = 0; g < groups(); g++) {
         SolveBatch P{};
@@ -162,7 +166,7 @@ struct dcg_batch {
           P.d[i] = m[g * BMAX + i]->D;
           P.arena[i] = arena_off[g * BMAX + i];
         }
-        launch_level_solve_batch(P, round, iters, grid, cache, tree, stream);
+        launch_level_solve_batch(P, round, iters, grid, cache, tree, stream);  // bit 1: alignment
       }
     }
   }
@@ -335,17 +339,19 @@ struct dcg_batch {
     for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35}) {
       const int occ = batch_solve_grid(sms, cache, 0) / std::max(1, sms);
       for (int k = 1; k <= occ; k++)
-        for (int tree = 0; tree < 2; tree++) {
+        for (int tb = 0; tb < 4; tb++) {  // bit 0: two-level barrier; bit 1: coarsest-aligned rounds
+          tune.solve_barrier = tb;
           const int grid = batch_solve_grid(sms, cache, k);
-          const float ms = time_ms(reps, [&] { solve(grid, cache, tree); });
+          const float ms = time_ms(reps, [&] { solve(grid, cache, tb & 1); });
           if (ms < best_solve) {
             best_solve = ms;
             best.solve_cache = cache;
             best.solve_ctas_per_sm = k;
-            best.solve_barrier = tree;
+            best.solve_barrier = tb;
           }
         }
     }
+    tune.solve_barrier = best.solve_barrier;  // the per-round schedules below use its alignment
     // each round of the first four on its own: the best schedule if it beats
     // the whole-cascade choice for that round
     for (int r = 0; r < 4 && r <= maxtop; r++) {

@@ -859,7 +859,7 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
     kcount += left <= 0 ? 0 : (left >= W ? W : (int)left);
   }
   auto barrier = [&]() {
-    if (tree) grid_barrier_tree(P.bar, P.err, nctas);
+    if (tree & 1) grid_barrier_tree(P.bar, P.err, nctas);
     else grid_barrier(P.bar, P.err, nctas);
   };
   // per buffer: arena index of the block's first cell and alpha (bits); own = ~0u: no block
@@ -954,7 +954,7 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
 // One round of the batched cascade: level maxtop - round of every member that
 // has it, optional prolongation from the member's parent level, then `sweeps`
 // Jacobi sweeps over the concatenated cells of all members, separated by grid
-// barriers (tree != 0: two-level barrier). Member m's cells of the level
+// barriers (tree & 1: two-level barrier). Member m's cells of the level
 // occupy [s_end[m-1], s_end[m]) of the concatenated index. With CACHE > 0 and
 // at most CACHE cells per thread, each thread keeps, per cell, the six
 // neighbour cells and its own cell as arena indices plus alpha*div in dynamic
@@ -971,9 +971,11 @@ __global__ void __launch_bounds__(256, NB ? DCG_PIPE_MINB : DCG_SOLVE_MINB)
   const int t = threadIdx.x;
   if (t == 0) {
     long long acc = 0;
-    const int lev = P.maxtop - round;
     for (int m = 0; m < P.n; m++) {
       const Dev &D = P.d[m];
+      // rounds aligned at every member's finest level (round r: level maxtop - r)
+      // or, with tree & 2, at its coarsest (round r: level levels - 1 - r)
+      const int lev = (tree & 2) ? D.g.levels - 1 - round : P.maxtop - round;
       if (lev >= 0 && lev < D.g.levels) acc += __ldcg(D.load + lev) * 64;
       s_lev[m] = lev;
       s_end[m] = acc;
@@ -996,7 +998,7 @@ __global__ void __launch_bounds__(256, NB ? DCG_PIPE_MINB : DCG_SOLVE_MINB)
     }
   if (sweeps <= 0) return;
   auto barrier = [&]() {
-    if (tree) grid_barrier_tree(P.bar, P.err, nctas);
+    if (tree & 1) grid_barrier_tree(P.bar, P.err, nctas);
     else grid_barrier(P.bar, P.err, nctas);
   };
   barrier();

@@ -320,7 +320,10 @@ typedef struct {
                                 16 + c (c = 0, 2, 3): pipelined staged sweeps, asynchronous
                                 copies into two tile buffers per warp; 32 + c: three     */
   int32_t solve_ctas_per_sm; /* CTAs per SM of the cooperative solve (0 = occupancy limit) */
-  int32_t solve_barrier;     /* grid barrier between sweeps: 0 flat, 1 two-level            */
+  int32_t solve_barrier;     /* bit 0: grid barrier between sweeps, 0 flat, 1 two-level;
+                                bit 1: cascade round r solves every member's level
+                                levels-1-r (coarsest levels aligned) instead of level
+                                maxtop-r (finest levels aligned)                          */
   int32_t persistent;        /* cell stages as persistent kernels over the allocated blocks */
   /* per cascade round r < 4: its own schedule when round_ctas_per_sm[r] != 0
    * (CTAs per SM, or -k: one CTA per k SMs; cache depth; barrier), else the
