@@ -22,7 +22,7 @@ struct SortScratch {
 };
 long long sort_tiles(long long n);
 void launch_radix_sort(uint32_t *keys, uint32_t *vals, long long n, const SortScratch &s,
-                       const long long *active, cudaStream_t st);
+                       const long long *active, cudaStream_t st, const long long *ndev = nullptr, int nmul = 1);
 // many sorts in the same launches (at most SORT_SEGS segments, each with its own scratch)
 constexpr int SORT_SEGS = 32;
 struct SortSeg {
@@ -30,6 +30,11 @@ struct SortSeg {
   long long n;
   const long long *active;
   SortScratch s;
+  // optional: sort only the first min(n, nmul * *ndev) entries (a device-side
+  // count); callers use it where the entries after that prefix are already in
+  // their stable-sorted place (equal largest keys in index order) or unused
+  const long long *ndev;
+  int nmul;
 };
 void launch_radix_sort_batch(const SortSeg *seg, int nseg, cudaStream_t st);
 

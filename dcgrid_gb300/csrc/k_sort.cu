@@ -20,6 +20,12 @@ constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 long long sort_tiles(long long n) { return (n + RS_TILE - 1) / RS_TILE; }
 
 __device__ inline bool gate_off(const long long *active) { return active && *active == 0; }
+// entries to sort: n, or the device-side prefix min(n, nmul * *ndev)
+__device__ inline long long eff_n(long long n, const long long *ndev, int nmul) {
+  if (!ndev) return n;
+  const long long m = (long long)nmul * *ndev;
+  return m < n ? m : n;
+}
 
 __device__ __forceinline__ void rs_hist_body(const uint32_t *__restrict__ keys, long long n, int shift, uint32_t *__restrict__ hist, long long ntiles, const long long *active, unsigned bx, unsigned gx) {
   if (gate_off(active)) return;
@@ -34,7 +40,7 @@ __device__ __forceinline__ void rs_hist_body(const uint32_t *__restrict__ keys, 
   __syncthreads();
   hist[(long long)threadIdx.x * ntiles + bx] = h[threadIdx.x];
 }
-__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint32_t *__restrict__ keys, long long n, int shift, uint32_t *__restrict__ hist, long long ntiles, const long long *active) { rs_hist_body(keys, n, shift, hist, ntiles, active, blockIdx.x, gridDim.x); }
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint32_t *__restrict__ keys, long long n, int shift, uint32_t *__restrict__ hist, long long ntiles, const long long *active, const long long *ndev, int nmul) { rs_hist_body(keys, eff_n(n, ndev, nmul), shift, hist, ntiles, active, blockIdx.x, gridDim.x); }
 
 // Block-wide exclusive scan of one value per thread (256 threads); returns
 // the exclusive prefix and writes the block total to *total.
@@ -133,20 +139,20 @@ __device__ __forceinline__ void rs_scatter_body(const uint32_t *__restrict__ kin
     __syncthreads();
   }
 }
-__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, long long n, int shift, const uint32_t *__restrict__ hist, const uint32_t *__restrict__ totals, long long ntiles, const long long *active) { rs_scatter_body(kin, vin, kout, vout, n, shift, hist, totals, ntiles, active, blockIdx.x, gridDim.x); }
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, long long n, int shift, const uint32_t *__restrict__ hist, const uint32_t *__restrict__ totals, long long ntiles, const long long *active, const long long *ndev, int nmul) { rs_scatter_body(kin, vin, kout, vout, eff_n(n, ndev, nmul), shift, hist, totals, ntiles, active, blockIdx.x, gridDim.x); }
 
 void launch_radix_sort(uint32_t *keys, uint32_t *vals, long long n, const SortScratch &s,
-                       const long long *active, cudaStream_t st) {
+                       const long long *active, cudaStream_t st, const long long *ndev, int nmul) {
   if (n <= 0) return;
   const long long nt = sort_tiles(n);
   uint32_t *kin = keys, *vin = vals, *kout = s.k1, *vout = s.v1;
   for (int pass = 0; pass < 4; pass++) {
     const int shift = 8 * pass;
-    k_rs_hist<<<(unsigned)nt, RS_THREADS, 0, st>>>(kin, n, shift, s.hist, nt, active);
+    k_rs_hist<<<(unsigned)nt, RS_THREADS, 0, st>>>(kin, n, shift, s.hist, nt, active, ndev, nmul);
     k_rs_scan_cols<<<256, RS_THREADS, 0, st>>>(s.hist, nt, s.totals, active);
     k_rs_scan_totals<<<1, RS_THREADS, 0, st>>>(s.totals, active);
     k_rs_scatter<<<(unsigned)nt, RS_THREADS, 0, st>>>(kin, vin, kout, vout, n, shift, s.hist,
-                                                     s.totals, nt, active);
+                                                     s.totals, nt, active, ndev, nmul);
     uint32_t *tk = kin, *tv = vin;
     kin = kout; vin = vout;
     kout = tk; vout = tv;
@@ -164,6 +170,8 @@ struct SortBatchP {
   uint32_t *hist[SORT_SEGS], *totals[SORT_SEGS];
   const long long *active[SORT_SEGS];
   long long n[SORT_SEGS], nt[SORT_SEGS];
+  const long long *ndev[SORT_SEGS];
+  int nmul[SORT_SEGS];
 };
 
 template <int OP> __global__ void __launch_bounds__(RS_THREADS) k_rs_batch(const __grid_constant__ SortBatchP P) {
@@ -171,12 +179,13 @@ template <int OP> __global__ void __launch_bounds__(RS_THREADS) k_rs_batch(const
   while (s < P.nseg - 1 && blockIdx.x >= P.end[s]) s++;
   const long long first = s ? P.end[s - 1] : 0;
   const unsigned bx = (unsigned)(blockIdx.x - first), gx = (unsigned)(P.end[s] - first);
-  if constexpr (OP == 0) rs_hist_body(P.kin[s], P.n[s], P.shift, P.hist[s], P.nt[s], P.active[s], bx, gx);
+  if constexpr (OP == 0)
+    rs_hist_body(P.kin[s], eff_n(P.n[s], P.ndev[s], P.nmul[s]), P.shift, P.hist[s], P.nt[s], P.active[s], bx, gx);
   if constexpr (OP == 1) rs_scan_cols_body(P.hist[s], P.nt[s], P.totals[s], P.active[s], bx, gx);
   if constexpr (OP == 2) rs_scan_totals_body(P.totals[s], P.active[s], bx, gx);
   if constexpr (OP == 3)
-    rs_scatter_body(P.kin[s], P.vin[s], P.kout[s], P.vout[s], P.n[s], P.shift, P.hist[s], P.totals[s], P.nt[s],
-                    P.active[s], bx, gx);
+    rs_scatter_body(P.kin[s], P.vin[s], P.kout[s], P.vout[s], eff_n(P.n[s], P.ndev[s], P.nmul[s]), P.shift,
+                    P.hist[s], P.totals[s], P.nt[s], P.active[s], bx, gx);
 }
 
 void launch_radix_sort_batch(const SortSeg *seg, int nseg, cudaStream_t st) {
@@ -188,6 +197,8 @@ void launch_radix_sort_batch(const SortSeg *seg, int nseg, cudaStream_t st) {
     P.hist[i] = seg[i].s.hist;
     P.totals[i] = seg[i].s.totals;
     P.active[i] = seg[i].active;
+    P.ndev[i] = seg[i].ndev;
+    P.nmul[i] = seg[i].nmul;
     k[i] = seg[i].keys;
     v[i] = seg[i].vals;
     ko[i] = seg[i].s.k1;

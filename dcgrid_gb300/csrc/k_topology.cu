@@ -207,7 +207,10 @@ __global__ void k_move_setup(Dev D, int L) { move_setup_body(D, L, blockIdx.x, g
 
 // Sort keys: blocks ascending by score, negative scores last; subblocks
 // descending by score. The sort is stable over index-ordered input, so
-// equal keys stay in index order.
+// equal keys stay in index order. Only the allocated prefix of each range is
+// sorted (load[L] blocks, 8 load[L+1] subblocks): unallocated blocks score
+// -FLT_MAX, whose key is the largest one, so in the stable order they follow
+// every allocated entry in index order, where they already are.
 __device__ __forceinline__ void keys_blocks_body(const Dev &D, int L, uint32_t *keys, uint32_t *vals, unsigned bx, unsigned gx) {
   if (D.ctr[C_MOVE_LIMIT] == 0) return;
   const long long i = (long long)bx * blockDim.x + threadIdx.x;
@@ -601,9 +604,9 @@ void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *
     const long long d0 = D.g.budget[L], d1 = 8 * D.g.budget[L + 1];
     k_move_setup<<<1, 1, 0, st>>>(D, L);
     k_keys_blocks<<<grid_for(d0), 256, 0, st>>>(D, L, keys, vals);
-    launch_radix_sort(keys, vals, d0, s, D.ctr + C_MOVE_LIMIT, st);
+    launch_radix_sort(keys, vals, d0, s, D.ctr + C_MOVE_LIMIT, st, D.load + L, 1);
     k_keys_dests<<<grid_for(d1), 256, 0, st>>>(D, L, keys2, vals2);
-    launch_radix_sort(keys2, vals2, d1, s, D.ctr + C_MOVE_LIMIT, st);
+    launch_radix_sort(keys2, vals2, d1, s, D.ctr + C_MOVE_LIMIT, st, D.load + L + 1, 8);
     k_match<<<gs, 256, 0, st>>>(D, vals, vals2);
     k_commit_moves<<<gs, 256, 0, st>>>(D, L, vals, vals2);
   }
@@ -622,7 +625,7 @@ void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *
       k_record_refines<<<gs, 256, 0, st>>>(D, L, vals, 1);
     } else {
       k_keys_cands<<<gs, 256, 0, st>>>(D, vals, keys, vals2, n8);
-      launch_radix_sort(keys, vals2, n8, s, D.ctr + C_MOVE_LIMIT, st);
+      launch_radix_sort(keys, vals2, n8, s, D.ctr + C_MOVE_LIMIT, st, D.ctr + C_NCAND, 1);
       cudaMemsetAsync(sel, 0, (size_t)8 * D.g.B, st);
       k_mark_selected<<<gs, 256, 0, st>>>(D, vals2, sel);
       k_cmp_count<<<(unsigned)nt, 256, 0, st>>>(D, L, sel, s.tile_sums);
@@ -933,8 +936,10 @@ struct AdaptLauncher {
       for (int i = 0; i < n; i++) {
         if (!has(i)) continue;
         const long long *act = m[i].D.ctr + C_MOVE_LIMIT;
-        seg[ns++] = SortSeg{m[i].keys, m[i].vals, m[i].D.g.budget[L], act, m[i].S2};
-        seg[ns++] = SortSeg{m[i].keys2, m[i].vals2, 8 * m[i].D.g.budget[L + 1], act, m[i].S};
+        // allocated prefixes only: the unallocated tails already sit in their
+        // stable-sorted place (largest keys, index order)
+        seg[ns++] = SortSeg{m[i].keys, m[i].vals, m[i].D.g.budget[L], act, m[i].S2, m[i].D.load + L, 1};
+        seg[ns++] = SortSeg{m[i].keys2, m[i].vals2, 8 * m[i].D.g.budget[L + 1], act, m[i].S, m[i].D.load + L + 1, 8};
       }
       launch_radix_sort_batch(seg, ns, st);
       for (int i = 0; i < n; i++) {
@@ -978,7 +983,8 @@ struct AdaptLauncher {
       int ns = 0;
       for (int i = 0; i < n; i++)
         if (score[i])
-          seg[ns++] = SortSeg{m[i].keys, m[i].vals2, 8 * m[i].D.g.budget[L], m[i].D.ctr + C_MOVE_LIMIT, m[i].S};
+          seg[ns++] = SortSeg{m[i].keys, m[i].vals2, 8 * m[i].D.g.budget[L], m[i].D.ctr + C_MOVE_LIMIT, m[i].S,
+                              m[i].D.ctr + C_NCAND, 1};  // the compacted candidates only
       launch_radix_sort_batch(seg, ns, st);
       for (int i = 0; i < n; i++) {
         P.p0[i] = m[i].keys2;
