@@ -805,6 +805,13 @@ __device__ __forceinline__ void cp_async8(void *dst, const void *src) {
                "l"(src)
                : "memory");
 }
+// the same with a 32-bit shared-memory address
+__device__ __forceinline__ void cp_async4s(uint32_t dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8s(uint32_t dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
@@ -864,9 +871,18 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
   };
   // per buffer: arena index of the block's first cell and alpha (bits); own = ~0u: no block
   uint32_t b_own[NB], b_alpha[NB];
+  // shared-memory addresses of the lane's copy targets in buffer 0 (buffer b: + b * TILE * 4)
+  const uint32_t s_own = (uint32_t)__cvta_generic_to_shared(&s_pt[w][0][oA]);
+  uint32_t s_halo[3];
+#pragma unroll
+  for (int q = 0; q < 3; q++) s_halo[q] = (uint32_t)__cvta_generic_to_shared(&s_pt[w][0][hpk[q] & 511u]);
+  const uint32_t s_div = (uint32_t)__cvta_generic_to_shared(&s_pd[w][0][2 * lane]);
+  const float *divl = P.div + 2 * lane;
   for (int it = 0; it < sweeps; it++) {
     const float *src = (it & 1) ? P.pt : P.p;
     float *dst = (it & 1) ? P.p : P.pt;
+    const float *srcl = src + 2 * lane;
+    float2 *dstl = reinterpret_cast<float2 *>(dst) + lane;
     if (t == 0) s_next[(it + 1) & 1] = 0u;  // the next sweep's counter; its last use ended before the barrier
     unsigned *cnt = &s_next[it & 1];
     auto issue = [&](int buf) {
@@ -874,10 +890,15 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
       if (lane == 0) kk = atomicAdd(cnt, 1u);
       const int k = (int)__shfl_sync(full, kk, 0);
       const bool act = k < kcount;  // warp-uniform; a warp's claims only grow
-      const long long gb = ((long long)(k >> 3) * nctas + blockIdx.x) * W + (k & 7);
       uint32_t biw = 0;
-      if (act && lane < BI_WORDS)
-        biw = cached ? s_cache[k * BI_WORDS + lane] : __ldcg(P.binfo + gb * BI_WORDS + lane);
+      if (act && lane < BI_WORDS) {
+        if (cached) {
+          biw = s_cache[k * BI_WORDS + lane];
+        } else {
+          const long long gb = ((long long)(k >> 3) * nctas + blockIdx.x) * W + (k & 7);
+          biw = __ldcg(P.binfo + gb * BI_WORDS + lane);
+        }
+      }
       const uint32_t own = __shfl_sync(full, biw, 0);
       const uint32_t alpha = __shfl_sync(full, biw, 1);
       const uint32_t c11 = __shfl_sync(full, biw, 11), c12 = __shfl_sync(full, biw, 12);
@@ -908,11 +929,11 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
       b_own[buf] = act ? own : ~0u;
       b_alpha[buf] = alpha;
       if (act) {
-        float *T = s_pt[w][buf];
-        cp_async8(T + oA, src + own + 2 * lane);
+        const uint32_t bo = (uint32_t)(buf * TILE * 4);
+        cp_async8s(s_own + bo, srcl + own);
 #pragma unroll
-        for (int q = 0; q < 3; q++) cp_async4(T + (hpk[q] & 511u), src + addr[q]);
-        cp_async8(s_pd[w][buf] + 2 * lane, P.div + own + 2 * lane);
+        for (int q = 0; q < 3; q++) cp_async4s(s_halo[q] + bo, src + addr[q]);
+        cp_async8s(s_div + (uint32_t)(buf * 64 * 4), divl + own);
       }
       cp_async_commit();
     };
@@ -942,7 +963,7 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
         float2 res;
         res.x = div6(L.x + R.x + Dn.x + Up.x + Bk + ab.y - adA);
         res.y = div6(L.y + R.y + Dn.y + Up.y + ab.x + Fw - adB);
-        reinterpret_cast<float2 *>(dst + own)[lane] = res;
+        dstl[own >> 1] = res;
       }
       __syncwarp();  // buffer `buf` may be refilled by the next issue
     }
