@@ -97,7 +97,8 @@ struct StatRecord {
 void launch_stats_zero(const CellBatch &P, cudaStream_t st);
 void launch_stats_gather(const CellBatch &P, StatRecord *dst, cudaStream_t st);
 // CTAs of the batched solve for a variant (cache depth 0, 3, 4, 8; 16, 18, 19: pipelined
-// staged sweeps with two tile buffers and cache depth 0, 2, 3; 32, 34, 35: three buffers)
+// staged sweeps with two tile buffers and cache depth 0, 2, 3; 32, 34, 35: three buffers;
+// 64, 66: two buffers, registers for 5 CTAs per SM)
 // and CTAs per SM (0 = occupancy limit)
 int batch_solve_grid(int sms, int cache, int ctas_per_sm);
 bool solve_variant_valid(int cache);

@@ -983,8 +983,8 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
 // store per cell. Larger levels are swept one block per warp through a 6^3
 // shared-memory tile holding the block and its face halo. Arithmetic is that
 // of k_jacobi (identical results).
-template <int CACHE, int NB = 0>
-__global__ void __launch_bounds__(256, NB ? DCG_PIPE_MINB : DCG_SOLVE_MINB)
+template <int CACHE, int NB = 0, int MB = DCG_PIPE_MINB>
+__global__ void __launch_bounds__(256, NB ? MB : DCG_SOLVE_MINB)
     k_level_solve_batch(const __grid_constant__ SolveBatch P, int round, int sweeps, int tree) {
   __shared__ long long s_end[BMAX];
   __shared__ int s_lev[BMAX];
@@ -1769,21 +1769,22 @@ void launch_restrict_batch(RestrictBatch &P, cudaStream_t st) {
   if (acc > 0) k_restrict_batch<<<(unsigned)acc, 256, 0, st>>>(P);
 }
 
-template <int C, int NB>
+template <int C, int NB, int MB = DCG_PIPE_MINB>
 static int solve_batch_occupancy() {
   // static + dynamic shared memory above 48 KB needs the opt-in
   const int smem = C * 8 * 256 * 4;
-  if (smem > 0 && cudaFuncSetAttribute(k_level_solve_batch<C, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       smem) != cudaSuccess)
+  if (smem > 0 && cudaFuncSetAttribute(k_level_solve_batch<C, NB, MB>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
     return 0;
   int a = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_level_solve_batch<C, NB>, 256, smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_level_solve_batch<C, NB, MB>, 256, smem) != cudaSuccess)
     return 0;
   return a;
 }
 // solve variants: cache depth 0, 3, 4 or 8 (cells per thread of the small-level
-// path; 8 KB of dynamic shared memory each); + SOLVE_PIPE (16): pipelined
-// staged sweeps with two tile buffers per warp, + 2 * SOLVE_PIPE: three
+// path; 8 KB of dynamic shared memory each); 16 + c: pipelined staged sweeps
+// with two tile buffers per warp (registers for 4 CTAs per SM), 32 + c: three
+// buffers, 64 + c: two buffers with registers for 5 CTAs per SM
 static int solve_occupancy(int cache) {
   switch (cache) {
     case 8: return solve_batch_occupancy<8, 0>();
@@ -1796,12 +1797,14 @@ static int solve_occupancy(int cache) {
     case 16 + 3: return solve_batch_occupancy<3, 2>();
     case 32 + 2: return solve_batch_occupancy<2, 3>();
     case 32 + 3: return solve_batch_occupancy<3, 3>();
+    case 64: return solve_batch_occupancy<0, 2, 5>();
+    case 64 + 2: return solve_batch_occupancy<2, 2, 5>();
     default: return 0;
   }
 }
 bool solve_variant_valid(int cache) {
   return cache == 0 || cache == 3 || cache == 4 || cache == 8 || cache == 16 || cache == 18 || cache == 19 ||
-         cache == 32 || cache == 34 || cache == 35;
+         cache == 32 || cache == 34 || cache == 35 || cache == 64 || cache == 66;
 }
 int batch_solve_grid(int sms, int cache, int ctas_per_sm) {
   const int occ = solve_occupancy(cache);
@@ -1833,6 +1836,8 @@ void launch_level_solve_batch(const SolveBatch &P, int round, int sweeps, int gr
     case 19: cudaLaunchKernelEx(&cfg, k_level_solve_batch<3, 2>, P, round, sweeps, tree); break;
     case 34: cudaLaunchKernelEx(&cfg, k_level_solve_batch<2, 3>, P, round, sweeps, tree); break;
     case 35: cudaLaunchKernelEx(&cfg, k_level_solve_batch<3, 3>, P, round, sweeps, tree); break;
+    case 64: cudaLaunchKernelEx(&cfg, k_level_solve_batch<0, 2, 5>, P, round, sweeps, tree); break;
+    case 66: cudaLaunchKernelEx(&cfg, k_level_solve_batch<2, 2, 5>, P, round, sweeps, tree); break;
     default: cudaLaunchKernelEx(&cfg, k_level_solve_batch<0, 0>, P, round, sweeps, tree); break;
   }
 }
