@@ -38,6 +38,7 @@ enum : int {
   C_MOVE_LIMIT = 3,   // scratch: limit l of the level being matched
   C_MATCHES = 4,      // scratch: first failing pair of the level being matched
   C_NCAND = 5,        // scratch: candidate count of a compaction
+  C_SELECT = 6,       // scratch: 1 when a level's refinement candidates outnumber its limit
   C_MOVE_BEGIN = 16,  // [16 + L]: first move of level L
   C_MOVE_END = 32,    // [32 + L]
   C_REF_BEGIN = 48,   // [48 + L]: first refinement creating blocks of level L

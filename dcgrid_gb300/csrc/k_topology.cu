@@ -345,6 +345,7 @@ __device__ __forceinline__ void refine_setup_body(const Dev &D, int L, unsigned 
   D.ctr[C_REF_END + L - 1] = D.ctr[C_REFINES];
   D.ctr[C_LOAD0 + L - 1] = D.load[L - 1];
   D.ctr[C_NCAND] = 0;
+  D.ctr[C_SELECT] = 0;
 }
 __global__ void k_refine_setup(Dev D, int L) { refine_setup_body(D, L, blockIdx.x, gridDim.x); }
 
@@ -357,7 +358,7 @@ __device__ inline bool cand_flag(const Dev &D, int L, long long i, const uint8_t
   return D.ss[8 * D.g.off[L] + i] > D.ph.refine_threshold;
 }
 __device__ __forceinline__ void cmp_count_body(const Dev &D, int L, const uint8_t *sel, uint32_t *tile_sums, unsigned bx, unsigned gx) {
-  if (D.ctr[C_MOVE_LIMIT] == 0) return;
+  if (D.ctr[C_MOVE_LIMIT] == 0 || (sel && D.ctr[C_SELECT] == 0)) return;
   const long long n = 8 * D.g.budget[L];
   const long long base = (long long)bx * CMP_TILE;
   int cnt = 0;
@@ -376,8 +377,11 @@ __device__ __forceinline__ void cmp_count_body(const Dev &D, int L, const uint8_
   }
 }
 __global__ void __launch_bounds__(256) k_cmp_count(Dev D, int L, const uint8_t *sel, uint32_t *tile_sums) { cmp_count_body(D, L, sel, tile_sums, blockIdx.x, gridDim.x); }
-__device__ __forceinline__ void cmp_scan_body(const Dev &D, uint32_t *tile_sums, long long ntiles, unsigned bx, unsigned gx) {
-  if (D.ctr[C_MOVE_LIMIT] == 0) return;
+// first: the threshold compaction, which also decides whether the
+// score-ordered selection is needed (C_SELECT); else the selection's
+// compaction, which runs only then
+__device__ __forceinline__ void cmp_scan_body(const Dev &D, uint32_t *tile_sums, long long ntiles, int first, unsigned bx, unsigned gx) {
+  if (D.ctr[C_MOVE_LIMIT] == 0 || (!first && D.ctr[C_SELECT] == 0)) return;
   __shared__ uint32_t ws[32];
   __shared__ uint32_t carry_s;
   if (threadIdx.x == 0) carry_s = 0;
@@ -409,11 +413,15 @@ __device__ __forceinline__ void cmp_scan_body(const Dev &D, uint32_t *tile_sums,
     if (threadIdx.x == 0) carry_s = carry + ws[31];
     __syncthreads();
   }
-  if (threadIdx.x == 0) D.ctr[C_NCAND] = carry_s;
+  if (threadIdx.x == 0) {
+    D.ctr[C_NCAND] = carry_s;
+    // more candidates than the limit: only then does their score order matter
+    if (first) D.ctr[C_SELECT] = (long long)carry_s > D.ctr[C_MOVE_LIMIT] ? 1 : 0;
+  }
 }
-__global__ void __launch_bounds__(1024) k_cmp_scan(Dev D, uint32_t *tile_sums, long long ntiles) { cmp_scan_body(D, tile_sums, ntiles, blockIdx.x, gridDim.x); }
+__global__ void __launch_bounds__(1024) k_cmp_scan(Dev D, uint32_t *tile_sums, long long ntiles, int first) { cmp_scan_body(D, tile_sums, ntiles, first, blockIdx.x, gridDim.x); }
 __device__ __forceinline__ void cmp_scatter_body(const Dev &D, int L, const uint8_t *sel, const uint32_t *tile_sums, uint32_t *out, unsigned bx, unsigned gx) {
-  if (D.ctr[C_MOVE_LIMIT] == 0) return;
+  if (D.ctr[C_MOVE_LIMIT] == 0 || (sel && D.ctr[C_SELECT] == 0)) return;
   __shared__ uint32_t ws[8];
   __shared__ uint32_t run_s;
   const long long n = 8 * D.g.budget[L];
@@ -442,6 +450,7 @@ __device__ __forceinline__ void cmp_scatter_body(const Dev &D, int L, const uint
 __global__ void __launch_bounds__(256) k_cmp_scatter(Dev D, int L, const uint8_t *sel, const uint32_t *tile_sums, uint32_t *out) { cmp_scatter_body(D, L, sel, tile_sums, out, blockIdx.x, gridDim.x); }
 // Score-ordered selection (ref_compat off): keys of the compacted candidates.
 __device__ __forceinline__ void keys_cands_body(const Dev &D, const uint32_t *cand, uint32_t *keys, uint32_t *vals, long long nmax, unsigned bx, unsigned gx) {
+  if (D.ctr[C_SELECT] == 0) return;  // every candidate is kept: no selection
   const long long n = D.ctr[C_NCAND];
   for (long long i = (long long)bx * blockDim.x + threadIdx.x; i < nmax; i += (long long)gx * blockDim.x) {
     if (i < n) {
@@ -458,7 +467,7 @@ __device__ __forceinline__ void keys_cands_body(const Dev &D, const uint32_t *ca
 }
 __global__ void __launch_bounds__(256) k_keys_cands(Dev D, const uint32_t *cand, uint32_t *keys, uint32_t *vals, long long nmax) { keys_cands_body(D, cand, keys, vals, nmax, blockIdx.x, gridDim.x); }
 __device__ __forceinline__ void mark_selected_body(const Dev &D, const uint32_t *sorted, uint8_t *sel, unsigned bx, unsigned gx) {
-  if (D.ctr[C_MOVE_LIMIT] == 0) return;
+  if (D.ctr[C_MOVE_LIMIT] == 0 || D.ctr[C_SELECT] == 0) return;
   const long long n = D.ctr[C_NCAND], limit = D.ctr[C_MOVE_LIMIT];
   const long long keep = n < limit ? n : limit;
   for (long long i = (long long)bx * blockDim.x + threadIdx.x; i < keep; i += (long long)gx * blockDim.x)
@@ -619,17 +628,17 @@ void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *
     const long long nt = (n8 + CMP_TILE - 1) / CMP_TILE;
     k_refine_setup<<<1, 1, 0, st>>>(D, L);
     k_cmp_count<<<(unsigned)nt, 256, 0, st>>>(D, L, nullptr, s.tile_sums);
-    k_cmp_scan<<<1, 1024, 0, st>>>(D, s.tile_sums, nt);
+    k_cmp_scan<<<1, 1024, 0, st>>>(D, s.tile_sums, nt, 1);
     k_cmp_scatter<<<(unsigned)nt, 256, 0, st>>>(D, L, nullptr, s.tile_sums, vals);
     if (D.g.ref_compat) {
       k_record_refines<<<gs, 256, 0, st>>>(D, L, vals, 1);
     } else {
       k_keys_cands<<<gs, 256, 0, st>>>(D, vals, keys, vals2, n8);
-      launch_radix_sort(keys, vals2, n8, s, D.ctr + C_MOVE_LIMIT, st, D.ctr + C_NCAND, 1);
+      launch_radix_sort(keys, vals2, n8, s, D.ctr + C_SELECT, st, D.ctr + C_NCAND, 1);
       cudaMemsetAsync(sel, 0, (size_t)8 * D.g.B, st);
       k_mark_selected<<<gs, 256, 0, st>>>(D, vals2, sel);
       k_cmp_count<<<(unsigned)nt, 256, 0, st>>>(D, L, sel, s.tile_sums);
-      k_cmp_scan<<<1, 1024, 0, st>>>(D, s.tile_sums, nt);
+      k_cmp_scan<<<1, 1024, 0, st>>>(D, s.tile_sums, nt, 0);
       k_cmp_scatter<<<(unsigned)nt, 256, 0, st>>>(D, L, sel, s.tile_sums, vals);
       k_record_refines<<<gs, 256, 0, st>>>(D, L, vals, 0);
     }
@@ -843,12 +852,13 @@ template <int OP, int T> __global__ void __launch_bounds__(T) k_adapt_batch(cons
   }
   if constexpr (OP == A_CMP_COUNT)
     cmp_count_body(D, L, reinterpret_cast<const uint8_t *>(P.p0[s]), P.p1[s], bx, gx);
-  if constexpr (OP == A_CMP_SCAN) cmp_scan_body(D, P.p1[s], P.nn[s], bx, gx);
+  if constexpr (OP == A_CMP_SCAN) cmp_scan_body(D, P.p1[s], P.nn[s], P.arg[s], bx, gx);
   if constexpr (OP == A_CMP_SCATTER)
     cmp_scatter_body(D, L, reinterpret_cast<const uint8_t *>(P.p0[s]), P.p1[s], P.p2[s], bx, gx);
   if constexpr (OP == A_RECORD) record_refines_body(D, L, P.p0[s], P.arg[s], bx, gx);
   if constexpr (OP == A_KEYS_CANDS) keys_cands_body(D, P.p0[s], P.p1[s], P.p2[s], P.nn[s], bx, gx);
   if constexpr (OP == A_CLEAR_SEL) {
+    if (D.ctr[C_SELECT] == 0) return;  // no selection at this level
     uint32_t *w = P.p0[s];
     for (long long i = (long long)bx * T + threadIdx.x; i < P.nn[s]; i += (long long)gx * T) w[i] = 0;
   }
@@ -904,6 +914,7 @@ struct AdaptLauncher {
       P.p1[i] = m[i].S.tile_sums;
       P.p2[i] = m[i].vals;
       P.nn[i] = nt(i);
+      P.arg[i] = sel ? 0 : 1;  // the threshold compaction decides C_SELECT
     }
     go<A_CMP_COUNT>([&](int i) { return in[i] ? nt(i) : 0; });
     go<A_CMP_SCAN, 1024>([&](int i) { return in[i] ? 1 : 0; });
@@ -983,8 +994,8 @@ struct AdaptLauncher {
       int ns = 0;
       for (int i = 0; i < n; i++)
         if (score[i])
-          seg[ns++] = SortSeg{m[i].keys, m[i].vals2, 8 * m[i].D.g.budget[L], m[i].D.ctr + C_MOVE_LIMIT, m[i].S,
-                              m[i].D.ctr + C_NCAND, 1};  // the compacted candidates only
+          seg[ns++] = SortSeg{m[i].keys, m[i].vals2, 8 * m[i].D.g.budget[L], m[i].D.ctr + C_SELECT, m[i].S,
+                              m[i].D.ctr + C_NCAND, 1};  // the compacted candidates only, when selecting
       launch_radix_sort_batch(seg, ns, st);
       for (int i = 0; i < n; i++) {
         P.p0[i] = m[i].keys2;
