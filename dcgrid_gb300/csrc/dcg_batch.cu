@@ -29,6 +29,13 @@ struct dcg_batch {
   float *p_arena = nullptr, *pt_arena = nullptr, *div_arena = nullptr;
   uint32_t *binfo = nullptr;  // block descriptions of a cascade round, 13 words per block
   uint32_t *bar = nullptr, *errw = nullptr;
+  // concurrent cascades (solve_barrier bit 2): members with two different level
+  // counts solved by two cooperative launch chains on parallel graph branches,
+  // each with its own barrier words and block-description table
+  std::vector<int> lgroup[2];
+  uint32_t *bar2 = nullptr, *binfo2 = nullptr;
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<unsigned long long> arena_off;
   int maxtop = 0, iters = 0;
   dcg_tuning tune{};
@@ -68,6 +75,9 @@ struct dcg_batch {
     for (dcg_sim *s : m) delete s;
     for (void *p : allocs) cudaFree(p);
     if (stage) cudaFreeHost(stage);
+    if (aux) cudaStreamDestroy(aux);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
 
@@ -75,8 +85,9 @@ struct dcg_batch {
   int groups() const { return (n() + BMAX - 1) / BMAX; }
 
   int set_solve_config() {
-    if (tune.solve_barrier < 0 || tune.solve_barrier > 3)
-      return fail(DCG_E_INVALID, "solve_barrier must be 0..3 (bit 0 two-level barrier, bit 1 coarsest-aligned rounds)");
+    if (tune.solve_barrier < 0 || tune.solve_barrier > 7)
+      return fail(DCG_E_INVALID, "solve_barrier must be 0..7 (bit 0 two-level barrier, bit 1 coarsest-aligned rounds, "
+                                 "bit 2 concurrent cascades of the two level counts)");
     if (!solve_variant_valid(tune.solve_cache))
       return fail(DCG_E_INVALID, "solve_cache must be 0, 3, 4, 8 or a pipelined variant 16, 18, 19, 32, 34, 35, 64, 66");
     for (int k = 0; k < 4; k++)
@@ -135,7 +146,42 @@ struct dcg_batch {
       }
   }
   // the cascade with the tuned schedule of each round
+  bool can_split() const { return n() <= BMAX && !lgroup[0].empty() && !lgroup[1].empty() && aux; }
+  // one member group's whole cascade (all its members have the same level count)
+  void solve_group(int gi, int grid, int cache, int tree, cudaStream_t st) {
+    const std::vector<int> &mem = lgroup[gi];
+    const int top = m[mem[0]]->D.g.levels - 1;
+    for (int round = 0; round <= top; round++) {
+      SolveBatch P{};
+      P.n = (int)mem.size();
+      P.maxtop = top;
+      P.prolong = 1;
+      P.p = p_arena;
+      P.pt = pt_arena;
+      P.div = div_arena;
+      P.binfo = gi ? binfo2 : binfo;
+      P.bar = gi ? bar2 : bar;
+      P.err = errw;
+      for (int i = 0; i < P.n; i++) {
+        P.d[i] = m[mem[i]]->D;
+        P.arena[i] = arena_off[mem[i]];
+      }
+      launch_level_solve_batch(P, round, iters, grid, cache, tree & 1, st);
+    }
+  }
+  void solve_split(int grid, int cache, int tree) {
+    cudaEventRecord(ev_fork, stream);
+    cudaStreamWaitEvent(aux, ev_fork, 0);
+    solve_group(0, grid, cache, tree, stream);
+    solve_group(1, grid, cache, tree, aux);
+    cudaEventRecord(ev_join, aux);
+    cudaStreamWaitEvent(stream, ev_join, 0);
+  }
   void solve_tuned() {
+    if ((tune.solve_barrier & 4) && can_split()) {
+      solve_split(solve_grid, tune.solve_cache, tune.solve_barrier);
+      return;
+    }
     for (int round = 0; round <= maxtop; round++) {
       if (round < 4 && tune.round_ctas_per_sm[round] != 0)
         solve_round(round, batch_solve_grid(sms, tune.round_cache[round], tune.round_ctas_per_sm[round]),
@@ -145,6 +191,10 @@ struct dcg_batch {
     }
   }
   void solve(int grid, int cache, int tree) {
+    if ((tune.solve_barrier & 4) && can_split()) {
+      solve_split(grid, cache, tree);
+      return;
+    }
     for (int round = 0; round <= maxtop; round++) solve_round(round, grid, cache, tree);
   }
   // tree: two-level barrier; the round alignment comes from tune.solve_barrier's bit 1
@@ -252,6 +302,7 @@ struct dcg_batch {
     int rc;
     if ((rc = cuda(cudaStreamSynchronize(stream), "sync"))) return rc;
     cudaMemsetAsync(bar, 0, 4 * (64 + 32 * 18), stream);
+    if (bar2) cudaMemsetAsync(bar2, 0, 4 * (64 + 32 * 18), stream);
     cudaMemsetAsync(errw, 0, 4, stream);
     for (dcg_sim *s : m)
       if ((rc = s->reset_adaptive())) return fail(rc, "member reset: " + s->err);
@@ -339,7 +390,9 @@ struct dcg_batch {
     for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66}) {
       const int occ = batch_solve_grid(sms, cache, 0) / std::max(1, sms);
       for (int k = 1; k <= occ; k++)
-        for (int tb = 0; tb < 4; tb++) {  // bit 0: two-level barrier; bit 1: coarsest-aligned rounds
+        for (int tb = 0; tb < 8; tb++) {  // bit 0: two-level barrier; bit 1: coarsest-aligned rounds;
+                                          // bit 2: concurrent cascades per level count
+          if ((tb & 4) && (!can_split() || (tb & 2))) continue;
           tune.solve_barrier = tb;
           const int grid = batch_solve_grid(sms, cache, k);
           const float ms = time_ms(reps, [&] { solve(grid, cache, tb & 1); });
@@ -353,8 +406,8 @@ struct dcg_batch {
     }
     tune.solve_barrier = best.solve_barrier;  // the per-round schedules below use its alignment
     // each round of the first four on its own: the best schedule if it beats
-    // the whole-cascade choice for that round
-    for (int r = 0; r < 4 && r <= maxtop; r++) {
+    // the whole-cascade choice for that round (not with concurrent cascades)
+    for (int r = 0; r < 4 && r <= maxtop && !(best.solve_barrier & 4); r++) {
       const float base = time_ms(reps, [&] {
         solve_round(r, batch_solve_grid(sms, best.solve_cache, best.solve_ctas_per_sm), best.solve_cache,
                     best.solve_barrier);
@@ -481,6 +534,11 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
     return rc;
   }
   cudaMemset(b->bar, 0, 4 * (64 + 32 * 18));
+  if ((rc = b->alloc(&b->bar2, 64 + 32 * 18)) || (rc = b->alloc(&b->binfo2, 13 * (cells / BV)))) {
+    delete b;
+    return rc;
+  }
+  cudaMemset(b->bar2, 0, 4 * (64 + 32 * 18));
   cudaMemset(b->errw, 0, 4);
   for (int i = 0; i < n; i++) {
     dcg_sim *s = new dcg_sim();
@@ -510,6 +568,26 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
     }
     S2.max_n = nb;
     b->S2.push_back(S2);
+  }
+  // level-count groups for concurrent cascades: exactly two level counts
+  {
+    int la = -1, lb = -1;
+    bool two = true;
+    for (int i = 0; i < n; i++) {
+      const int L = b->m[i]->D.g.levels;
+      if (la < 0 || L == la) la = L;
+      else if (lb < 0 || L == lb) lb = L;
+      else two = false;
+    }
+    if (two && lb >= 0) {
+      for (int i = 0; i < n; i++) b->lgroup[b->m[i]->D.g.levels == la ? 0 : 1].push_back(i);
+      if (cudaStreamCreateWithFlags(&b->aux, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        delete b;
+        return DCG_E_CUDA;
+      }
+    }
   }
   for (int k = 0; k < 4; k++) b->tune.tile[k] = 4;
   b->tune.solve_cache = 4;

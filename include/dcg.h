@@ -324,7 +324,10 @@ typedef struct {
   int32_t solve_barrier;     /* bit 0: grid barrier between sweeps, 0 flat, 1 two-level;
                                 bit 1: cascade round r solves every member's level
                                 levels-1-r (coarsest levels aligned) instead of level
-                                maxtop-r (finest levels aligned)                          */
+                                maxtop-r (finest levels aligned); bit 2 (batches of at
+                                most 16 members with two level counts): the members of
+                                each level count as a separate cascade, the two running
+                                concurrently; per-round schedules are then not used      */
   int32_t persistent;        /* cell stages as persistent kernels over the allocated blocks */
   /* per cascade round r < 4: its own schedule when round_ctas_per_sm[r] != 0
    * (CTAs per SM, or -k: one CTA per k SMs; cache depth; barrier), else the
