@@ -272,7 +272,11 @@ def run_batch(args, ctx):
     def make_batch(prec):
         b = Batch(batch_params(prec))
         b.set_stream(ctx.stream.cuda_stream)
-        tune = b.autotune(spinup_steps=5, reps=3)  # leaves the batch reset
+        if args.tuning:  # a given schedule (profiling runs), else autotuned
+            b.set_tuning(capi.tuning_from_dict(json.loads(args.tuning)))
+            tune = capi.tuning_to_dict(b.get_tuning())
+        else:
+            tune = b.autotune(spinup_steps=5, reps=3)  # leaves the batch reset
         for i, m in enumerate(b):
             m.set_emission(ems[i])
             m._em = ems[i]
@@ -293,6 +297,13 @@ def run_batch(args, ctx):
     ms, cells = ctx.max_sum(ms, cells)
     value = cells / (ms * 1e-3)
     info = bm.info()
+    if args.profile:  # the headline leg only (profiling runs)
+        line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ctx.world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "config": {"workload": "profile: headline leg only", "tuning": tune_m},
+                "gpu_launches": int(info["launches_per_step"] * args.steps)}
+        bm.close()
+        return line
 
     # FP32 batch (batching alone)
     bf, tune_f = make_batch(capi.PRECISION_FP32)
@@ -590,6 +601,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch", choices=["batch", "cloud", "large"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and FP64 error legs")
+    ap.add_argument("--profile", action="store_true",
+                    help="batch workload: time the headline leg only (for profiler runs)")
+    ap.add_argument("--tuning", default=None,
+                    help="batch workload: a tuning as JSON (the config.tuning of an earlier line) instead of autotuning")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

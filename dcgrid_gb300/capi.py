@@ -152,6 +152,21 @@ def tuning_to_dict(t):
             "round_cache": list(t.round_cache), "round_barrier": list(t.round_barrier)}
 
 
+def tuning_from_dict(d):
+    """Inverse of tuning_to_dict (missing keys stay zero)."""
+    t = DcgTuning()
+    for k, v in d.items():
+        if not hasattr(t, k):
+            continue
+        if isinstance(v, (list, tuple)):
+            arr = getattr(t, k)
+            for i, x in enumerate(v):
+                arr[i] = x
+        else:
+            setattr(t, k, v)
+    return t
+
+
 def default_params(gx, gy, gz, max_blocks):
     """The reference's SimParams defaults (src/data/sim_params.cpp:4-34) and its
     hard-wired solver/adaptation constants; mirrors dcg_default_params()."""
