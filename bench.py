@@ -145,9 +145,10 @@ class Ctx:
         build.build()
         self.stream = torch.cuda.Stream()
         self.flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-        d = os.path.join(ROOT, "gpurun_out")
-        self.clock_path = os.path.join(d, f"clocks_r{self.rank}.csv") if os.path.isdir(d) \
-            else f"/tmp/dcg_clocks_r{self.rank}.csv"
+        # the clock samples of the timed region (DCG_CLOCKS_DIR, else the temp directory)
+        import tempfile
+        d = os.environ.get("DCG_CLOCKS_DIR") or tempfile.gettempdir()
+        self.clock_path = os.path.join(d, f"dcg_clocks_r{self.rank}.csv")
 
     def barrier(self):
         if self.dist:

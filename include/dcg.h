@@ -422,8 +422,8 @@ int dcg_state_bytes(dcg_sim *sim, int64_t *bytes);
 int dcg_save_state(dcg_sim *sim, void *dst, int32_t where);
 int dcg_load_state(dcg_sim *sim, const void *src, int32_t where);
 
-/* ---- adjoint of the density path (spec extension; no reference
- * counterpart) ----------------------------------------------------------------
+/* ---- adjoint of the density path (extension; no reference counterpart) ------
+ * ------------------------------------------------------------------------------
  * With the flow and the topology of the last step held fixed, one step maps
  * the density linearly. dcg_adjoint_step applies the transpose of that map
  * for the step that produced the current state: lam_in (device, 64*max_blocks

@@ -1,4 +1,4 @@
-"""Adjoint of the density path on the GPU (spec extension).
+"""Adjoint of the density path on the GPU (an extension without reference counterpart).
 
 * state save/load reproduces a run exactly (checkpoints of the adjoint);
 * the GPU adjoint is the transpose of the GPU step (dot-product tests) and
