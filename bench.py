@@ -126,6 +126,15 @@ class Clocks:
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def reduce_max_sum(dist, torch, ms, cells, device):
+    """Whole-job figures of N replicas: the slowest rank's time and the cells
+    of all ranks (every rank receives both)."""
+    a = torch.tensor([ms, float(cells)], dtype=torch.float64, device=device)
+    dist.all_reduce(a[:1], op=dist.ReduceOp.MAX)
+    dist.all_reduce(a[1:], op=dist.ReduceOp.SUM)
+    return float(a[0].item()), float(a[1].item())
+
+
 class Ctx:
     """Process / rank context: torch device, stream, optional process group."""
 
@@ -159,11 +168,7 @@ class Ctx:
         """max of the time and sum of the cells over the ranks"""
         if not self.dist:
             return ms, cells
-        t = self.torch.tensor([ms, float(cells)], dtype=self.torch.float64, device="cuda")
-        a = t.clone()
-        self.dist.all_reduce(a[:1], op=self.dist.ReduceOp.MAX)
-        self.dist.all_reduce(a[1:], op=self.dist.ReduceOp.SUM)
-        return float(a[0].item()), float(a[1].item())
+        return reduce_max_sum(self.dist, self.torch, ms, cells, "cuda")
 
     def timed(self, steps, step_fn, cells_fn, nvtx="timed"):
         """device time of `steps` calls of step_fn (CUDA events on the sims'

@@ -57,3 +57,13 @@ def test_null_handles_are_rejected(dcg_lib):
 def test_oracle_exports(oracle_lib):
     for n in ["dcgo_create", "dcgo_step", "dcgo_get_field", "dcgo_apron_mismatches", "dcgo_adapt_replay"]:
         assert hasattr(oracle_lib, n)
+
+
+def test_tuning_dict_round_trip():
+    from dcgrid_gb300 import capi
+    t = capi.DcgTuning()
+    t.tile[0], t.tile[3], t.solve_cache, t.solve_ctas_per_sm, t.solve_barrier = 1, 8, 19, 3, 2
+    t.round_ctas_per_sm[2], t.round_cache[2], t.round_barrier[2] = -4, 18, 1
+    d = capi.tuning_to_dict(t)
+    back = capi.tuning_to_dict(capi.tuning_from_dict(d))
+    assert back == d
