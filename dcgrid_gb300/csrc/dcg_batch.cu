@@ -37,6 +37,8 @@ struct dcg_batch {
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<unsigned long long> arena_off;
+  float *emis_arena = nullptr;  // members' emission maps, consecutive in member order
+  size_t emis_floats = 0;
   int maxtop = 0, iters = 0;
   dcg_tuning tune{};
   int solve_grid = 0;
@@ -534,12 +536,20 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
     return rc;
   }
   cudaMemset(b->bar, 0, 4 * (64 + 32 * 18));
+  for (int i = 0; i < n; i++)
+    if (params[i].emission_n > 0)
+      b->emis_floats += (size_t)params[i].emission_n * params[i].emission_n * params[i].emission_n;
+  if (b->emis_floats > 0 && (rc = b->alloc(&b->emis_arena, b->emis_floats))) {
+    delete b;
+    return rc;
+  }
   if ((rc = b->alloc(&b->bar2, 64 + 32 * 18)) || (rc = b->alloc(&b->binfo2, 13 * (cells / BV)))) {
     delete b;
     return rc;
   }
   cudaMemset(b->bar2, 0, 4 * (64 + 32 * 18));
   cudaMemset(b->errw, 0, 4);
+  size_t emis_at = 0;
   for (int i = 0; i < n; i++) {
     dcg_sim *s = new dcg_sim();
     s->P = params[i];
@@ -552,6 +562,10 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
     s->ext_p = b->p_arena + b->arena_off[i];
     s->ext_pt = b->pt_arena + b->arena_off[i];
     s->ext_div = b->div_arena + b->arena_off[i];
+    if (params[i].emission_n > 0) {
+      s->ext_emis = b->emis_arena + emis_at;
+      emis_at += (size_t)params[i].emission_n * params[i].emission_n * params[i].emission_n;
+    }
     b->m.push_back(s);
     if ((rc = s->create_adaptive())) {
       b->err = "member " + std::to_string(i) + ": " + s->err;
@@ -664,6 +678,13 @@ int dcg_batch_get_info(const dcg_batch *b, int32_t *n, int64_t *device_bytes, in
 int dcg_batch_time_solve(dcg_batch *b, int32_t reps, float *avg_ms, double *bytes) {
   if (bad(b) || reps <= 0 || !avg_ms) return DCG_E_INVALID;
   return b->time_solve(reps, avg_ms, bytes);
+}
+int dcg_batch_set_emission(dcg_batch *b, const float *maps, int32_t where) {
+  if (bad(b) || !maps) return DCG_E_INVALID;
+  if (b->emis_floats == 0) return b->fail(DCG_E_INVALID, "no member has an emission map");
+  return b->cuda(cudaMemcpyAsync(b->emis_arena, maps, b->emis_floats * 4,
+                                 where == DCG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, b->stream),
+                 "batch set_emission");
 }
 int dcg_batch_get_stats(dcg_batch *b, dcg_stats *out) {
   if (bad(b) || !out) return DCG_E_INVALID;

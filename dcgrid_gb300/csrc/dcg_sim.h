@@ -72,6 +72,7 @@ struct dcg_sim {
   // batch members: p and p~ are slices of the batch's arenas, and the batch
   // steps the member (its own step and stage entry points are refused)
   float *ext_p = nullptr, *ext_pt = nullptr, *ext_div = nullptr;
+  float *ext_emis = nullptr;  // batch members: the emission map is a slice of the batch's arena
   bool batch_member = false;
 
   int fail(int code, const std::string &msg) {
@@ -287,7 +288,8 @@ struct dcg_sim {
     if (ls_grid_staged <= 0 && ls_epoch == 3) ls_epoch = 2;
     if (P.emission_n > 0) {
       const size_t ne = (size_t)P.emission_n * P.emission_n * P.emission_n;
-      if ((rc = alloc(&emis, ne))) return rc;
+      if (ext_emis) emis = ext_emis;
+      else if ((rc = alloc(&emis, ne))) return rc;
       if ((rc = cuda(cudaMemset(emis, 0, ne * 4), "emission"))) return rc;
       fill_phys(D.ph);
       fill_phys(U.ph);

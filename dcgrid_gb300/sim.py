@@ -81,6 +81,7 @@ def lib():
         L.dcg_batch_get_info.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.dcg_batch_time_solve.argtypes = [vp, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_double)]
         L.dcg_batch_get_stats.argtypes = [vp, vp]
+        L.dcg_batch_set_emission.argtypes = [vp, vp, C.c_int32]
         L.dcg_batch_last_error_string.argtypes = [vp]
         L.dcg_batch_last_error_string.restype = C.c_char_p
         for name in ["dcg_sizeof_params", "dcg_sizeof_info", "dcg_sizeof_stats", "dcg_sizeof_tuning",
@@ -507,6 +508,18 @@ class Batch:
         n, nb, nl = C.c_int32(), C.c_int64(), C.c_int64()
         self._chk(self.L.dcg_batch_get_info(self.h, C.byref(n), C.byref(nb), C.byref(nl)), "get_info")
         return {"n": n.value, "device_bytes": nb.value, "launches_per_step": nl.value}
+
+    def set_emission(self, maps):
+        """Every member's emission map in one copy: the maps of the members with
+        emission_n > 0, in member order, as one contiguous host array or CUDA
+        torch tensor (pinned host tensors are copied asynchronously)."""
+        if hasattr(maps, "data_ptr"):
+            where = capi.DEVICE if maps.is_cuda else capi.HOST
+            self._chk(self.L.dcg_batch_set_emission(self.h, C.c_void_p(maps.data_ptr()), where), "set_emission")
+            return
+        a = np.ascontiguousarray(maps, np.float32)
+        self._emis_keep = a
+        self._chk(self.L.dcg_batch_set_emission(self.h, _ptr(a), capi.HOST), "set_emission")
 
     def stats(self):
         """dcg_get_stats of every member, with one synchronisation."""

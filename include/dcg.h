@@ -357,6 +357,11 @@ int dcg_batch_autotune(dcg_batch *batch, int32_t spinup_steps, int32_t reps, dcg
 int dcg_batch_get_tuning(const dcg_batch *batch, dcg_tuning *out);
 int dcg_batch_set_tuning(dcg_batch *batch, const dcg_tuning *tuning);
 int dcg_batch_get_info(const dcg_batch *batch, int32_t *n, int64_t *device_bytes, int64_t *launches_per_step);
+/* Every member's emission map in one copy (stream-ordered on the batch's
+ * stream): maps holds the emission_n^3 maps of the members with emission_n > 0,
+ * in member order, consecutively; `where` says whether it is host or device
+ * memory. Equivalent to dcg_set_emission on each of those members. */
+int dcg_batch_set_emission(dcg_batch *batch, const float *maps, int32_t where);
 /* dcg_get_stats of every member (out: n entries), one launch per group of 16
  * members and one synchronisation */
 int dcg_batch_get_stats(dcg_batch *batch, dcg_stats *out);

@@ -170,3 +170,19 @@ def test_batch_stats_equal_member_stats(persistent):
         one = m.stats()
         assert st.active_cells == one.active_cells and list(st.load) == list(one.load)
         assert st.mass == pytest.approx(one.mass, rel=1e-12) and st.residual == pytest.approx(one.residual, rel=1e-9)
+
+
+def test_batch_emission_upload_equals_member_uploads():
+    from dcgrid_gb300 import Batch
+    params = scenarios.plume_batch(3, 4, sizes=(16, 32), iters=10, em_n=8)
+    rng = np.random.default_rng(5)
+    maps = [rng.random((8, 8, 8), dtype=np.float32) for _ in params]
+    a, b = Batch(params), Batch(params)
+    for i, m in enumerate(a):
+        m.set_emission(maps[i])
+    b.set_emission(np.concatenate([x.ravel() for x in maps]))
+    for s in (a, b):
+        s.step(3)
+        s.sync()
+    for i, p in enumerate(params):
+        compare(a[i], b[i], p, f"member {i}")
