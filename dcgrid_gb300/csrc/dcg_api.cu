@@ -442,6 +442,7 @@ int dcg_set_graphs(dcg_sim *s, int32_t on) {
 int dcg_time_kernel(dcg_sim *s, int32_t which, int32_t level, int32_t reps, float *avg_ms, double *bytes) {
   if (bad(s) || !avg_ms || reps <= 0 || s->mode != DCG_MODE_ADAPTIVE) return DCG_E_INVALID;
   if (level < 0 || level >= s->D.g.levels) return s->fail(DCG_E_INVALID, "no such level");
+  if (which == 4 && s->ls_grid <= 0) return s->fail(DCG_E_INVALID, "no cooperative level solve on this device");
   long long load[MAXL];
   int rc;
   if ((rc = s->cuda(cudaMemcpyAsync(load, s->D.load, sizeof(load), cudaMemcpyDeviceToHost, s->stream), "load")))
@@ -468,7 +469,6 @@ int dcg_time_kernel(dcg_sim *s, int32_t which, int32_t level, int32_t reps, floa
       default: launch_divergence(s->D, s->stream); break;
     }
   };
-  if (which == 4 && s->ls_grid <= 0) return s->fail(DCG_E_INVALID, "no cooperative level solve on this device");
   launch(0);  // warm
   cudaEventRecord(e0, s->stream);
   for (int i = 0; i < reps; i++) launch(i);
