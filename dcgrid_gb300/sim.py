@@ -117,6 +117,31 @@ def _field_id(field):
     return capi.FIELD_NAMES[field] if isinstance(field, str) else int(field)
 
 
+def _buf(obj, count, dtype, what, writable=False, device=False):
+    """(pointer, capi.HOST | capi.DEVICE) of a C-contiguous numpy array or
+    torch tensor of exactly `count` elements of `dtype`. The C library reads or
+    writes that many elements behind the pointer, so anything else (wrong size,
+    dtype or layout, a read-only output, a host buffer where the call needs
+    device memory) raises DcgError(DCG_E_INVALID) before it is called."""
+    dt = np.dtype(dtype)
+    if hasattr(obj, "data_ptr"):
+        got = f"tensor {tuple(obj.shape)} {obj.dtype}{' cuda' if obj.is_cuda else ''}"
+        ok = (str(obj.dtype).rsplit(".", 1)[-1] == dt.name and obj.is_contiguous() and obj.numel() == count
+              and (obj.is_cuda or not device))
+        if ok:
+            return C.c_void_p(obj.data_ptr()), (capi.DEVICE if obj.is_cuda else capi.HOST)
+    elif isinstance(obj, np.ndarray):
+        got = f"array {obj.shape} {obj.dtype}"
+        ok = (obj.dtype == dt and obj.flags.c_contiguous and obj.size == count and not device
+              and (obj.flags.writeable or not writable))
+        if ok:
+            return _ptr(obj), capi.HOST
+    else:
+        got = type(obj).__name__
+    where = "CUDA tensor" if device else "array or tensor"
+    raise DcgError(capi.DCG_E_INVALID, f"{what}: expected a contiguous {dt.name} {where} of {count} elements, got {got}")
+
+
 class Simulation:
     """One simulation handle (adaptive or uniform)."""
 
@@ -199,13 +224,14 @@ class Simulation:
     def set_emission(self, field):
         """Emission field (emission_n^3, x fastest) from a host array or a CUDA
         torch tensor (pinned host tensors are copied asynchronously)."""
-        if hasattr(field, "data_ptr"):
-            where = capi.DEVICE if field.is_cuda else capi.HOST
-            self._chk(self.L.dcg_set_emission(self.h, C.c_void_p(field.data_ptr()), where), "set_emission")
-            return
-        a = np.ascontiguousarray(field, np.float32)
-        self._emis_keep = a
-        self._chk(self.L.dcg_set_emission(self.h, _ptr(a), capi.HOST), "set_emission")
+        n = int(self.params.emission_n) ** 3
+        a = field if hasattr(field, "data_ptr") else np.ascontiguousarray(field, np.float32)
+        if n == 0:  # no emission map: the library reports it
+            self._chk(self.L.dcg_set_emission(self.h, _ptr(np.zeros(1, np.float32)), capi.HOST), "set_emission")
+        ptr, where = _buf(a, n, np.float32, "set_emission")
+        if where == capi.HOST:
+            self._emis_keep = a  # an asynchronous copy may still read it
+        self._chk(self.L.dcg_set_emission(self.h, ptr, where), "set_emission")
 
     def add_velocity_noise(self, seed, amplitude):
         self._chk(self.L.dcg_add_velocity_noise(self.h, seed, amplitude), "noise")
@@ -219,20 +245,16 @@ class Simulation:
         """Host copy (float32 numpy) in the canonical layout, or, when `out` is a
         CUDA torch tensor, a device-to-device copy into it."""
         fid = _field_id(field)
-        if out is not None and hasattr(out, "data_ptr") and out.is_cuda:
-            self._chk(self.L.dcg_get_field(self.h, fid, C.c_void_p(out.data_ptr()), capi.DEVICE), "get_field")
-            return out
         a = np.empty(self.num_cells, np.float32) if out is None else out
-        self._chk(self.L.dcg_get_field(self.h, fid, _ptr(a), capi.HOST), "get_field")
+        ptr, where = _buf(a, self.num_cells, np.float32, "get_field", writable=True)
+        self._chk(self.L.dcg_get_field(self.h, fid, ptr, where), "get_field")
         return a
 
     def set_field(self, field, values):
         fid = _field_id(field)
-        if hasattr(values, "data_ptr") and values.is_cuda:
-            self._chk(self.L.dcg_set_field(self.h, fid, C.c_void_p(values.data_ptr()), capi.DEVICE), "set_field")
-            return
-        a = np.ascontiguousarray(values, np.float32)
-        self._chk(self.L.dcg_set_field(self.h, fid, _ptr(a), capi.HOST), "set_field")
+        a = values if hasattr(values, "data_ptr") else np.ascontiguousarray(values, np.float32)
+        ptr, where = _buf(a, self.num_cells, np.float32, "set_field")
+        self._chk(self.L.dcg_set_field(self.h, fid, ptr, where), "set_field")
 
     def get_dense(self, field):
         p = self.params
@@ -255,9 +277,13 @@ class Simulation:
                     load=load[:lv], move_limit=ml[:lv])
 
     def set_topology(self, topo):
+        B = int(self.info.max_blocks)
         pos = np.ascontiguousarray(topo["pos"], np.int32)
         parent = np.ascontiguousarray(topo["parent"], np.uint32)
         child = np.ascontiguousarray(topo["child"], np.uint32)
+        _buf(pos, 4 * B, np.int32, "set_topology pos")
+        _buf(parent, B, np.uint32, "set_topology parent")
+        _buf(child, 8 * B, np.uint32, "set_topology child")
         load = np.zeros(16, np.int64)
         load[: len(topo["load"])] = topo["load"]
         ml = np.zeros(16, np.int64)
@@ -297,12 +323,9 @@ class Simulation:
         """RGBA image (height, width, 4) float32: numpy (host) or a CUDA torch
         tensor given as `out`."""
         if out is None:
-            out = np.empty((rp.height, rp.width, 4), np.float32)
-        if hasattr(out, "data_ptr"):
-            where = capi.DEVICE if out.is_cuda else capi.HOST
-            self._chk(self.L.dcg_render(self.h, C.byref(rp), C.c_void_p(out.data_ptr()), where), "render")
-        else:
-            self._chk(self.L.dcg_render(self.h, C.byref(rp), _ptr(out), capi.HOST), "render")
+            out = np.empty((max(rp.height, 0), max(rp.width, 0), 4), np.float32)
+        ptr, where = _buf(out, max(rp.height, 0) * max(rp.width, 0) * 4, np.float32, "render", writable=True)
+        self._chk(self.L.dcg_render(self.h, C.byref(rp), ptr, where), "render")
         return out
 
     # -- state I/O (checkpoint / resume) ------------------------------------
@@ -314,22 +337,17 @@ class Simulation:
     def save_state(self, out=None):
         """The state a step depends on, into a uint8 buffer: a numpy array (host)
         or a CUDA torch tensor (device); a new host array when out is None."""
+        n = self.state_bytes()
         if out is None:
-            out = np.empty(self.state_bytes(), np.uint8)
-        if hasattr(out, "data_ptr"):
-            where = capi.DEVICE if out.is_cuda else capi.HOST
-            self._chk(self.L.dcg_save_state(self.h, C.c_void_p(out.data_ptr()), where), "save_state")
-        else:
-            self._chk(self.L.dcg_save_state(self.h, _ptr(out), capi.HOST), "save_state")
+            out = np.empty(n, np.uint8)
+        ptr, where = _buf(out, n, np.uint8, "save_state", writable=True)
+        self._chk(self.L.dcg_save_state(self.h, ptr, where), "save_state")
         return out
 
     def load_state(self, buf):
-        if hasattr(buf, "data_ptr"):
-            where = capi.DEVICE if buf.is_cuda else capi.HOST
-            self._chk(self.L.dcg_load_state(self.h, C.c_void_p(buf.data_ptr()), where), "load_state")
-        else:
-            a = np.ascontiguousarray(buf, np.uint8)
-            self._chk(self.L.dcg_load_state(self.h, _ptr(a), capi.HOST), "load_state")
+        a = buf if hasattr(buf, "data_ptr") else np.ascontiguousarray(buf, np.uint8)
+        ptr, where = _buf(a, self.state_bytes(), np.uint8, "load_state")
+        self._chk(self.L.dcg_load_state(self.h, ptr, where), "load_state")
 
     def save(self, path):
         """Writes the state to a file (checkpoint)."""
@@ -342,18 +360,54 @@ class Simulation:
     def adjoint_step(self, lam_in, lam_out, lam_emission=None):
         """lam_out <- transpose of the last step's density map applied to
         lam_in; lam_emission (emission_n^3) accumulates the emission adjoint."""
-        em = C.c_void_p(lam_emission.data_ptr()) if lam_emission is not None else None
-        self._chk(self.L.dcg_adjoint_step(self.h, C.c_void_p(lam_in.data_ptr()), C.c_void_p(lam_out.data_ptr()), em),
-                  "adjoint_step")
+        n = self.num_cells
+        li, _ = _buf(lam_in, n, np.float32, "adjoint_step lam_in", device=True)
+        lo, _ = _buf(lam_out, n, np.float32, "adjoint_step lam_out", device=True)
+        em = None
+        if lam_emission is not None and self.params.emission_n > 0:
+            em, _ = _buf(lam_emission, int(self.params.emission_n) ** 3, np.float32, "adjoint_step lam_emission",
+                         device=True)
+        self._chk(self.L.dcg_adjoint_step(self.h, li, lo, em), "adjoint_step")
 
     def adjoint_dense(self, lam_dense, lam_cells):
-        self._chk(self.L.dcg_adjoint_dense(self.h, C.c_void_p(lam_dense.data_ptr()),
-                                           C.c_void_p(lam_cells.data_ptr())), "adjoint_dense")
+        p = self.params
+        ld, _ = _buf(lam_dense, p.gx * p.gy * p.gz, np.float32, "adjoint_dense lam_dense", device=True)
+        lc, _ = _buf(lam_cells, self.num_cells, np.float32, "adjoint_dense lam_cells", device=True)
+        self._chk(self.L.dcg_adjoint_dense(self.h, ld, lc), "adjoint_dense")
 
     def stats(self):
         st = capi.DcgStats()
         self._chk(self.L.dcg_get_stats(self.h, C.byref(st)), "stats")
         return st
+
+
+def _reference_render(sim, dest, resolution, eyePos, eyeDir, fov, sunDir, switches):
+    """FluidSimulation::render(dest, resolution, eyePos, eyeDir, fov, sunDir)
+    (src/fluid_simulation.h:18-20). The reference writes float4 texels into a
+    CUDA surface (dcgrid/dcgrid_rendering.cu:91); here `dest` is a (height,
+    width, 4) float32 numpy array or CUDA tensor, or None for a new host image.
+    The reference reads its render switches from SimParams; `switches` sets
+    the matching dcg_render_params fields (channel, shadows, solids, precise,
+    aa_samples, ambient, smoke_color, scene_color, floor_color), the rest keep
+    the reference's defaults."""
+    width, height = int(resolution[0]), int(resolution[1])
+    rp = default_render_params(width, height)
+    for name, v in (("eye", eyePos), ("eye_dir", eyeDir), ("sun_dir", sunDir)):
+        arr = getattr(rp, name)
+        for i in range(3):
+            arr[i] = float(v[i])
+    rp.fov = float(fov)
+    for name, v in switches.items():
+        if name not in ("channel", "shadows", "solids", "precise", "aa_samples", "ambient", "smoke_color",
+                        "scene_color", "floor_color"):
+            raise TypeError(f"render: unknown switch {name!r}")
+        if name.endswith("_color"):
+            arr = getattr(rp, name)
+            for i in range(3):
+                arr[i] = float(v[i])
+        else:
+            setattr(rp, name, v)
+    return Simulation.render(sim, rp, dest)
 
 
 class FluidSimulationDCGrid(Simulation):
@@ -381,6 +435,14 @@ class FluidSimulationDCGrid(Simulation):
     def advectDensity(self):
         self.advect_scalars()
 
+    def render(self, dest, resolution=None, eyePos=None, eyeDir=None, fov=None, sunDir=None, **switches):
+        """The reference's render(dest, resolution, eyePos, eyeDir, fov,
+        sunDir) (fluid_simulation_dcgrid.cu:485); given a DcgRenderParams
+        first, Simulation.render(rp, out)."""
+        if isinstance(dest, capi.DcgRenderParams):
+            return Simulation.render(self, dest, resolution)
+        return _reference_render(self, dest, resolution, eyePos, eyeDir, fov, sunDir, switches)
+
     def debugStats(self):
         return self.stats().residual
 
@@ -407,6 +469,14 @@ class FluidSimulationUniform(Simulation):
 
     def advectDensity(self):
         self.advect_scalars()
+
+    def render(self, dest, resolution=None, eyePos=None, eyeDir=None, fov=None, sunDir=None, **switches):
+        """The reference's render(dest, resolution, eyePos, eyeDir, fov,
+        sunDir) (fluid_simulation_uniform.cu:149); given a DcgRenderParams
+        first, Simulation.render(rp, out)."""
+        if isinstance(dest, capi.DcgRenderParams):
+            return Simulation.render(self, dest, resolution)
+        return _reference_render(self, dest, resolution, eyePos, eyeDir, fov, sunDir, switches)
 
     def debugStats(self):
         return self.stats().mass
@@ -513,13 +583,15 @@ class Batch:
         """Every member's emission map in one copy: the maps of the members with
         emission_n > 0, in member order, as one contiguous host array or CUDA
         torch tensor (pinned host tensors are copied asynchronously)."""
-        if hasattr(maps, "data_ptr"):
-            where = capi.DEVICE if maps.is_cuda else capi.HOST
-            self._chk(self.L.dcg_batch_set_emission(self.h, C.c_void_p(maps.data_ptr()), where), "set_emission")
-            return
-        a = np.ascontiguousarray(maps, np.float32)
-        self._emis_keep = a
-        self._chk(self.L.dcg_batch_set_emission(self.h, _ptr(a), capi.HOST), "set_emission")
+        n = sum(int(p.emission_n) ** 3 for p in self.params)
+        a = maps if hasattr(maps, "data_ptr") else np.ascontiguousarray(maps, np.float32)
+        if n == 0:  # no member has an emission map: the library reports it
+            self._chk(self.L.dcg_batch_set_emission(self.h, _ptr(np.zeros(1, np.float32)), capi.HOST),
+                      "set_emission")
+        ptr, where = _buf(a, n, np.float32, "set_emission")
+        if where == capi.HOST:
+            self._emis_keep = a  # an asynchronous copy may still read it
+        self._chk(self.L.dcg_batch_set_emission(self.h, ptr, where), "set_emission")
 
     def stats(self):
         """dcg_get_stats of every member, with one synchronisation."""
