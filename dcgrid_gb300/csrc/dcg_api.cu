@@ -230,6 +230,42 @@ int dcg_set_emission(dcg_sim *s, const float *field, int32_t where) {
                  "set_emission");
 }
 
+int dcg_set_heightmap(dcg_sim *s, const float *heights, int32_t nx, int32_t nz, int32_t where) {
+  if (bad(s)) return DCG_E_INVALID;
+  if (member_refused(s)) return DCG_E_INVALID;
+  if (heights && (nx <= 0 || nz <= 0 || nx > 65536 || nz > 65536 || (long long)nx * nz > (1ll << 27)))
+    return s->fail(DCG_E_INVALID, "heightmap: 1 <= nx, nz <= 65536 and nx * nz <= 2^27");
+  if (!heights && (nx != 0 || nz != 0)) return s->fail(DCG_E_INVALID, "heightmap: no heights given for nx, nz > 0");
+  int rc;
+  if ((rc = s->sync("set_heightmap"))) return rc;  // steps in flight may read the old map
+  // captured step graphs hold the physics, and with it the map pointer, by value
+  for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
+  if (s->hmap) cudaFree(s->hmap);
+  s->hmap = nullptr;
+  s->hm_nx = s->hm_nz = 0;
+  if (heights) {
+    const size_t n = (size_t)nx * nz;
+    float *h = nullptr;
+    rc = s->cuda(cudaMalloc(&h, n * sizeof(float)), "set_heightmap");
+    if (!rc)
+      rc = s->cuda(cudaMemcpyAsync(h, heights, n * sizeof(float),
+                                   where == DCG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                   s->stream), "set_heightmap");
+    if (rc) {
+      if (h) cudaFree(h);
+    } else {
+      s->hmap = h;
+      s->hm_nx = nx;
+      s->hm_nz = nz;
+    }
+  }
+  s->fill_phys(s->D.ph);
+  s->fill_phys(s->U.ph);
+  if (rc) return rc;  // back on the noise terrain
+  return s->mode == DCG_MODE_ADAPTIVE ? s->reset_adaptive() : s->reset_uniform();
+}
+
 int dcg_add_velocity_noise(dcg_sim *s, uint64_t seed, float amplitude) {
   if (bad(s)) return DCG_E_INVALID;
   if (s->mode == DCG_MODE_ADAPTIVE) launch_add_noise(s->D, seed, amplitude, s->stream);

@@ -75,6 +75,9 @@ struct Phys {
   const float *em;  // em_n^3 emission field (device), or null
   float src_jit;    // source temperature jitter amplitude
   unsigned src_seed;
+  const float *hm;  // hm_nx * hm_nz terrain heightmap (device, x fastest), or null
+  int hm_nx, hm_nz;
+  float hm_sx, hm_sz;  // texels per finest cell: hm_nx / gx, hm_nz / gz
 };
 
 struct Dev {
@@ -315,7 +318,26 @@ __device__ inline float noise_unit(unsigned long long seed, int x, int y, int z,
   return 2.0f * u - 1.0f;
 }
 
+// Bilinear sample of the heightmap at (x, z) in finest cells; texel centres
+// at (i + 0.5) / hm_sx, edge texels extended. The coordinate is clamped to
+// [-1, n] before the conversion to int, so far-away or NaN positions (render
+// rays) index inside the map.
+__device__ inline float heightmap_sample(const Phys &P, float x, float z) {
+  const float u = fminf(fmaxf(x * P.hm_sx - 0.5f, -1.f), (float)P.hm_nx);
+  const float v = fminf(fmaxf(z * P.hm_sz - 0.5f, -1.f), (float)P.hm_nz);
+  const float iu = floorf(u), iv = floorf(v);
+  const float fu = u - iu, fv = v - iv;
+  const int i0 = min(max((int)iu, 0), P.hm_nx - 1), i1 = min(max((int)iu + 1, 0), P.hm_nx - 1);
+  const int k0 = min(max((int)iv, 0), P.hm_nz - 1), k1 = min(max((int)iv + 1, 0), P.hm_nz - 1);
+  const float h00 = P.hm[k0 * P.hm_nx + i0], h10 = P.hm[k0 * P.hm_nx + i1];
+  const float h01 = P.hm[k1 * P.hm_nx + i0], h11 = P.hm[k1 * P.hm_nx + i1];
+  const float a = h00 + (h10 - h00) * fu;
+  const float b = h01 + (h11 - h01) * fu;
+  return a + (b - a) * fv;
+}
+
 __device__ inline float terrain_height(const Phys &P, float x, float z) {
+  if (P.hm) return P.ter_base + P.ter_amp * heightmap_sample(P, x, z);
   float sum = 0.f, amp = 1.f, norm = 0.f, f = P.ter_freq;
   for (int o = 0; o < P.ter_oct; o++) {
     const float u = x * f, v = z * f;

@@ -50,6 +50,8 @@ struct dcg_sim {
   float *adj_tmp = nullptr;    // adjoint scratch (allocated on first use)
   float *render_tmp = nullptr; // renderer output staging for host buffers
   size_t render_cap = 0;
+  float *hmap = nullptr;       // terrain heightmap (dcg_set_heightmap), or null
+  int hm_nx = 0, hm_nz = 0;
   int vpar = 0, qpar = 0;
 
   // uniform
@@ -112,6 +114,7 @@ struct dcg_sim {
   }
   ~dcg_sim() {
     if (render_tmp) cudaFree(render_tmp);
+    if (hmap) cudaFree(hmap);
     free_all();
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
@@ -171,6 +174,11 @@ struct dcg_sim {
     ph.em_n = P.emission_n;
     ph.em_band = P.emission_band;
     ph.em = emis;
+    ph.hm = hmap;
+    ph.hm_nx = hm_nx;
+    ph.hm_nz = hm_nz;
+    ph.hm_sx = hmap ? (float)hm_nx / (float)P.gx : 0.f;
+    ph.hm_sz = hmap ? (float)hm_nz / (float)P.gz : 0.f;
   }
 
   int validate_common() {

@@ -1,7 +1,8 @@
 """Scene builders: the reference's default scene and the benchmark scenes
 (smoke plume, terrain cloud, batches of uneven plumes) as dcg_params, plus
 seeded emission maps. Terrain comes from seeded value noise evaluated on the
-device (src/noise.cpp:20-107 inspired; the reference's Noise has no seed)."""
+device (src/noise.cpp:20-107 inspired; the reference's Noise has no seed), or
+from a heightmap (dcg_set_heightmap) such as the seeded one built here."""
 import random
 
 import numpy as np
@@ -144,6 +145,21 @@ def cloud256(precision=capi.PRECISION_FP32, blocks=40000, levels=3, iters=100, e
     p.emission_n = em_n
     p.emission_band = 16.0
     return p
+
+
+def heightmap(nx=48, nz=40, seed=0, waves=3):
+    """Seeded (nz, nx) float32 heightmap in [0, 1] for dcg_set_heightmap: a sum
+    of `waves` plane waves with random wave vectors (1 to 4 periods across the
+    map) and phases, rescaled to [0, 1]."""
+    rng = np.random.default_rng(seed)
+    x = (np.arange(nx) + 0.5) / nx
+    z = (np.arange(nz) + 0.5) / nz
+    X, Z = np.meshgrid(x, z)
+    h = np.zeros_like(X)
+    for _ in range(waves):
+        kx, kz = rng.uniform(1.0, 4.0, 2)
+        h += np.sin(2.0 * np.pi * (kx * X + kz * Z) + rng.uniform(0.0, 2.0 * np.pi))
+    return ((h - h.min()) / (h.max() - h.min())).astype(np.float32)
 
 
 def emission_field(n=16, seed=1, scale=0.05):

@@ -61,6 +61,7 @@ def lib():
                                       C.POINTER(C.c_double)]
         L.dcg_launches_per_step.argtypes = [vp, C.POINTER(C.c_int64)]
         L.dcg_set_emission.argtypes = [vp, vp, C.c_int32]
+        L.dcg_set_heightmap.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32]
         L.dcg_default_render_params.argtypes = [C.POINTER(capi.DcgRenderParams), C.c_int32, C.c_int32]
         L.dcg_default_render_params.restype = None
         L.dcg_render.argtypes = [vp, C.POINTER(capi.DcgRenderParams), vp, C.c_int32]
@@ -232,6 +233,21 @@ class Simulation:
         if where == capi.HOST:
             self._emis_keep = a  # an asynchronous copy may still read it
         self._chk(self.L.dcg_set_emission(self.h, ptr, where), "set_emission")
+
+    def set_heightmap(self, heights):
+        """Terrain from a (nz, nx) heightmap (x fastest; a host array or CUDA
+        torch tensor) instead of the value noise: height = terrain_base_height
+        + terrain_amplitude * bilinear sample. None restores the noise terrain.
+        Resets the simulation."""
+        if heights is None:
+            self._chk(self.L.dcg_set_heightmap(self.h, None, 0, 0, capi.HOST), "set_heightmap")
+            return
+        a = heights if hasattr(heights, "data_ptr") else np.ascontiguousarray(heights, np.float32)
+        if len(a.shape) != 2:
+            raise DcgError(capi.DCG_E_INVALID, f"set_heightmap: expected (nz, nx) heights, got shape {tuple(a.shape)}")
+        nz, nx = int(a.shape[0]), int(a.shape[1])
+        ptr, where = _buf(a, nx * nz, np.float32, "set_heightmap")
+        self._chk(self.L.dcg_set_heightmap(self.h, ptr, nx, nz, where), "set_heightmap")
 
     def add_velocity_noise(self, seed, amplitude):
         self._chk(self.L.dcg_add_velocity_noise(self.h, seed, amplitude), "noise")

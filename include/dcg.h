@@ -227,6 +227,20 @@ int dcg_sync(dcg_sim *sim);                /* wait for the handle's stream; read
  * steps; the step reads it in place, so it may change between steps. */
 int dcg_set_emission(dcg_sim *sim, const float *field, int32_t where);
 
+/* Terrain from a heightmap instead of the seeded value noise (the role of the
+ * reference's MipmappedTex::loadFromBuffer, utils/mipmapped_tex.h:64-66, an
+ * input its step never reads). heights: nx*nz floats, x fastest, from host or
+ * device memory; texel (i, k) sits at x = (i + 0.5)*gx/nx, z = (k + 0.5)*gz/nz
+ * in finest cells. The terrain height at (x, z) is terrain_base_height +
+ * terrain_amplitude * m, m the bilinear sample of the map (edge texels
+ * extended), and enters the SDF and fluidity like the noise terrain
+ * (solids must include DCG_SOLIDS_TERRAIN). The scene's solids are part of
+ * the initial state, so the call resets the simulation. heights == NULL
+ * (nx = nz = 0) returns to the noise terrain, also with a reset. The map is
+ * an input, not state: dcg_save_state does not store it. Not for members of
+ * a batch. */
+int dcg_set_heightmap(dcg_sim *sim, const float *heights, int32_t nx, int32_t nz, int32_t where);
+
 /* Adds seeded uniform noise in [-amplitude, amplitude] to every velocity
  * component of every allocated cell (deterministic counter-based hash). */
 int dcg_add_velocity_noise(dcg_sim *sim, uint64_t seed, float amplitude);

@@ -132,6 +132,17 @@ struct Base {
   virtual int stats(dcg_stats *st) = 0;
   virtual int set_emission(const double *src) = 0;
   virtual int render(const dcg_render_params &rp, double *out) const = 0;
+  // dcg_set_heightmap: replaces the noise terrain (empty map: back to it) and resets
+  virtual int set_heightmap(const float *h, int nx, int nz) = 0;
+  std::vector<float> hmap;
+  int store_heightmap(const float *h, int nx, int nz) {
+    if (h && (nx <= 0 || nz <= 0 || nx > 65536 || nz > 65536 || (int64_t)nx * nz > (1ll << 27)))
+      return fail(DCG_E_INVALID, "heightmap: 1 <= nx, nz <= 65536 and nx * nz <= 2^27");
+    if (!h && (nx != 0 || nz != 0)) return fail(DCG_E_INVALID, "heightmap: no heights given for nx, nz > 0");
+    if (h) hmap.assign(h, h + (size_t)nx * nz);
+    else hmap.clear();
+    return DCG_OK;
+  }
   int fail(int code, const char *msg) {
     err = msg;
     return code;
@@ -155,9 +166,38 @@ template <typename R> struct Physics {
   const dcg_params *P;
   R rdx, dt, dx;
   int gx, gy, gz;
+  // terrain heightmap (extension, dcg_set_heightmap): nx*nz texels, x fastest
+  const float *hm = nullptr;
+  int hm_nx = 0, hm_nz = 0;
+  R hm_sx = 0, hm_sz = 0;  // texels per finest cell
+
+  // Bilinear sample at (x, z), texel centres at (i + 0.5) / hm_sx, edge
+  // texels extended; the coordinate is clamped to [-1, n] first (fmax/fmin:
+  // a NaN coordinate becomes -1).
+  R heightmap_sample(R x, R z) const {
+    const R u = std::fmin(std::fmax(x * hm_sx - (R)0.5f, (R)-1), (R)hm_nx);
+    const R v = std::fmin(std::fmax(z * hm_sz - (R)0.5f, (R)-1), (R)hm_nz);
+    const R iu = std::floor(u), iv = std::floor(v);
+    const R fu = u - iu, fv = v - iv;
+    const int i0 = std::min(std::max((int)iu, 0), hm_nx - 1), i1 = std::min(std::max((int)iu + 1, 0), hm_nx - 1);
+    const int k0 = std::min(std::max((int)iv, 0), hm_nz - 1), k1 = std::min(std::max((int)iv + 1, 0), hm_nz - 1);
+    const R h00 = (R)hm[(size_t)k0 * hm_nx + i0], h10 = (R)hm[(size_t)k0 * hm_nx + i1];
+    const R h01 = (R)hm[(size_t)k1 * hm_nx + i0], h11 = (R)hm[(size_t)k1 * hm_nx + i1];
+    const R a = h00 + (h10 - h00) * fu;
+    const R b = h01 + (h11 - h01) * fu;
+    return a + (b - a) * fv;
+  }
+  void set_heightmap(const std::vector<float> &m, int nx, int nz) {
+    hm = m.empty() ? nullptr : m.data();
+    hm_nx = hm ? nx : 0;
+    hm_nz = hm ? nz : 0;
+    hm_sx = hm ? (R)nx / (R)gx : (R)0;
+    hm_sz = hm ? (R)nz / (R)gz : (R)0;
+  }
 
   // sphereSDF (src/sdf.cuh:8-20) and the terrain extension y - h(x, z).
   R terrain_height(R x, R z) const {
+    if (hm) return (R)P->terrain_base_height + (R)P->terrain_amplitude * heightmap_sample(x, z);
     R sum = 0, amp = 1, norm = 0, f = (R)P->terrain_frequency;
     for (int o = 0; o < P->terrain_octaves; o++) {
       const R u = x * f, v = z * f;
@@ -550,6 +590,12 @@ template <typename R> struct DC : Base {
     if (n <= 0) return fail(DCG_E_INVALID, "created with emission_n = 0");
     emis.assign(src, src + (size_t)n * n * n);
     return DCG_OK;
+  }
+  int set_heightmap(const float *h, int nx, int nz) override {
+    const int rc = store_heightmap(h, nx, nz);
+    if (rc) return rc;
+    ph.set_heightmap(hmap, nx, nz);
+    return reset();
   }
 
   R rdx() const { return ph.rdx; }
@@ -1762,6 +1808,12 @@ template <typename R> struct UG : Base {
     emis.assign(src, src + (size_t)n * n * n);
     return DCG_OK;
   }
+  int set_heightmap(const float *h, int nx, int nz) override {
+    const int rc = store_heightmap(h, nx, nz);
+    if (rc) return rc;
+    ph.set_heightmap(hmap, nx, nz);
+    return reset();
+  }
   std::vector<R> q[3], v[3], w, p, pt, dv, tv[3], tq[3];
 
   // mipmapCells / mipmapIdx (src/utils/grid_math.cuh:24-52)
@@ -2371,6 +2423,9 @@ int dcgo_get_scores(dcgo_sim *s, float *subblock, float *block) {
 }
 int dcgo_set_emission(dcgo_sim *s, const double *src) {
   return s && src ? s->impl->set_emission(src) : DCG_E_INVALID;
+}
+int dcgo_set_heightmap(dcgo_sim *s, const float *heights, int32_t nx, int32_t nz) {
+  return s ? s->impl->set_heightmap(heights, nx, nz) : DCG_E_INVALID;
 }
 int dcgo_get_stats(dcgo_sim *s, dcg_stats *st) { return s && st ? s->impl->stats(st) : DCG_E_INVALID; }
 int dcgo_render(dcgo_sim *s, const dcg_render_params *rp, double *rgba) {

@@ -72,6 +72,9 @@ int dcgo_adapt_replay(dcgo_sim *s, const int64_t *moves, int64_t n_moves,
 int dcgo_get_scores(dcgo_sim *s, float *subblock, float *block);
 int dcgo_get_stats(dcgo_sim *s, dcg_stats *st);
 int dcgo_set_emission(dcgo_sim *s, const double *src);
+/* dcg_set_heightmap: terrain from nx*nz heights (x fastest) instead of the
+ * value noise, then a reset; heights == NULL with nx = nz = 0 restores it */
+int dcgo_set_heightmap(dcgo_sim *s, const float *heights, int32_t nx, int32_t nz);
 /* the renderer's ray march on the CPU: width*height*4 values (RGBA) */
 int dcgo_render(dcgo_sim *s, const dcg_render_params *rp, double *rgba);
 /* FP64 host adjoint of the density path: transpose of the step that produced

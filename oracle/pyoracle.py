@@ -54,6 +54,7 @@ def lib():
         L.dcgo_get_scores.argtypes = [vp, vp, vp]
         L.dcgo_get_stats.argtypes = [vp, C.POINTER(capi.DcgStats)]
         L.dcgo_set_emission.argtypes = [vp, vp]
+        L.dcgo_set_heightmap.argtypes = [vp, vp, C.c_int32, C.c_int32]
         L.dcgo_render.argtypes = [vp, C.POINTER(capi.DcgRenderParams), vp]
         L.dcgo_adjoint_step.argtypes = [vp, vp, vp, vp]
         L.dcgo_adjoint_dense.argtypes = [vp, vp, vp]
@@ -120,6 +121,15 @@ class OracleSim:
     def set_emission(self, field):
         a = np.ascontiguousarray(field, dtype=np.float64).reshape(-1)
         self._chk(self.L.dcgo_set_emission(self.h, _ptr(a)), "set_emission")
+
+    def set_heightmap(self, heights):
+        """(nz, nx) float32 heights (x fastest), or None for the noise terrain;
+        resets the simulation."""
+        if heights is None:
+            self._chk(self.L.dcgo_set_heightmap(self.h, None, 0, 0), "set_heightmap")
+            return
+        a = np.ascontiguousarray(heights, dtype=np.float32)
+        self._chk(self.L.dcgo_set_heightmap(self.h, _ptr(a), a.shape[1], a.shape[0]), "set_heightmap")
 
     def get_field(self, field):
         fid = capi.FIELD_NAMES[field] if isinstance(field, str) else field
