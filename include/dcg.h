@@ -237,8 +237,8 @@ int dcg_set_emission(dcg_sim *sim, const float *field, int32_t where);
  * (solids must include DCG_SOLIDS_TERRAIN). The scene's solids are part of
  * the initial state, so the call resets the simulation. heights == NULL
  * (nx = nz = 0) returns to the noise terrain, also with a reset. The map is
- * an input, not state: dcg_save_state does not store it. Not for members of
- * a batch. */
+ * an input, not state: dcg_save_state does not store it, and dcg_set_mode
+ * recreates the handle without it. Not for members of a batch. */
 int dcg_set_heightmap(dcg_sim *sim, const float *heights, int32_t nx, int32_t nz, int32_t where);
 
 /* Adds seeded uniform noise in [-amplitude, amplitude] to every velocity
