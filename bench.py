@@ -212,21 +212,30 @@ def oracle_from_gpu(sim, p):
 
 def cpu_sample(sims, params, steps=1):
     """The FP64 oracle on the host cores, started from the GPU states: `steps`
-    steps of every simulation, active cell-steps per second."""
+    steps of every simulation on all host threads, then the next `steps` steps
+    of the same simulations on one thread; active cell-steps per second."""
     from oracle import pyoracle
     threads = os.cpu_count() or 1
-    pyoracle.set_threads(threads)
     orcs = [oracle_from_gpu(s, p) for s, p in zip(sims, params)]
-    cells = 0
-    t0 = time.perf_counter()
-    for o in orcs:
-        for _ in range(steps):
-            o.step(1)
-            cells += o.stats().active_cells
-    dt = time.perf_counter() - t0
-    return {"value": cells / dt, "unit": METRIC, "cores": threads, "kind": "port",
+
+    def rate(n_threads):
+        pyoracle.set_threads(n_threads)
+        cells = 0
+        t0 = time.perf_counter()
+        for o in orcs:
+            for _ in range(steps):
+                o.step(1)
+                cells += o.stats().active_cells
+        return cells / (time.perf_counter() - t0)
+
+    value = rate(threads)
+    one = rate(1)
+    pyoracle.set_threads(threads)
+    return {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
             "sample": f"{steps} step(s) of each of the {len(sims)} simulation(s) from the GPU's spun-up state "
-                      f"(same topology and fields), FP64 oracle, {threads} OpenMP threads"}
+                      f"(same topology and fields), FP64 oracle, {threads} OpenMP threads",
+            "single_core": {"value": one, "unit": METRIC, "cores": 1,
+                            "sample": f"the next {steps} step(s) of the same simulations on one thread"}}
 
 
 def density_error_fp16(params, steps=10):
