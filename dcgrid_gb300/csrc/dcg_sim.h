@@ -63,9 +63,9 @@ struct dcg_sim {
   bool use_graphs = true;
   long long kernels_per_step = 0;
   int ls_grid = 0;  // CTAs of the cooperative level solve (0 = per-sweep launches)
-  // level solve kernel and sweep ordering: 3 = the staged solve shared with
-  // batches (two-level barrier); the per-level kernel with 0 flat grid
-  // barrier, 1 neighbour epochs, 2 two-level barrier
+  // level solve kernel: 3 = the staged solve shared with batches (two-level
+  // barrier); 2 = the per-level kernel with a two-level barrier, taken when
+  // the staged solve's cooperative grid cannot be formed on the device
   int ls_epoch = 3;
   int ls_grid_staged = 0;  // CTAs of the staged solve
   // level solve of single simulations: pipelined staged sweeps, two tile buffers,
@@ -289,9 +289,6 @@ struct dcg_sim {
     }
     if (plan_only) return plan_tail_adaptive(B);
     ls_grid = level_solve_grid(sms);
-    if (const char *m = std::getenv("DCG_SOLVE_SYNC"))
-      ls_epoch = std::strcmp(m, "epoch") == 0 ? 1 : std::strcmp(m, "barrier") == 0 ? 0
-                 : std::strcmp(m, "tree") == 0 ? 2 : 3;
     ls_grid_staged = batch_solve_grid(sms, kSolveVariant, 0);
     if (ls_grid_staged <= 0 && ls_epoch == 3) ls_epoch = 2;
     if (P.emission_n > 0) {
