@@ -1,10 +1,10 @@
 """Terrain from a heightmap (dcg_set_heightmap).
 
 CPU (oracle): a constant map equals the flat noise terrain at the same
-height, bit for bit; the map shapes the solid (cells well below its lowest
-height are solid, well above its highest are fluid, both kinds and partial
-cells occur); removing the map returns to the noise terrain of a new handle;
-invalid shapes are refused.
+height, bit for bit, in the fields and in the rendered image; the map shapes
+the solid (cells well below its lowest height are solid, well above its
+highest are fluid, both kinds and partial cells occur); removing the map
+returns to the noise terrain of a new handle; invalid shapes are refused.
 GPU: the CUDA path against the oracle's float mirror, bit-exact, adaptive and
 uniform, after the reset the call performs and after steps.
 """
@@ -77,6 +77,26 @@ def test_removing_the_map_restores_the_noise_terrain():
     assert not np.array_equal(a.get_field("fluidity"), b.get_field("fluidity"))
     a.set_heightmap(None)
     same_fields(a, b)
+
+
+@pytest.mark.usefixtures("oracle_lib")
+def test_renderer_sees_the_map():
+    """The ray march shades the same SDF: a constant map renders exactly as
+    the flat noise terrain at that height, a shaped map differently."""
+    from tests.test_render_oracle import render_params
+    p = terrain_cloud()
+    p.terrain_base_height, p.terrain_amplitude = 10.0, 1.0
+    flat_map = orc(p)
+    flat_map.set_heightmap(np.full((5, 7), 5.0, np.float32))
+    q = terrain_cloud()
+    q.terrain_base_height, q.terrain_amplitude = 15.0, 0.0
+    flat_noise = orc(q)
+    rp = render_params(p, 32, 24, solids=1, shadows=1)
+    a, b = flat_map.render(rp), flat_noise.render(rp)
+    assert np.isfinite(a).all() and np.array_equal(a, b)
+    hills = orc(terrain_cloud())
+    hills.set_heightmap(scenarios.heightmap(48, 40, 1))
+    assert not np.array_equal(hills.render(rp), b)
 
 
 @pytest.mark.usefixtures("oracle_lib")
