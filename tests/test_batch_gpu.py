@@ -172,6 +172,34 @@ def test_batch_stats_equal_member_stats(persistent):
         assert st.mass == pytest.approx(one.mass, rel=1e-12) and st.residual == pytest.approx(one.residual, rel=1e-9)
 
 
+def test_headline_batch_full_size_members_equal_standalone():
+    """The benchmark's workload at its full size (16 plumes of 64^3 to 256^3,
+    2 or 3 levels, 100 sweeps per level, FP16 scalar storage, a 16^3 emission
+    map each): after 4 steps every member equals the same plume stepped as a
+    standalone simulation, bit for bit. A size-independent check at a size
+    where the oracle would take minutes; the members' parity with the oracle
+    is checked on small batches above."""
+    from dcgrid_gb300 import Batch, Simulation
+    params = scenarios.plume_batch(16, 0, sizes=(64, 96, 128, 192, 256), iters=100,
+                                   precision=capi.PRECISION_MIXED_FP16, em_n=16)
+    ems = [scenarios.emission_field(16, 100 + i) for i in range(16)]
+    b = Batch(params)
+    for i, m in enumerate(b):
+        m.set_emission(ems[i])
+        m.add_velocity_noise(11, 0.05)
+    b.step(4)
+    b.sync()
+    for i, p in enumerate(params):
+        s = Simulation(p)
+        s.set_emission(ems[i])
+        s.add_velocity_noise(11, 0.05)
+        s.step(4)
+        s.sync()
+        compare(b[i], s, p, f"member {i} ({p.gx}^3, {p.levels} levels)")
+        s.close()
+    b.close()
+
+
 def test_batch_emission_upload_equals_member_uploads():
     from dcgrid_gb300 import Batch
     params = scenarios.plume_batch(3, 4, sizes=(16, 32), iters=10, em_n=8)
