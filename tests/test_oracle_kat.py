@@ -7,6 +7,9 @@ scheme rather than from another implementation.
   uniform velocity advects itself unchanged, away from the walls.
 * The central-difference divergence (dcgrid_fluid.cu:174-230) of the linear
   field v = (a x, b y, c z) is rdx (a + b + c) in every interior cell.
+* Refinement fills a new block by trilinear (27/9/3/1) prolongation from
+  its parent's neighbourhood (dcgrid_adaptation.cu:92-143): exact for
+  linear density and velocity.
 * The leaf cells tile the domain exactly once at any level count, so
   sum_l leaf_cells[l] 8^l = gx gy gz, and the statistics' mass of a constant
   density (uniformgrid_structure.cu:41-42) is that density times the volume.
@@ -118,3 +121,30 @@ def test_leaf_cells_tile_the_domain_and_mass_is_density_times_volume(levels, blo
     u = make(capi.MODE_UNIFORM, 1)
     u.set_field("density", np.full(G ** 3, 0.25))
     assert u.stats().mass == 0.25 * G ** 3
+
+
+def test_refinement_prolongs_linear_fields_exactly():
+    """A replayed refinement of an interior subblock fills the new block by
+    the 27/9/3/1 stencil from the parent's neighbourhood
+    (dcgrid_adaptation.cu:92-143): trilinear interpolation at the child
+    centres, exact for linear fields."""
+    from oracle.pyoracle import OracleSim
+    p = params(2, 64 + 64)
+    p.init_adapt_passes = 0  # level 1 dense, level 0 empty: every leaf on level 1
+    s = OracleSim(p, precision="double")
+    assert list(s.get_topology()["load"]) == [0, 64]
+    X, valid = centres(s)
+    grads = {"density": [0.01, 0.02, -0.015], "vel_x": [0.3, -0.1, 0.05],
+             "vel_y": [-0.02, 0.04, 0.01], "vel_z": [0.0, 0.07, -0.03]}
+    for f, gvec in grads.items():
+        s.set_field(f, 2.0 + X @ np.array(gvec))
+    pos = s.get_topology()["pos"]
+    pb = int(np.nonzero((pos == [4, 4, 4, 1]).all(axis=1))[0][0])  # level-1 block at finest 8..15
+    s.adapt_replay(np.zeros((0, 2), np.int64), [(8 * pb + 7, 0)])  # its upper subblock -> block 0
+    pos = s.get_topology()["pos"]
+    assert list(pos[0]) == [12, 12, 12, 0]  # finest cells 12..15: every stencil inside the domain
+    X, _ = centres(s)
+    new = slice(0, 64)
+    for f, gvec in grads.items():
+        np.testing.assert_allclose(s.get_field(f)[new], (2.0 + X @ np.array(gvec))[new], rtol=0, atol=1e-12,
+                                   err_msg=f)
