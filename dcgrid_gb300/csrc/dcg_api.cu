@@ -571,7 +571,7 @@ void dcg_default_render_params(dcg_render_params *rp, int32_t width, int32_t hei
   const float sx = .5f, sy = 1.f, sz = .3f, sn = std::sqrt(sx * sx + sy * sy + sz * sz);
   rp->sun_dir[0] = sx / sn; rp->sun_dir[1] = sy / sn; rp->sun_dir[2] = sz / sn;
   rp->aa_samples = 1;              // src/data/sim_params.cpp:24
-  rp->channel = DCG_RENDER_FLUID;
+  rp->channel = DCG_RENDER_FLUID;  // the displayed frame's channel, simulation.cpp:153
   rp->shadows = 1;                 // cpp:21
   rp->solids = 1;                  // cpp:20
   rp->precise = 1;                 // cpp:22

@@ -412,8 +412,11 @@ typedef struct {
   float smoke_color[3], scene_color[3], floor_color[3];
   int32_t reserved[4];
 } dcg_render_params;
-/* the reference's defaults (src/data/sim_params.cpp:16-31) for a width*height
- * image, eye outside the domain looking along +z */
+/* the reference's render settings for a width*height image: colours and
+ * ambient from SimParams::defaultParams (src/data/sim_params.cpp:16-31);
+ * channel, AA samples, solids and shadows as in the frame it displays
+ * (src/simulation.cpp:153-156: Fluid, 1, on, on; defaultParams' Resolution
+ * channel is overwritten every frame); eye outside the domain looking along +z */
 void dcg_default_render_params(dcg_render_params *rp, int32_t width, int32_t height);
 int dcg_render(dcg_sim *sim, const dcg_render_params *rp, float *rgba, int32_t where);
 
