@@ -401,7 +401,10 @@ constexpr int LS_CACHE = 4;
 // `sweeps` Jacobi sweeps (ping-pong p -> p~ -> p, as k_dcgrid_jacobi/_inv).
 // Work split: CTA c owns the level's blocks 4*(r*grid + c) .. +3 in round r.
 // One grid barrier follows prolongation and the epoch reset; sweeps are then
-// ordered block by block through neighbour epochs instead of grid barriers.
+// separated by a flat (epoch_sync 0) or two-level (2) grid barrier, or ordered
+// block by block through neighbour epochs (1). The library uses this kernel
+// only where the staged solve (k_level_solve_batch) cannot form its
+// cooperative grid, with the two-level barrier.
 // The level's topology is fixed during the solve, so each thread resolves the
 // six neighbour cells of its (at most LS_CACHE) cells once and keeps them and
 // alpha*div in registers; a sweep is then six loads and one store per cell.
