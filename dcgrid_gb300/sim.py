@@ -85,6 +85,10 @@ def lib():
         L.dcg_batch_set_emission.argtypes = [vp, vp, C.c_int32]
         L.dcg_batch_last_error_string.argtypes = [vp]
         L.dcg_batch_last_error_string.restype = C.c_char_p
+        L.dcg_get_dense_noalloc.argtypes = [vp, C.c_int32, vp, C.c_int32]
+        L.dcg_plan_bytes.argtypes = [vp, C.c_int32, C.POINTER(C.c_int64)]
+        L.dcg_blocks_for_budget.argtypes = [vp, C.c_int64, C.POINTER(C.c_int64)]
+        L.dcg_check_div6.argtypes = [C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]
         for name in ["dcg_sizeof_params", "dcg_sizeof_info", "dcg_sizeof_stats", "dcg_sizeof_tuning",
                      "dcg_sizeof_render_params"]:
             getattr(L, name).restype = C.c_size_t

@@ -67,3 +67,26 @@ def test_tuning_dict_round_trip():
     d = capi.tuning_to_dict(t)
     back = capi.tuning_to_dict(capi.tuning_from_dict(d))
     assert back == d
+
+
+def declared_arities():
+    """{function: parameter count} from include/dcg.h."""
+    txt = open(os.path.join(ROOT, "include", "dcg.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    out = {}
+    for name, args in re.findall(r"\b(dcg_[a-z0-9_]+)\s*\(([^()]*)\)\s*;", txt):
+        args = args.strip()
+        out[name] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_python_bindings_match_the_header_arities(dcg_lib):
+    arity = declared_arities()
+    assert len(arity) >= 60
+    checked = 0
+    for name, n in arity.items():
+        fn = getattr(dcg_lib, name)
+        if fn.argtypes is not None:
+            assert len(fn.argtypes) == n, f"{name}: header has {n} parameters, binding {len(fn.argtypes)}"
+            checked += 1
+    assert checked == len(arity)  # every declared function has its argument types bound
