@@ -16,7 +16,6 @@ import pytest
 
 from dcgrid_gb300 import capi
 from tests import scenarios
-from tests.test_parity_gpu import compare
 
 pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("cuda_ok", "dcg_lib", "oracle_lib")]
 

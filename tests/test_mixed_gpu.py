@@ -11,7 +11,7 @@ import pytest
 
 from dcgrid_gb300 import capi
 from tests import scenarios
-from tests.test_parity_gpu import compare, field_names, gpu, orc
+from tests.test_parity_gpu import compare, gpu, orc
 
 pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("cuda_ok", "dcg_lib", "oracle_lib")]
 
