@@ -148,3 +148,28 @@ def test_refinement_prolongs_linear_fields_exactly():
     for f, gvec in grads.items():
         np.testing.assert_allclose(s.get_field(f)[new], (2.0 + X @ np.array(gvec))[new], rtol=0, atol=1e-12,
                                    err_msg=f)
+
+
+def test_linear_shift_holds_for_random_velocities_and_gradients():
+    """The exact shift of a linear scalar for random uniform velocities (up to
+    0.9 cells per step in each direction) and random gradients."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    comp = st.floats(-0.9, 0.9, allow_nan=False)
+    slope = st.floats(-0.05, 0.05, allow_nan=False)
+    s = make(capi.MODE_UNIFORM, 1)
+    X, valid = centres(s)
+    inner = interior(X, valid, 3)
+
+    @hyp.settings(max_examples=25, deadline=None, database=None)
+    @hyp.given(st.tuples(comp, comp, comp), st.tuples(slope, slope, slope))
+    def check(v, grad):
+        v, grad = np.array(v), np.array(grad)
+        for k, f in enumerate(["vel_x", "vel_y", "vel_z"]):
+            s.set_field(f, np.full(len(X), v[k]))
+        rho = 1.0 + X @ grad
+        s.set_field("density", rho)
+        s.advect_scalars()
+        np.testing.assert_allclose(s.get_field("density")[inner], (rho - grad @ v)[inner], rtol=0, atol=1e-12)
+
+    check()
