@@ -1,7 +1,8 @@
-"""The C ABI from plain C: include/dcg.h compiles as C99 under -Wall -Wextra
--pedantic -Werror, and a C program linked against libdcgrid_gb300.so runs the
-calls that need no GPU (defaults, struct sizes, the memory planner, null-handle
-rejection) with the same results as the Python mirror."""
+"""The C ABI from plain C and C++: include/dcg.h compiles as C99 and as C++11
+under -Wall -Wextra -pedantic -Werror, and a program linked against
+libdcgrid_gb300.so runs the calls that need no GPU (defaults, struct sizes,
+the memory planner, null-handle rejection) with the same results as the
+Python mirror."""
 import ctypes as C
 import os
 import shutil
@@ -75,3 +76,20 @@ def test_defaults_and_planner_match_the_python_mirror(c_program, dcg_lib):
 
 def test_null_handles_from_c(c_program):
     assert [int(x) for x in c_program["null"].split()] == [capi.DCG_E_INVALID, capi.DCG_E_INVALID]
+
+
+def test_header_compiles_as_cpp(tmp_path, dcg_lib):
+    """The reference's side is C++: the header also compiles as C++11 under
+    -pedantic -Werror, and its extern "C" names link."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "prog.cpp"
+    src.write_text(PROGRAM.replace("#include <stdio.h>", "#include <cstdio>"))
+    libdir = os.path.join(ROOT, "dcgrid_gb300")
+    cmd = [cxx, "-std=c++11", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+           str(src), "-o", str(tmp_path / "prog"), "-L", libdir, "-ldcgrid_gb300", f"-Wl,-rpath,{libdir}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(tmp_path / "prog")], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "plan 0 " in r.stdout, r.stdout + r.stderr
