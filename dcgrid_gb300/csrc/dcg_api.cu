@@ -24,6 +24,22 @@ static int member_refused(dcg_sim *s) {
   return s->batch_member ? s->fail(DCG_E_INVALID, "member of a batch: use the dcg_batch_* calls") : DCG_OK;
 }
 
+// Status of a nonzero device error word: DCG_E_NAN when the only bit is the
+// non-finite-value flag, else DCG_E_DEVICE (a bounded wait gave up, a block
+// budget ran out, a lookup failed).
+static int device_error_status(uint32_t e) { return e == DCG_DEVERR_NAN ? DCG_E_NAN : DCG_E_DEVICE; }
+static std::string device_error_text(uint32_t e) {
+  std::string t = "device error word 0x";
+  char buf[16];
+  std::snprintf(buf, sizeof buf, "%x", e);
+  t += buf;
+  if (e & DCG_DEVERR_BUDGET) t += ", a refinement found its level full";
+  if (e & DCG_DEVERR_LOOKUP) t += ", a block lookup failed";
+  if (e & DCG_DEVERR_NAN) t += ", a non-finite value in a leaf cell";
+  if (e & DCG_DEVERR_TIMEOUT) t += ", a bounded device-side wait gave up";
+  return t;
+}
+
 extern "C" {
 
 void dcg_default_params(dcg_params *p, int32_t gx, int32_t gy, int32_t gz, int64_t max_blocks) {
@@ -212,11 +228,7 @@ int dcg_sync(dcg_sim *s) {
   if (s->mode == DCG_MODE_ADAPTIVE) {
     uint32_t e = 0;
     if ((rc = s->cuda(cudaMemcpy(&e, s->D.err, 4, cudaMemcpyDeviceToHost), "err word"))) return rc;
-    if (e) {
-      char buf[64];
-      std::snprintf(buf, sizeof buf, "device error word 0x%x", e);
-      return s->fail(DCG_E_DEVICE, buf);
-    }
+    if (e) return s->fail(device_error_status(e), device_error_text(e));
   }
   return DCG_OK;
 }
@@ -429,6 +441,7 @@ int dcg_get_stats(dcg_sim *s, dcg_stats *st) {
   st->steps = s->steps;
   int rc;
   double red[32];
+  bool nan_seen = false;
   if (s->mode == DCG_MODE_ADAPTIVE) {
     launch_stats(s->D, s->stream);
     long long ctr[C_COUNT], load[MAXL];
@@ -448,6 +461,7 @@ int dcg_get_stats(dcg_sim *s, dcg_stats *st) {
     st->moved_blocks = ctr[C_MOVES];
     st->refined_subblocks = ctr[C_REFINES];
     st->device_error = e;
+    nan_seen = (e & DCG_DEVERR_NAN) != 0;
     if (s->P.defect_passes > 0) {
       const int K = s->P.defect_passes;
       std::vector<double> dn(2 * (K + 1));
@@ -464,6 +478,8 @@ int dcg_get_stats(dcg_sim *s, dcg_stats *st) {
     st->leaf_cells[0] = s->U.nc;
     st->active_cells = s->U.nc;
   }
+  // the statistics are filled either way; the status reports a non-finite value
+  if (nan_seen) return s->fail(DCG_E_NAN, device_error_text(st->device_error));
   return DCG_OK;
 }
 
@@ -555,6 +571,19 @@ int dcg_check_div6(uint64_t *mismatches, uint32_t *first) {
   *mismatches = h[0];
   *first = (uint32_t)h[1];
   return DCG_OK;
+}
+
+int dcg_check_barrier_timeout(dcg_sim *s, uint32_t poll_limit) {
+  if (bad(s) || s->mode != DCG_MODE_ADAPTIVE || poll_limit == 0 || poll_limit > (1u << 20)) return DCG_E_INVALID;
+  if (member_refused(s)) return DCG_E_INVALID;
+  const size_t bar_bytes = 4 * (64 + 32 * 18);
+  int rc;
+  if ((rc = s->cuda(cudaMemsetAsync(s->D.bar, 0, bar_bytes, s->stream), "barrier check"))) return rc;
+  if ((rc = s->cuda((cudaError_t)launch_barrier_probe(s->D.bar, s->D.err, poll_limit, 2, s->stream),
+                    "barrier check launch")))
+    return rc;
+  // the waiting CTA's arrival stays counted: clear the words for the next solve
+  return s->cuda(cudaMemsetAsync(s->D.bar, 0, bar_bytes, s->stream), "barrier check");
 }
 
 size_t dcg_sizeof_params(void) { return sizeof(dcg_params); }
@@ -777,12 +806,12 @@ int dcg_adjoint_dense(dcg_sim *s, const float *lam_dense, float *lam_cells) {
 //
 // dcg_get_dense stages the resampled volume in a device buffer that it
 // cudaMallocs on its first call. Some callers cannot allocate at that point:
-// code running while a stream is being captured into a CUDA graph (an
-// allocation there breaks or invalidates the capture), hosts that hand the
-// library a fixed device-memory budget up front, and real-time loops that must
-// not hit the allocator's synchronisation. dcg_get_dense_noalloc runs the same
-// resampling kernel but stages through the fixed array below, so the call
-// itself allocates nothing.
+// hosts that hand the library a fixed device-memory budget up front and
+// account for every byte it may take, and real-time loops that must not hit
+// cudaMalloc's implicit device synchronisation in the middle of a frame.
+// dcg_get_dense_noalloc runs the same resampling kernel but stages through the
+// fixed array below, so the call itself allocates nothing. Like dcg_get_dense
+// it waits for the handle's stream before it returns.
 //
 // The array is a file-scope __device__ variable: every GPU that loads this
 // library holds its 4 MiB until the process exits. In host code its name is

@@ -89,6 +89,7 @@ def lib():
         L.dcg_plan_bytes.argtypes = [vp, C.c_int32, C.POINTER(C.c_int64)]
         L.dcg_blocks_for_budget.argtypes = [vp, C.c_int64, C.POINTER(C.c_int64)]
         L.dcg_check_div6.argtypes = [C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]
+        L.dcg_check_barrier_timeout.argtypes = [vp, C.c_uint32]
         for name in ["dcg_sizeof_params", "dcg_sizeof_info", "dcg_sizeof_stats", "dcg_sizeof_tuning",
                      "dcg_sizeof_render_params"]:
             getattr(L, name).restype = C.c_size_t
@@ -281,6 +282,18 @@ class Simulation:
         a = np.empty(p.gx * p.gy * p.gz, np.float32)
         self._chk(self.L.dcg_get_dense(self.h, _field_id(field), _ptr(a), capi.HOST), "get_dense")
         return a.reshape(p.gz, p.gy, p.gx)
+
+    def get_dense_noalloc(self, field, out=None):
+        """get_dense without a device allocation (dcg_get_dense_noalloc): for
+        hosts that cap the library's device memory up front. Domains above 2^20
+        finest cells are refused. `out`: a host array or CUDA tensor of
+        gx*gy*gz float32 (returned as given), else a new (gz, gy, gx) array."""
+        p = self.params
+        n = p.gx * p.gy * p.gz
+        a = np.empty(n, np.float32) if out is None else out
+        ptr, where = _buf(a, n, np.float32, "get_dense_noalloc", writable=True)
+        self._chk(self.L.dcg_get_dense_noalloc(self.h, _field_id(field), ptr, where), "get_dense_noalloc")
+        return a.reshape(p.gz, p.gy, p.gx) if out is None else a
 
     def get_topology(self):
         B = int(self.info.max_blocks)

@@ -220,7 +220,9 @@ int dcg_adapt(dcg_sim *sim);               /* adaptTopology                     
 int dcg_project(dcg_sim *sim);             /* cascadic Jacobi projection             */
 int dcg_project_local(dcg_sim *sim);       /* projectLocal                           */
 int dcg_advect_scalars(dcg_sim *sim);      /* advectDensity (+ temperature, vapor, sources) */
-int dcg_sync(dcg_sim *sim);                /* wait for the handle's stream; read device error word */
+int dcg_sync(dcg_sim *sim);                /* wait for the handle's stream; read the device error
+                                               word: DCG_E_NAN when it holds only DCG_DEVERR_NAN,
+                                               DCG_E_DEVICE for any other bit */
 
 /* Sets the emission field (emission_n^3 floats, x fastest) from host or
  * device memory. The copy is ordered on the handle's stream before later
@@ -257,15 +259,17 @@ int dcg_set_field(dcg_sim *sim, int32_t field, const float *src, int32_t where);
 int dcg_get_dense(dcg_sim *sim, int32_t field, float *dst, int32_t where);
 /* Same result as dcg_get_dense, but the call allocates no device memory.
  * No counterpart in the reference. dcg_get_dense cudaMallocs a staging buffer
- * on its first call; callers that cannot allocate at that moment - code that
- * runs while a stream is being captured into a CUDA graph, hosts that give the
- * library a fixed memory budget up front, loops that must not wait on the
- * allocator - use this variant. It stages through a fixed device array of
- * 2^20 floats (4 MiB, held by every GPU that loads the library until exit),
- * so domains of more than 2^20 finest cells are rejected with DCG_E_INVALID.
- * The first call on a device looks the array up (cudaGetSymbolAddress), so
- * make that first call before any stream capture. All calls on a device share
- * the array: calls that overlap on the GPU (other streams or handles) race. */
+ * on its first call; callers that cannot allocate at that moment - hosts that
+ * give the library a fixed device-memory budget up front, real-time loops that
+ * must not take cudaMalloc's device-wide synchronisation mid-frame - use this
+ * variant. It stages through a fixed device array of 2^20 floats (4 MiB, held
+ * by every GPU that loads the library until exit), so domains of more than
+ * 2^20 finest cells are rejected with DCG_E_INVALID. The handle's device must
+ * be current, as for every other call. The first call on a device looks the
+ * array up (cudaGetSymbolAddress), so make that first call before any stream
+ * capture. All calls on a device share the array: calls that overlap on the
+ * GPU (other streams or handles) race. Like dcg_get_dense, the call waits for
+ * the handle's stream before it returns. */
 int dcg_get_dense_noalloc(dcg_sim *sim, int32_t field, float *dst, int32_t where);
 
 /* Block table, host buffers sized by dcg_info.max_blocks:
@@ -292,6 +296,10 @@ int dcg_get_apron(dcg_sim *sim, int64_t *dst);
 int dcg_get_last_adapt(dcg_sim *sim, int64_t *moves, int64_t *n_moves,
                        int64_t *refines, int64_t *n_refines);
 
+/* Runs the statistics pass (which also flags non-finite values: a NaN or
+ * infinity in a leaf cell's pressure, divergence, density or fluidity sets
+ * DCG_DEVERR_NAN) and fills *stats; returns DCG_E_NAN, with *stats filled,
+ * when the device error word holds DCG_DEVERR_NAN. */
 int dcg_get_stats(dcg_sim *sim, dcg_stats *stats);
 
 /* ---- extras without a counterpart in the reference -------------------- */
@@ -313,6 +321,15 @@ int dcg_launches_per_step(dcg_sim *sim, int64_t *n);
  * (NaNs compare equal), *first = the smallest such input's bit pattern
  * (0xFFFFFFFF when none). */
 int dcg_check_div6(uint64_t *mismatches, uint32_t *first);
+/* Self-check of the bounded device-side waits (no reference counterpart; the
+ * reference has no grid-wide waits). Launches, on the handle's stream, a
+ * two-CTA cooperative kernel in which one CTA never arrives at the grid
+ * barrier that the level solves use: the other gives up after poll_limit
+ * polls (1 .. 2^20; the solves use 2^22) and sets DCG_DEVERR_TIMEOUT in the
+ * handle's device error word, so the next dcg_sync returns DCG_E_DEVICE.
+ * Nothing hangs and the context stays usable; dcg_reset clears the word.
+ * Adaptive handles that are not batch members. */
+int dcg_check_barrier_timeout(dcg_sim *sim, uint32_t poll_limit);
 /* ---- batches: many independent adaptive simulations stepped together -----
  * No reference counterpart: the reference runs one simulation per process
  * (one global __constant__ parameter set, src/utils/sim_utils.h:5-6). A batch
@@ -357,7 +374,8 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out);
 int dcg_batch_destroy(dcg_batch *batch);
 int dcg_batch_reset(dcg_batch *batch);     /* every member as after creation */
 int dcg_batch_step(dcg_batch *batch, int32_t n);
-int dcg_batch_sync(dcg_batch *batch);      /* stream sync + every member's device error word */
+int dcg_batch_sync(dcg_batch *batch);      /* stream sync + every member's device error word
+                                               (DCG_E_NAN / DCG_E_DEVICE as for dcg_sync) */
 /* Borrowed handle of member i for field, stats, topology and emission access
  * (issued on the batch's stream). Stepping, stage calls, set_params,
  * set_stream, set_mode and destroy are refused on member handles. */
@@ -377,7 +395,8 @@ int dcg_batch_get_info(const dcg_batch *batch, int32_t *n, int64_t *device_bytes
  * memory. Equivalent to dcg_set_emission on each of those members. */
 int dcg_batch_set_emission(dcg_batch *batch, const float *maps, int32_t where);
 /* dcg_get_stats of every member (out: n entries), one launch per group of 16
- * members and one synchronisation */
+ * members and one synchronisation; DCG_E_NAN (entries filled) when a member's
+ * error word holds DCG_DEVERR_NAN */
 int dcg_batch_get_stats(dcg_batch *batch, dcg_stats *out);
 /* Times the pressure cascade of the current state (all rounds, the members'
  * jacobi_iters sweeps each) `reps` times; *bytes = algorithmic bytes of one
