@@ -301,7 +301,12 @@ def run_batch(args, ctx):
         return b, tune
 
     def batch_cells(b):
-        return sum(st.active_cells for st in b.stats())
+        sts = b.stats()  # raises on a non-finite value (DCG_E_NAN)
+        bad = [i for i, st in enumerate(sts) if st.device_error]
+        if bad:
+            raise RuntimeError(f"device error word set for members {bad}: "
+                               f"{[hex(sts[i].device_error) for i in bad]}")
+        return sum(st.active_cells for st in sts)
 
     # mixed-precision batch: the headline
     bm, tune_m = make_batch(capi.PRECISION_MIXED_FP16)
@@ -309,6 +314,7 @@ def run_batch(args, ctx):
     clocks.start()
     ms, cells = ctx.timed(args.steps, lambda: bm.step(1), lambda: batch_cells(bm))
     clk = clocks.stop(ctx.local)
+    bm.sync()  # raises when a device error word (timeout, budget, lookup, NaN) was set
     ms, cells = ctx.max_sum(ms, cells)
     value = cells / (ms * 1e-3)
     info = bm.info()
@@ -323,6 +329,7 @@ def run_batch(args, ctx):
     # FP32 batch (batching alone)
     bf, tune_f = make_batch(capi.PRECISION_FP32)
     ms_f, cells_f = ctx.timed(args.steps, lambda: bf.step(1), lambda: batch_cells(bf), "timed_fp32_batch")
+    bf.sync()
     ms_f, cells_f = ctx.max_sum(ms_f, cells_f)
     batched_fp32 = cells_f / (ms_f * 1e-3)
     bf.close()
@@ -343,8 +350,15 @@ def run_batch(args, ctx):
         for s in plain:
             s.step(1)
 
-    ms_p, cells_p = ctx.timed(args.steps, plain_step, lambda: sum(s.stats().active_cells for s in plain),
-                              "timed_plain_fp32")
+    def plain_cells():
+        sts = [s.stats() for s in plain]
+        if any(st.device_error for st in sts):
+            raise RuntimeError("device error word set in a plain FP32 simulation")
+        return sum(st.active_cells for st in sts)
+
+    ms_p, cells_p = ctx.timed(args.steps, plain_step, plain_cells, "timed_plain_fp32")
+    for s in plain:
+        s.sync()
     ms_p, cells_p = ctx.max_sum(ms_p, cells_p)
     plain_fp32 = cells_p / (ms_p * 1e-3)
     plain_launches = sum(s.launches_per_step() for s in plain)
@@ -364,6 +378,7 @@ def run_batch(args, ctx):
         e2e_cells += batch_cells(bm)
     torch.cuda.synchronize()
     e2e_ms, e2e_cells = ctx.max_sum((time.perf_counter() - t0) * 1e3, e2e_cells)
+    bm.sync()
     stats_bytes = C.sizeof(capi.DcgStats)
     e2e = {"value": e2e_cells / (e2e_ms * 1e-3), "unit": METRIC,
            "h2d_bytes_per_step": 4 * EM_N ** 3 * BATCH_N, "d2h_bytes_per_step": stats_bytes * BATCH_N,
@@ -383,12 +398,23 @@ def run_batch(args, ctx):
                 "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_cascade": solve_bytes,
                 "cascade_ms": solve_ms,
                 "note": "algorithmic bytes: 12 per allocated cell per sweep (p read, div read, p~ write); "
-                        "traffic: ncu dram bytes per cell-sweep of a smaller capture scaled to these cells"}
+                        "traffic: ncu dram bytes per cell-sweep of a smaller capture scaled to these cells; "
+                        "the cascade is timed back to back (L2 warm between repetitions), the steps with "
+                        "L2 flushed"}
+    # the whole step against the per-cell-step byte count of the path:
+    # 104 + (2k + 2) s_q + 12 N bytes per active cell-step (k scalars of s_q
+    # bytes, N sweeps per level)
+    kq = batch_params(0)[0].n_scalars
+    step_bytes = 104 + (2 * kq + 2) * 2 + 12 * ITERS
+    roofline["step_level"] = {"bytes_per_active_cell_step": step_bytes, "achieved": step_bytes * value / 1e9,
+                              "frac": step_bytes * value / 1e9 / peak, "unit": "GB/s",
+                              "note": f"k={kq} FP16 scalars (s_q=2), N={ITERS}: whole-step rate x bytes per "
+                                      "active cell-step, against the same peak"}
 
     members = [{"edge": p.gx, "levels": p.levels, "max_blocks": p.max_blocks} for p in batch_params(0)]
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ctx.world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp16 storage / fp32 compute",
             "data": "synthetic (seeded plume sources, emission maps, velocity noise)",
             "config": {"workload": f"batch of {BATCH_N} independent plumes, edges from {{64,96,128,192,256}} "
                                    f"(seed 0), 2-3 levels, {ITERS} Jacobi sweeps/level, FP16 scalar storage / "
@@ -431,6 +457,7 @@ def run_cloud(args, ctx):
     clocks.start()
     ms, cells = ctx.timed(args.steps, lambda: sim.step(1), lambda: sim.stats().active_cells)
     clk = clocks.stop(ctx.local)
+    sim.sync()  # raises when the device error word was set
     ms, cells = ctx.max_sum(ms, cells)
     value = cells / (ms * 1e-3)
     launches = sim.launches_per_step()
@@ -523,6 +550,7 @@ def run_large(args, ctx):
             clocks = Clocks(ctx.clock_path)
             clocks.start()
         ms, cells = ctx.timed(args.steps, lambda: s.step(1), lambda: s.stats().active_cells, "timed_" + name)
+        s.sync()
         if name == "fp16":
             clk = clocks.stop(ctx.local)
             launches = s.launches_per_step()
@@ -540,7 +568,7 @@ def run_large(args, ctx):
     v = out["fp16"]
     line = {"metric": METRIC, "value": v["value"], "unit": METRIC, "n_gpus": ctx.world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": v["ms_per_step"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp16 storage / fp32 compute",
             "data": "synthetic (seeded terrain, jittered heat source, velocity noise)",
             "config": {"workload": "fire plume, effective 512^3, 4 levels, block budget sized to 100 GB "
                                    f"(= the full {v['max_blocks']} blocks), crosswind 2 cells/step, "
@@ -572,19 +600,20 @@ def run_reference(args):
     if args.workload == "batch":
         params = batch_params(capi.PRECISION_FP32)
         ems = [member_emission(i) for i in range(BATCH_N)]
-        spin = 5
+        spin = BATCH_SPINUP
         workload = f"batch of {BATCH_N} independent plumes (same members as the GPU arm), FP64"
     else:
         params = [scenes.cloud256()]
         ems = [scenes.emission_field(EM_N, 1)]
-        spin = 10
+        spin = CLOUD_SPINUP
         workload = "adaptive cloud scene, effective 256^3, 3 levels, 40000 block budget, FP64"
+    # the GPU arm's spin-up: the same number of steps before the timed ones
     orcs = []
     for p, e in zip(params, ems):
         o = pyoracle.OracleSim(p, precision="double")
         o.set_emission(e)
         o.add_velocity_noise(0, 0.01)
-        o.step(spin + args.warmup)
+        o.step(spin + max(args.warmup, 3))
         orcs.append(o)
     cells = 0
     t0 = time.perf_counter()
@@ -593,15 +622,16 @@ def run_reference(args):
             o.step(1)
             cells += o.stats().active_cells
     dt = time.perf_counter() - t0
+    warm = max(args.warmup, 3)
     val = cells / dt
     line = {"metric": METRIC, "value": val, "unit": METRIC, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload, "spinup_steps": spin},
+            "config": {"workload": workload, "spinup_steps": spin, "warmup_steps": warm},
             "cpu_baseline": {"value": val, "unit": METRIC, "cores": threads, "kind": "port",
                              "sample": f"{args.steps} oracle steps of every simulation after {spin} spin-up and "
-                                       f"{args.warmup} warm-up steps, {threads} OpenMP threads"},
+                                       f"{warm} warm-up steps (the GPU arm's), {threads} OpenMP threads"},
             "e2e": {"value": val, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0

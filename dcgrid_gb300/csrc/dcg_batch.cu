@@ -322,14 +322,21 @@ struct dcg_batch {
       std::snprintf(buf, sizeof buf, "batch device error word 0x%x", e);
       return fail(DCG_E_DEVICE, buf);
     }
+    // a non-finite value (DCG_E_NAN) is reported only when no member has a
+    // more serious error
+    int nan_member = -1;
     for (int i = 0; i < n(); i++) {
       if ((rc = cuda(cudaMemcpy(&e, m[i]->D.err, 4, cudaMemcpyDeviceToHost), "err word"))) return rc;
-      if (e) {
+      if (e == DCG_DEVERR_NAN) {
+        if (nan_member < 0) nan_member = i;
+      } else if (e) {
         char buf[80];
         std::snprintf(buf, sizeof buf, "member %d device error word 0x%x", i, e);
         return fail(DCG_E_DEVICE, buf);
       }
     }
+    if (nan_member >= 0)
+      return fail(DCG_E_NAN, "member " + std::to_string(nan_member) + ": a non-finite value in a leaf cell");
     return DCG_OK;
   }
 
@@ -475,6 +482,10 @@ struct dcg_batch {
       st.refined_subblocks = x.ctr[C_REFINES];
       st.device_error = x.err;
     }
+    // the statistics are filled either way; the status reports a non-finite value
+    for (int i = 0; i < n(); i++)
+      if (out[i].device_error & DCG_DEVERR_NAN)
+        return fail(DCG_E_NAN, "member " + std::to_string(i) + ": a non-finite value in a leaf cell");
     return DCG_OK;
   }
 

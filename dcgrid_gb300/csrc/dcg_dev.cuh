@@ -126,14 +126,17 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
 __device__ __forceinline__ void st_relaxed(unsigned *p, unsigned v) {
   asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-// Bounded wait for the generation word to leave g: after 2^22 polls the CTA
-// records DCG_DEVERR_TIMEOUT (8) in the error word and gives up.
-__device__ __forceinline__ void barrier_wait(const unsigned *gen, unsigned g, uint32_t *errw) {
+// Bounded wait for the generation word to leave g: after `limit` polls (2^22
+// by default) the CTA records DCG_DEVERR_TIMEOUT (8) in the error word and
+// gives up.
+constexpr unsigned kPollLimit = 1u << 22;
+__device__ __forceinline__ void barrier_wait(const unsigned *gen, unsigned g, uint32_t *errw,
+                                             unsigned limit = kPollLimit) {
   volatile unsigned *err = errw;
   unsigned spins = 0;
   while (ld_acquire(gen) == g) {
     __nanosleep(32);
-    if (++spins > (1u << 22) || (*err & 8u)) {
+    if (++spins > limit || (*err & 8u)) {
       atomicOr(errw, 8u);
       break;
     }
@@ -177,7 +180,7 @@ __device__ inline void grid_barrier_tree(const Dev &D, unsigned nctas) { grid_ba
 // is bounded: after 2^22 polls the CTA records DCG_DEVERR_TIMEOUT (8) in the
 // error word and continues; once that bit is set every later barrier returns
 // at once, so a broken barrier costs one bounded wait and never hangs the GPU.
-__device__ inline void grid_barrier(uint32_t *bar, uint32_t *errw, unsigned nctas) {
+__device__ inline void grid_barrier(uint32_t *bar, uint32_t *errw, unsigned nctas, unsigned limit = kPollLimit) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned *err = errw;
@@ -187,7 +190,7 @@ __device__ inline void grid_barrier(uint32_t *bar, uint32_t *errw, unsigned ncta
         st_relaxed(bar, 0u);
         red_add_release(bar + 1, 1u);
       } else {
-        barrier_wait(bar + 1, g, errw);
+        barrier_wait(bar + 1, g, errw, limit);
       }
     }
   }
@@ -709,9 +712,13 @@ __device__ inline WarpStats stats_warp(const Dev &D, long long b, int c) {
   const int lev = stats_vals(D, b, c, r, m);
   return warp_sum_stats((double)r, (double)m, lev);
 }
-// adds warp totals into the member's reduction slots (lane 0)
+// adds warp totals into the member's reduction slots (lane 0). A non-finite
+// total means a leaf cell's pressure, divergence, density or fluidity is NaN
+// or infinite (a NaN anywhere in the velocity or the other scalars reaches
+// these within one step); it sets DCG_DEVERR_NAN (4) in the error word.
 __device__ inline void stats_flush(const Dev &D, double res, double mass, int lvl, double cnt) {
   if ((threadIdx.x & 31) == 0) {
+    if (!isfinite(res) || !isfinite(mass)) atomicOr(D.err, 4u);
     if (res != 0.0) atomicAdd(&D.red[0], res);
     if (mass != 0.0) atomicAdd(&D.red[1], mass);
     if (cnt != 0.0) atomicAdd(&D.red[2 + lvl], cnt);

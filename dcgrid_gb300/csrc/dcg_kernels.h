@@ -107,6 +107,7 @@ void launch_level_solve_batch(const SolveBatch &P, int round, int sweeps, int gr
 
 // self-check of the solver's division by six: bad[0] += mismatches, bad[1] = min mismatching input
 void launch_check_div6(unsigned long long *bad, int sms, cudaStream_t st);
+int launch_barrier_probe(uint32_t *bar, uint32_t *errw, unsigned limit, unsigned nctas, cudaStream_t st);
 
 // k_topology.cu
 void launch_init_blocks(const Dev &D, cudaStream_t st);

@@ -1707,6 +1707,22 @@ void launch_check_div6(unsigned long long *bad, int sms, cudaStream_t st) {
   k_check_div6<<<(unsigned)(sms > 0 ? sms * 8 : 1024), 256, 0, st>>>(bad);
 }
 
+// Self-check of the bounded grid-barrier wait: CTA `absent` leaves without
+// arriving, so the others wait on a generation word that nothing advances,
+// give up after `limit` polls and record DCG_DEVERR_TIMEOUT; the second
+// barrier must then return at once (the error bit short-cuts it).
+__global__ void __launch_bounds__(64) k_barrier_probe(uint32_t *bar, uint32_t *errw, unsigned limit,
+                                                      unsigned absent) {
+  if (blockIdx.x == absent) return;
+  grid_barrier(bar, errw, gridDim.x, limit);
+  grid_barrier(bar, errw, gridDim.x, limit);
+}
+int launch_barrier_probe(uint32_t *bar, uint32_t *errw, unsigned limit, unsigned nctas, cudaStream_t st) {
+  unsigned absent = nctas - 1;
+  void *args[] = {&bar, &errw, &limit, &absent};
+  return (int)cudaLaunchCooperativeKernel((const void *)k_barrier_probe, dim3(nctas), dim3(64), args, 0, st);
+}
+
 template <int TB, int STAGE> static unsigned persist_grid() {
   static unsigned g = 0;
   if (!g) {

@@ -8,12 +8,14 @@
 # Each cubin is one translation unit that #includes the reference .cu files by
 # path. -fmad=false keeps the reference's float operations unfused, so its
 # results are comparable bit for bit with the oracle's float mirror.
-# Needs the reference tree (REF, default /root/reference) and nvcc.
+# Usage: build_ref.sh <reference tree>   (or REF=<reference tree> build_ref.sh)
+# Needs the reference's sources and nvcc.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${REF:-/root/reference}"
+REF="${1:-${REF:-}}"
 OUT="$HERE/_ref"
 NVCC="${NVCC:-nvcc}"
+[ -n "$REF" ] || { echo "usage: $0 <reference tree>" >&2; exit 2; }
 [ -d "$REF/src/dcgrid" ] || { echo "reference tree not found at $REF" >&2; exit 2; }
 mkdir -p "$OUT"
 FLAGS=(-std=c++17 -O3 -fmad=false -diag-suppress 2506,177,550 -include "$HERE/ref_shim/ref_prelude.h"
