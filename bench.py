@@ -240,12 +240,12 @@ def cpu_sample(sims, params, steps=1):
 
 def density_error_fp16(params, steps=10):
     """Relative L2 density error of FP16 scalar storage against the FP64
-    oracle after `steps` steps of the smallest plume (both driven with the
+    oracle after `steps` steps of the largest plume (both driven with the
     GPU's adaptation decisions so they share one topology)."""
     from dcgrid_gb300 import Simulation, capi
     from oracle import pyoracle
     import numpy as np
-    i = min(range(len(params)), key=lambda k: params[k].max_blocks)
+    i = max(range(len(params)), key=lambda k: params[k].max_blocks)
     p = params[i]
     q = capi.params_from_dict(capi.params_to_dict(p))
     q.precision = capi.PRECISION_MIXED_FP16
@@ -284,11 +284,14 @@ def run_batch(args, ctx):
     torch = ctx.torch
     ems = [member_emission(i) for i in range(BATCH_N)]
 
-    def make_batch(prec):
-        b = Batch(batch_params(prec))
+    def make_batch(prec, defect_passes=0, tuning=None):
+        params = batch_params(prec)
+        for q in params:
+            q.defect_passes = defect_passes
+        b = Batch(params)
         b.set_stream(ctx.stream.cuda_stream)
-        if args.tuning:  # a given schedule (profiling runs), else autotuned
-            b.set_tuning(capi.tuning_from_dict(json.loads(args.tuning)))
+        if tuning or args.tuning:  # a given schedule (profiling runs), else autotuned
+            b.set_tuning(capi.tuning_from_dict(tuning or json.loads(args.tuning)))
             tune = capi.tuning_to_dict(b.get_tuning())
         else:
             tune = b.autotune(spinup_steps=5, reps=3)  # leaves the batch reset
@@ -333,6 +336,21 @@ def run_batch(args, ctx):
     ms_f, cells_f = ctx.max_sum(ms_f, cells_f)
     batched_fp32 = cells_f / (ms_f * 1e-3)
     bf.close()
+
+    # the mixed batch with one FP64 defect-correction pass after the cascade
+    # (FP64 residual and norms, the FP32 cascade on the residual, p += e), on
+    # the headline's schedule
+    bd, _ = make_batch(capi.PRECISION_MIXED_FP16, defect_passes=1, tuning=tune_m)
+    ms_d, cells_d = ctx.timed(args.steps, lambda: bd.step(1), lambda: batch_cells(bd), "timed_defect")
+    bd.sync()
+    ms_d, cells_d = ctx.max_sum(ms_d, cells_d)
+    rel = [tuple(st.defect_rel_residual) for st in bd.stats()]
+    defect = {"value": cells_d / (ms_d * 1e-3), "ms_per_step": ms_d / args.steps, "passes": 1,
+              "cost_ms_per_step": (ms_d - ms) / args.steps,
+              "rel_residual_before": max(r[0] for r in rel), "rel_residual_after": max(r[1] for r in rel),
+              "rel_residual_note": "FP64 ||div - A p|| / ||div|| over every level's equations, worst member, "
+                                   "before the first and after the last pass"}
+    bd.close()
 
     # plain FP32 path: 16 standalone simulations, one after another on one stream
     plain = []
@@ -428,13 +446,16 @@ def run_batch(args, ctx):
                            "plain_fp32_launches_per_step": plain_launches,
                            "batched_fp32": batched_fp32, "batched_fp32_tuning": tune_f,
                            "speedup_vs_plain_fp32": value / plain_fp32,
+                           "mixed_batch_fp64_defect_correction": defect,
                            "speedup_batching_fp32": batched_fp32 / plain_fp32},
             "gpu_launches": int(info["launches_per_step"] * args.steps),
             "launches_per_step": info["launches_per_step"], "roofline": roofline, "e2e": e2e}
     if clk:
         line["clocks"] = clk
     if ctx.rank == 0 and not args.no_cpu:
-        line["comparison"]["rel_err_fp16_vs_fp64"] = density_error_fp16(batch_params(capi.PRECISION_FP32))
+        # the largest member over the headline's horizon: spin-up, warm-up and timed steps
+        line["comparison"]["rel_err_fp16_vs_fp64"] = density_error_fp16(
+            batch_params(capi.PRECISION_FP32), BATCH_SPINUP + max(args.warmup, 3) + args.steps)
         line["cpu_baseline"] = cpu_sample(list(bm), batch_params(capi.PRECISION_FP32), 1)
     bm.close()
     return line

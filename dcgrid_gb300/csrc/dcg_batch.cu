@@ -27,6 +27,14 @@ struct dcg_batch {
   std::vector<void *> allocs;
   size_t bytes = 0;
   float *p_arena = nullptr, *pt_arena = nullptr, *div_arena = nullptr;
+  // FP64 defect correction (every member the same number of passes): the
+  // correction e, its ping-pong plane and the residual, as arenas laid out like
+  // p; the members' norms, 2 (passes + 1) doubles each
+  int dpass = 0;
+  float *e_arena = nullptr, *et_arena = nullptr, *rr_arena = nullptr;
+  double *dnorm_arena = nullptr;
+  // planes the cascade runs on: 0 = p, p~, div; 1 = e, e~, r (the correction)
+  int planes = 0;
   uint32_t *binfo = nullptr;  // block descriptions of a cascade round, 13 words per block
   uint32_t *bar = nullptr, *errw = nullptr;
   // concurrent cascades (solve_barrier bit 2): members with two different level
@@ -37,6 +45,7 @@ struct dcg_batch {
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<unsigned long long> arena_off;
+  unsigned long long arena_cells = 0;
   float *emis_arena = nullptr;  // members' emission maps, consecutive in member order
   size_t emis_floats = 0;
   int maxtop = 0, iters = 0;
@@ -147,6 +156,50 @@ struct dcg_batch {
         launch_restrict_batch(P, stream);
       }
   }
+  // the arenas of the planes the cascade runs on; with the correction planes,
+  // the members' descriptors name them too (the prolongation and the cached
+  // alpha * div read them through the descriptor)
+  void bind_planes(SolveBatch &P) const {
+    if (planes == 0) {
+      P.p = p_arena;
+      P.pt = pt_arena;
+      P.div = div_arena;
+      return;
+    }
+    P.p = e_arena;
+    P.pt = et_arena;
+    P.div = rr_arena;
+    for (int i = 0; i < P.n; i++) {
+      P.d[i].p = P.d[i].e;
+      P.d[i].pt = P.d[i].et;
+      P.d[i].div = P.d[i].rr;
+    }
+  }
+  // FP64 defect correction after the cascade (dcg_sim::defect_correct for
+  // every member): per pass the FP64 residual and norms, the cascade on the
+  // residual into e, and p += e; a last residual measures the result
+  void defect_correct() {
+    cudaMemsetAsync(dnorm_arena, 0, sizeof(double) * 2 * (dpass + 1) * n(), stream);
+    for (int k = 0; k <= dpass; k++) {
+      for (int g = 0; g < groups(); g++) {
+        CellBatch P{};
+        P.n = std::min(BMAX, n() - g * BMAX);
+        for (int i = 0; i < P.n; i++) P.d[i] = m[g * BMAX + i]->D;
+        launch_defect_batch(0, P, k, stream);
+      }
+      if (k == dpass) break;
+      cudaMemsetAsync(e_arena, 0, (size_t)arena_cells * sizeof(float), stream);
+      planes = 1;
+      solve_tuned();
+      planes = 0;
+      for (int g = 0; g < groups(); g++) {
+        CellBatch P{};
+        P.n = std::min(BMAX, n() - g * BMAX);
+        for (int i = 0; i < P.n; i++) P.d[i] = m[g * BMAX + i]->D;
+        launch_defect_batch(1, P, k, stream);
+      }
+    }
+  }
   // the cascade with the tuned schedule of each round
   bool can_split() const { return n() <= BMAX && !lgroup[0].empty() && !lgroup[1].empty() && aux; }
   // one member group's whole cascade (all its members have the same level count)
@@ -158,9 +211,6 @@ struct dcg_batch {
       P.n = (int)mem.size();
       P.maxtop = top;
       P.prolong = 1;
-      P.p = p_arena;
-      P.pt = pt_arena;
-      P.div = div_arena;
       P.binfo = gi ? binfo2 : binfo;
       P.bar = gi ? bar2 : bar;
       P.err = errw;
@@ -168,6 +218,7 @@ struct dcg_batch {
         P.d[i] = m[mem[i]]->D;
         P.arena[i] = arena_off[mem[i]];
       }
+      bind_planes(P);
       launch_level_solve_batch(P, round, iters, grid, cache, tree & 1, st);
     }
   }
@@ -208,9 +259,6 @@ struct dcg_batch {
         P.n = std::min(BMAX, n() - g * BMAX);
         P.maxtop = maxtop;
         P.prolong = 1;
-        P.p = p_arena;
-        P.pt = pt_arena;
-        P.div = div_arena;
         P.binfo = binfo;
         P.bar = bar;
         P.err = errw;
@@ -218,6 +266,7 @@ struct dcg_batch {
           P.d[i] = m[g * BMAX + i]->D;
           P.arena[i] = arena_off[g * BMAX + i];
         }
+        bind_planes(P);
         launch_level_solve_batch(P, round, iters, grid, cache, tree, stream);  // bit 1: alignment
       }
     }
@@ -255,11 +304,49 @@ struct dcg_batch {
     cells(2);  // divergence
     restrict_fields(2);
     solve_tuned();
+    if (dpass > 0) defect_correct();
     cells(3);  // apply pressure
     restrict_fields(0);
     cells(1);  // advect scalars (+ sources, emission)
     flip_q();
     restrict_fields(1);
+  }
+
+  // One step as step_once() without the graph, with CUDA events between the
+  // stages: ms[0] velocity advection (+ its restriction), [1] adaptation,
+  // [2] divergence (+ restriction), [3] pressure cascade (+ defect
+  // correction), [4] pressure application (+ restriction), [5] scalar
+  // advection (+ restriction), [6] the whole step.
+  int profile_step(float *ms) {
+    cudaEvent_t ev[7];
+    for (auto &e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], stream);
+    cells(0);
+    flip_v();
+    restrict_fields(0);
+    cudaEventRecord(ev[1], stream);
+    adapt();
+    cudaEventRecord(ev[2], stream);
+    cells(2);
+    restrict_fields(2);
+    cudaEventRecord(ev[3], stream);
+    solve_tuned();
+    if (dpass > 0) defect_correct();
+    cudaEventRecord(ev[4], stream);
+    cells(3);
+    restrict_fields(0);
+    cudaEventRecord(ev[5], stream);
+    cells(1);
+    flip_q();
+    restrict_fields(1);
+    cudaEventRecord(ev[6], stream);
+    int rc = cuda(cudaEventSynchronize(ev[6]), "profile step");
+    for (int k = 0; k < 6 && !rc; k++) cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]);
+    if (!rc) cudaEventElapsedTime(&ms[6], ev[0], ev[6]);
+    for (auto &e : ev) cudaEventDestroy(e);
+    for (dcg_sim *s : m) s->steps++;
+    if (rc) return rc;
+    return cuda(cudaGetLastError(), "profile step");
   }
 
   int step(int count) {
@@ -481,6 +568,11 @@ struct dcg_batch {
       st.moved_blocks = x.ctr[C_MOVES];
       st.refined_subblocks = x.ctr[C_REFINES];
       st.device_error = x.err;
+      if (dpass > 0) {
+        auto rel = [](double r2, double b2) { return b2 > 0 ? std::sqrt(r2 / b2) : 0.0; };
+        st.defect_rel_residual[0] = rel(x.dn[0], x.dn[1]);
+        st.defect_rel_residual[1] = rel(x.dn[2], x.dn[3]);
+      }
     }
     // the statistics are filled either way; the status reports a non-finite value
     for (int i = 0; i < n(); i++)
@@ -521,6 +613,7 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
   }
   b->own_stream = true;
   b->iters = params[0].jacobi_iters;
+  b->dpass = params[0].defect_passes;
   // arenas for p and p~: member i's planes start at cell arena_off[i]
   unsigned long long cells = 0;
   for (int i = 0; i < n; i++) {
@@ -528,9 +621,10 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
       delete b;
       return DCG_E_INVALID;  // one sweep schedule per batch
     }
-    if (params[i].max_blocks <= 0 || params[i].max_blocks >= (1ll << 28) || params[i].defect_passes != 0) {
+    if (params[i].max_blocks <= 0 || params[i].max_blocks >= (1ll << 28) || params[i].defect_passes != b->dpass ||
+        b->dpass < 0 || b->dpass > 16) {
       delete b;
-      return DCG_E_INVALID;  // defect correction runs on single simulations
+      return DCG_E_INVALID;  // one defect-correction schedule per batch
     }
     b->arena_off.push_back(cells);
     cells += (unsigned long long)params[i].max_blocks * BV;
@@ -539,7 +633,14 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
     delete b;
     return DCG_E_INVALID;  // arena cells are addressed with 32-bit indices
   }
+  b->arena_cells = cells;
   int rc;
+  if (b->dpass > 0 &&
+      ((rc = b->alloc(&b->e_arena, cells)) || (rc = b->alloc(&b->et_arena, cells)) ||
+       (rc = b->alloc(&b->rr_arena, cells)) || (rc = b->alloc(&b->dnorm_arena, 2 * (b->dpass + 1) * (size_t)n)))) {
+    delete b;
+    return rc;
+  }
   if ((rc = b->alloc(&b->p_arena, cells)) || (rc = b->alloc(&b->pt_arena, cells)) ||
       (rc = b->alloc(&b->div_arena, cells)) || (rc = b->alloc(&b->binfo, 13 * (cells / BV))) ||
       (rc = b->alloc(&b->bar, 64 + 32 * 18)) || (rc = b->alloc(&b->errw, 4))) {
@@ -573,6 +674,12 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
     s->ext_p = b->p_arena + b->arena_off[i];
     s->ext_pt = b->pt_arena + b->arena_off[i];
     s->ext_div = b->div_arena + b->arena_off[i];
+    if (b->dpass > 0) {
+      s->ext_rr = b->rr_arena + b->arena_off[i];
+      s->ext_e = b->e_arena + b->arena_off[i];
+      s->ext_et = b->et_arena + b->arena_off[i];
+      s->ext_dnorm = b->dnorm_arena + 2 * (size_t)(b->dpass + 1) * i;
+    }
     if (params[i].emission_n > 0) {
       s->ext_emis = b->emis_arena + emis_at;
       emis_at += (size_t)params[i].emission_n * params[i].emission_n * params[i].emission_n;
@@ -637,6 +744,10 @@ int dcg_batch_step(dcg_batch *b, int32_t n) {
   return b->step(n);
 }
 int dcg_batch_sync(dcg_batch *b) { return bad(b) ? DCG_E_INVALID : b->sync(); }
+int dcg_batch_profile_step(dcg_batch *b, float *stage_ms) {
+  if (bad(b) || !stage_ms) return DCG_E_INVALID;
+  return b->profile_step(stage_ms);
+}
 int dcg_batch_member(dcg_batch *b, int32_t i, dcg_sim **out) {
   if (bad(b) || !out || i < 0 || i >= b->n()) return DCG_E_INVALID;
   *out = b->m[i];

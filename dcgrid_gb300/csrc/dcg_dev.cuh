@@ -49,6 +49,7 @@ enum : int {
 
 struct Geom {
   int gx, gy, gz, levels, sparse, nq, ref_compat, mixed;
+  int dpass, gpad;  // FP64 defect-correction passes of the pressure solve
   long long B;
   long long full[MAXL], budget[MAXL], off[MAXL];
   int rx[MAXL], ry[MAXL], rz[MAXL];

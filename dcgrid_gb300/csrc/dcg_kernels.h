@@ -93,9 +93,12 @@ struct StatRecord {
   double red[32];
   long long ctr[C_COUNT], load[MAXL];
   uint32_t err, pad;
+  double dn[4];  // defect correction: ||r||^2, ||div||^2 before the first and after the last pass
 };
 void launch_stats_zero(const CellBatch &P, cudaStream_t st);
 void launch_stats_gather(const CellBatch &P, StatRecord *dst, cudaStream_t st);
+// batched defect correction: op 0 = FP64 residual of pass `pass`, op 1 = p += e
+void launch_defect_batch(int op, CellBatch &P, int pass, cudaStream_t st);
 // CTAs of the batched solve for a variant (cache depth 0, 3, 4, 8; 16, 18, 19: pipelined
 // staged sweeps with two tile buffers and cache depth 0, 2, 3; 32, 34, 35: three buffers;
 // 64, 66: two buffers, registers for 5 CTAs per SM)

@@ -75,6 +75,10 @@ struct dcg_sim {
   // steps the member (its own step and stage entry points are refused)
   float *ext_p = nullptr, *ext_pt = nullptr, *ext_div = nullptr;
   float *ext_emis = nullptr;  // batch members: the emission map is a slice of the batch's arena
+  // batch members with defect correction: residual, correction and its
+  // ping-pong plane are slices of the batch's arenas, the norms of its array
+  float *ext_rr = nullptr, *ext_e = nullptr, *ext_et = nullptr;
+  double *ext_dnorm = nullptr;
   bool batch_member = false;
 
   int fail(int code, const std::string &msg) {
@@ -239,6 +243,7 @@ struct dcg_sim {
     g.nq = P.n_scalars;
     g.ref_compat = P.ref_compat;
     g.mixed = P.precision == DCG_PRECISION_MIXED ? 1 : (P.precision == DCG_PRECISION_MIXED_FP16 ? 2 : 0);
+    g.dpass = P.defect_passes;
     fill_phys(D.ph);
 
     const size_t nc = (size_t)B * BV;
@@ -282,10 +287,17 @@ struct dcg_sim {
     if ((rc = alloc(&D.epoch, B))) return rc;
     if ((rc = alloc(&D.binfo, 13 * B))) return rc;
     if (P.defect_passes > 0) {
-      if ((rc = alloc(&D.rr, nc))) return rc;
-      if ((rc = alloc(&D.e, nc))) return rc;
-      if ((rc = alloc(&D.et, nc))) return rc;
-      if ((rc = alloc(&D.dnorm, 2 * (P.defect_passes + 1)))) return rc;
+      if (ext_rr) {
+        D.rr = ext_rr;
+        D.e = ext_e;
+        D.et = ext_et;
+        D.dnorm = ext_dnorm;
+      } else {
+        if ((rc = alloc(&D.rr, nc))) return rc;
+        if ((rc = alloc(&D.e, nc))) return rc;
+        if ((rc = alloc(&D.et, nc))) return rc;
+        if ((rc = alloc(&D.dnorm, 2 * (P.defect_passes + 1)))) return rc;
+      }
     }
     if (plan_only) return plan_tail_adaptive(B);
     ls_grid = level_solve_grid(sms);

@@ -504,8 +504,7 @@ __device__ __forceinline__ void apply_pressure_cell(const Dev &D, long long b, i
 // k_jacobi: sum6 p - 6 p = alpha div, alpha = (2^L dx)^2 in float as there),
 // r = div - (sum6 p - 6 p) / alpha, stored in FP32, with FP64 sums of r^2 and
 // div^2 reduced per warp into norms[0..1].
-__global__ void __launch_bounds__(256) k_defect_residual(Dev D, double *norms) {
-  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+__device__ __forceinline__ void defect_residual_cell(const Dev &D, long long b, double *norms) {
   double r2 = 0.0, b2 = 0.0;
   if (b < D.g.B) {
     const int4 bp = D.pos[b];
@@ -532,12 +531,17 @@ __global__ void __launch_bounds__(256) k_defect_residual(Dev D, double *norms) {
     atomicAdd(norms + 1, b2);
   }
 }
+__global__ void __launch_bounds__(256) k_defect_residual(Dev D, double *norms) {
+  defect_residual_cell(D, (long long)blockIdx.x * 4 + (threadIdx.x >> 6), norms);
+}
 // p += e on every allocated cell
-__global__ void __launch_bounds__(256) k_add_correction(Dev D) {
-  const long long b = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+__device__ __forceinline__ void add_correction_cell(const Dev &D, long long b) {
   if (b >= D.g.B || D.pos[b].w < 0) return;
   const long long cell = b * BV + (threadIdx.x & 63);
   D.p[cell] = D.p[cell] + D.e[cell];
+}
+__global__ void __launch_bounds__(256) k_add_correction(Dev D) {
+  add_correction_cell(D, (long long)blockIdx.x * 4 + (threadIdx.x >> 6));
 }
 
 // ------------------------------------------------------------ single-simulation kernels
@@ -725,10 +729,35 @@ __global__ void __launch_bounds__(128) k_stats_gather(const __grid_constant__ Ce
   if (t < C_COUNT) r.ctr[t] = __ldcg(D.ctr + t);
   if (t < MAXL) r.load[t] = __ldcg(D.load + t);
   if (t == 0) r.err = __ldcg(D.err);
+  // defect correction: the norms before the first and after the last pass
+  if (t < 4) r.dn[t] = D.g.dpass > 0 ? __ldcg(D.dnorm + (t < 2 ? t : 2 * D.g.dpass + t - 2)) : 0.0;
 }
 void launch_stats_zero(const CellBatch &P, cudaStream_t st) { k_stats_zero<<<P.n, 128, 0, st>>>(P); }
 void launch_stats_gather(const CellBatch &P, StatRecord *dst, cudaStream_t st) {
   k_stats_gather<<<P.n, 128, 0, st>>>(P, dst);
+}
+
+// Defect correction of a batch, one launch over all members (4 blocks per
+// CTA, P.end cumulative): OP 0 the FP64 residual of pass `pass` into each
+// member's rr and dnorm[2 pass], [2 pass + 1]; OP 1 p += e. The cell bodies are
+// the single simulation's.
+template <int OP>
+__global__ void __launch_bounds__(256) k_defect_batch(const __grid_constant__ CellBatch P, int pass) {
+  const int s = batch_member(P.end, P.n, blockIdx.x);
+  const Dev &D = P.d[s];
+  const long long b = ((long long)blockIdx.x - (s ? P.end[s - 1] : 0)) * 4 + (threadIdx.x >> 6);
+  if (OP == 0) defect_residual_cell(D, b, D.dnorm + 2 * pass);
+  else add_correction_cell(D, b);
+}
+void launch_defect_batch(int op, CellBatch &P, int pass, cudaStream_t st) {
+  long long acc = 0;
+  for (int m = 0; m < P.n; m++) {
+    acc += (P.d[m].g.B + 3) / 4;
+    P.end[m] = acc;
+  }
+  if (acc == 0) return;
+  if (op == 0) k_defect_batch<0><<<(unsigned)acc, 256, 0, st>>>(P, pass);
+  else k_defect_batch<1><<<(unsigned)acc, 256, 0, st>>>(P, pass);
 }
 
 __global__ void __launch_bounds__(256) k_restrict_batch(const __grid_constant__ RestrictBatch P) {

@@ -81,6 +81,7 @@ def lib():
         L.dcg_batch_set_tuning.argtypes = [vp, C.POINTER(capi.DcgTuning)]
         L.dcg_batch_get_info.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.dcg_batch_time_solve.argtypes = [vp, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_double)]
+        L.dcg_batch_profile_step.argtypes = [vp, vp]
         L.dcg_batch_get_stats.argtypes = [vp, vp]
         L.dcg_batch_set_emission.argtypes = [vp, vp, C.c_int32]
         L.dcg_batch_last_error_string.argtypes = [vp]
@@ -631,6 +632,15 @@ class Batch:
         arr = (capi.DcgStats * len(self.members))()
         self._chk(self.L.dcg_batch_get_stats(self.h, C.cast(arr, C.c_void_p)), "stats")
         return list(arr)
+
+    STAGES = ("advect_velocity", "adapt", "divergence", "cascade", "apply_pressure", "advect_scalars", "step")
+
+    def profile_step(self):
+        """One step outside the step graph, timed per stage (dcg_batch_profile_step):
+        a dict of milliseconds per stage and for the whole step."""
+        ms = (C.c_float * 7)()
+        self._chk(self.L.dcg_batch_profile_step(self.h, C.cast(ms, C.c_void_p)), "profile_step")
+        return dict(zip(self.STAGES, [float(x) for x in ms]))
 
     def time_solve(self, reps=5):
         ms, b = C.c_float(), C.c_double()

@@ -374,6 +374,12 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out);
 int dcg_batch_destroy(dcg_batch *batch);
 int dcg_batch_reset(dcg_batch *batch);     /* every member as after creation */
 int dcg_batch_step(dcg_batch *batch, int32_t n);
+/* One batch step without the step graph, timed per stage with CUDA events on
+ * the batch's stream (advances the batch like dcg_batch_step(batch, 1)).
+ * stage_ms[7]: velocity advection, adaptation, divergence, pressure cascade
+ * (with any defect correction), pressure application, scalar advection (each
+ * with its fine-to-coarse restriction), the whole step. */
+int dcg_batch_profile_step(dcg_batch *batch, float *stage_ms);
 int dcg_batch_sync(dcg_batch *batch);      /* stream sync + every member's device error word
                                                (DCG_E_NAN / DCG_E_DEVICE as for dcg_sync) */
 /* Borrowed handle of member i for field, stats, topology and emission access

@@ -146,6 +146,46 @@ def test_member_handles_are_borrowed():
     assert np.isfinite(b[0].get_field("density")).all()
 
 
+@pytest.mark.parametrize("prec", [capi.PRECISION_FP32, capi.PRECISION_MIXED_FP16], ids=["fp32", "fp16"])
+def test_batch_defect_correction_members_equal_standalone(prec):
+    """FP64 defect correction inside a batch: every member equals a standalone
+    simulation with the same passes bit for bit (fields and topology); the
+    relative residuals are FP64 sums of the same terms in another order."""
+    params = small_batch(5, 23, prec)
+    for q in params:
+        q.defect_passes = 2
+    b = batch_run(params, 4)
+    bst = b.stats()
+    for i, p in enumerate(params):
+        s = standalone(p, 4)
+        compare(b[i], s, p, f"member {i}")
+        one = s.stats()
+        assert one.defect_rel_residual[1] < one.defect_rel_residual[0]
+        for k in range(2):
+            assert bst[i].defect_rel_residual[k] == pytest.approx(one.defect_rel_residual[k], rel=1e-9)
+
+
+def test_batch_defect_correction_member_equals_oracle():
+    params = small_batch(3, 29)
+    for q in params:
+        q.defect_passes = 1
+    b = batch_run(params, 3, tuning(1, 19, 0, 2, 1))
+    for i, p in enumerate(params):
+        o = orc(p)
+        o.add_velocity_noise(11, 0.05)
+        o.step(3)
+        compare(b[i], o, p, f"member {i} vs oracle")
+
+
+def test_batch_rejects_mixed_defect_passes():
+    from dcgrid_gb300 import Batch, DcgError
+    params = small_batch(2, 1)
+    params[1].defect_passes = 1
+    with pytest.raises(DcgError) as e:
+        Batch(params)
+    assert e.value.code == capi.DCG_E_INVALID
+
+
 def test_batch_rejects_mixed_sweep_counts():
     from dcgrid_gb300 import Batch, DcgError
     params = small_batch(2, 1)
