@@ -793,6 +793,64 @@ int dcg_adjoint_step(dcg_sim *s, const float *lam_in, float *lam_out, float *lam
   launch_adjoint_step(s->D, s->adj_tmp, lam_out, s->P.emission_n > 0 ? lam_emission : nullptr, s->sms, s->stream);
   return s->check_launch("adjoint_step");
 }
+// Full adjoint of one step: the handle holds the state before the step; the
+// call records it, runs the step (stage by stage, the same kernels as
+// dcg_step) and applies the transposes of its stages in reverse order.
+int dcg_adjoint_step_full(dcg_sim *s, const float *lam_in, float *lam_out, float *lam_emission) {
+  if (bad(s) || !lam_in || !lam_out || s->mode != DCG_MODE_ADAPTIVE) return DCG_E_INVALID;
+  if (member_refused(s)) return DCG_E_INVALID;
+  if (s->D.g.mixed) return s->fail(DCG_E_INVALID, "the adjoint is implemented for FP32 scalar storage");
+  if (s->P.defect_passes) return s->fail(DCG_E_INVALID, "the full adjoint does not transpose the defect correction");
+  const size_t B = (size_t)s->D.g.B, nc = B * BV;
+  const int nq = s->P.n_scalars;
+  int rc;
+  if (!s->afull) {
+    if ((rc = s->alloc(&s->afull, 19 * nc)) || (rc = s->alloc(&s->afull_pos, B)) ||
+        (rc = s->alloc(&s->afull_parent, B)) || (rc = s->alloc(&s->afull_child, 8 * B)) ||
+        (rc = s->alloc(&s->afull_nbr, 27 * B)))
+      return rc;
+  }
+  float *V0 = s->afull, *Q0 = V0 + 3 * nc, *Q0P = Q0 + 3 * nc, *W0 = Q0P + 3 * nc, *LV = W0 + nc,
+        *LQ = LV + 3 * nc, *LP = LQ + 3 * nc;
+  auto cp = [&](void *dst, const void *src, size_t bytes) {
+    if (!rc) rc = s->cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s->stream), "adjoint_step_full");
+  };
+  rc = 0;
+  // the state before the step and the incoming adjoint
+  for (int d = 0; d < 3; d++) cp(V0 + d * nc, s->D.v[d], nc * 4);
+  for (int k = 0; k < nq; k++) cp(Q0 + k * nc, s->D.q[k], nc * 4);
+  cp(W0, s->D.w, nc * 4);
+  cp(s->afull_pos, s->D.pos, B * sizeof(int4));
+  cp(s->afull_parent, s->D.parent, B * 4);
+  cp(s->afull_child, s->D.child, 8 * B * 4);
+  cp(s->afull_nbr, s->D.nbr, 27 * B * 4);
+  cp(LV, lam_in, 3 * nc * 4);
+  cp(LQ, lam_in + 3 * nc, nq * nc * 4);
+  if (rc) return rc;
+  Dev D0 = s->D;
+  D0.pos = s->afull_pos;
+  D0.parent = s->afull_parent;
+  D0.child = s->afull_child;
+  D0.nbr = s->afull_nbr;
+  D0.w = W0;
+  for (int d = 0; d < 3; d++) D0.v[d] = V0 + d * nc;
+  for (int k = 0; k < nq; k++) D0.q[k] = Q0 + k * nc;
+  // the step, keeping the scalars its advection reads (after the propagation)
+  s->stage_advect_velocity();
+  s->stage_adapt();
+  for (int k = 0; k < nq; k++) cp(Q0P + k * nc, s->D.q[k], nc * 4);
+  if (rc) return rc;
+  s->stage_project(false);
+  s->stage_advect_scalars();
+  s->steps++;
+  Dev DA = s->D;
+  for (int k = 0; k < nq; k++) DA.q[k] = Q0P + k * nc;
+  AdjFull A{LV, LQ, LP, LP + nc, LP + 2 * nc, lam_out, lam_out + 3 * nc};
+  launch_adjoint_full_phase_a(DA, A, s->P.emission_n > 0 ? lam_emission : nullptr, s->P.jacobi_iters, s->sms,
+                              s->stream);
+  launch_adjoint_full_phase_b(D0, A, s->stream);
+  return s->check_launch("adjoint_step_full");
+}
 int dcg_adjoint_dense(dcg_sim *s, const float *lam_dense, float *lam_cells) {
   if (bad(s) || !lam_dense || !lam_cells || s->mode != DCG_MODE_ADAPTIVE) return DCG_E_INVALID;
   launch_adjoint_dense(s->D, lam_dense, lam_cells, s->stream);

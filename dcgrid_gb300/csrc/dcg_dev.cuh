@@ -296,6 +296,25 @@ __device__ inline unsigned long long apron_cell(const Dev &D, uint32_t b, int4 b
   return (unsigned long long)nb * BV + local_of((cx >> k) & 3, (cy >> k) & 3, (cz >> k) & 3);
 }
 
+// The six Jacobi neighbours (L, R, D, U, B, F) of a cell, as global cell indices.
+struct Nb6 {
+  uint32_t i0, i1, i2, i3, i4, i5;
+};
+__device__ inline Nb6 jacobi_neighbours(const Dev &D, long long cell) {
+  const uint32_t b = (uint32_t)(cell >> 6);
+  const int4 bp = D.pos[b];
+  int lx, ly, lz;
+  local_xyz((int)(cell & 63), lx, ly, lz);
+  const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+  Nb6 n;
+  n.i0 = (uint32_t)apron_cell(D, b, bp, ax - 1, ay, az);
+  n.i1 = (uint32_t)apron_cell(D, b, bp, ax + 1, ay, az);
+  n.i2 = (uint32_t)apron_cell(D, b, bp, ax, ay - 1, az);
+  n.i3 = (uint32_t)apron_cell(D, b, bp, ax, ay + 1, az);
+  n.i4 = (uint32_t)apron_cell(D, b, bp, ax, ay, az - 1);
+  n.i5 = (uint32_t)apron_cell(D, b, bp, ax, ay, az + 1);
+  return n;
+}
 // ---------------------------------------------------------------- physics
 // All float expressions below keep the operation order of the reference
 // (src/utils/sim_utils.cu, src/sdf.cuh); the library is compiled with

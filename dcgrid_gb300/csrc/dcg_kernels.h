@@ -136,6 +136,19 @@ void launch_apron_table(const Dev &D, long long *dst, cudaStream_t st);
 void launch_adjoint_step(const Dev &D, float *lam_in_scratch, float *lam_out, float *lam_em, int sms,
                          cudaStream_t st);
 void launch_adjoint_dense(const Dev &D, const float *lam_dense, float *lam, cudaStream_t st);
+// Full adjoint of one step (planes of nc = 64 * max_blocks cells). Phase A
+// runs on the state after the step (DA: its topology, projected velocity,
+// and as scalars those its advection read), phase B on the state before it
+// (D0: topology, velocity, scalars and fluidity of its start).
+struct AdjFull {
+  float *lv;               // 3 planes: adjoint of the velocity, after the step in, worked in place
+  float *lq;               // nq planes: adjoint of the scalars after the step, worked in place
+  float *lp0, *lp1, *ld;   // adjoint of p, p~ and div in the transposed cascade (consecutive planes)
+  float *out_v, *out_q;    // 3 and nq planes: adjoint of the state before the step
+};
+void launch_adjoint_full_phase_a(const Dev &DA, const AdjFull &A, float *lam_em, int sweeps, int sms,
+                                 cudaStream_t st);
+void launch_adjoint_full_phase_b(const Dev &D0, const AdjFull &A, cudaStream_t st);
 
 // k_render.cu — headless ray marcher (parameters mirror dcg_render_params)
 struct RenderP {

@@ -48,6 +48,12 @@ struct dcg_sim {
   uint16_t *qhbuf[2][3] = {};  // 16-bit scalar storage (mixed precision)
   float *conv_tmp = nullptr;   // FP32 staging for access to 16-bit fields
   float *adj_tmp = nullptr;    // adjoint scratch (allocated on first use)
+  // full adjoint scratch (first use): 19 planes (the state before the step,
+  // the scalars the advection read, the adjoint planes) and a copy of the
+  // block table of the step's start
+  float *afull = nullptr;
+  int4 *afull_pos = nullptr;
+  uint32_t *afull_parent = nullptr, *afull_child = nullptr, *afull_nbr = nullptr;
   float *render_tmp = nullptr; // renderer output staging for host buffers
   size_t render_cap = 0;
   float *hmap = nullptr;       // terrain heightmap (dcg_set_heightmap), or null

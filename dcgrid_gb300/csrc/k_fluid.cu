@@ -314,25 +314,6 @@ __device__ inline void prolong_cell(const Dev &D, long long cell) {
   D.p[cell] = (27.f * p000 + 9.f * (p001 + p010 + p100) + 3.f * (p011 + p101 + p110) + p111) / 64.f;
 }
 
-// The six Jacobi neighbours (L, R, D, U, B, F) of a cell, as global cell indices.
-struct Nb6 {
-  uint32_t i0, i1, i2, i3, i4, i5;
-};
-__device__ inline Nb6 jacobi_neighbours(const Dev &D, long long cell) {
-  const uint32_t b = (uint32_t)(cell >> 6);
-  const int4 bp = D.pos[b];
-  int lx, ly, lz;
-  local_xyz((int)(cell & 63), lx, ly, lz);
-  const int ax = lx + 1, ay = ly + 1, az = lz + 1;
-  Nb6 n;
-  n.i0 = (uint32_t)apron_cell(D, b, bp, ax - 1, ay, az);
-  n.i1 = (uint32_t)apron_cell(D, b, bp, ax + 1, ay, az);
-  n.i2 = (uint32_t)apron_cell(D, b, bp, ax, ay - 1, az);
-  n.i3 = (uint32_t)apron_cell(D, b, bp, ax, ay + 1, az);
-  n.i4 = (uint32_t)apron_cell(D, b, bp, ax, ay, az - 1);
-  n.i5 = (uint32_t)apron_cell(D, b, bp, ax, ay, az + 1);
-  return n;
-}
 // Loads go through L2 (__ldcg): inside one persistent launch the ping-pong
 // buffers are rewritten by other SMs, so no SM may serve them from its L1.
 __device__ inline float jacobi_update(const float *src, const Nb6 &n, float ad) {

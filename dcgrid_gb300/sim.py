@@ -70,6 +70,7 @@ def lib():
         L.dcg_load_state.argtypes = [vp, vp, C.c_int32]
         L.dcg_adjoint_step.argtypes = [vp, vp, vp, vp]
         L.dcg_adjoint_dense.argtypes = [vp, vp, vp]
+        L.dcg_adjoint_step_full.argtypes = [vp, vp, vp, vp]
         L.dcg_batch_create.argtypes = [C.c_int32, vp, C.POINTER(vp)]
         for name in ["dcg_batch_destroy", "dcg_batch_reset", "dcg_batch_sync"]:
             getattr(L, name).argtypes = [vp]
@@ -402,6 +403,21 @@ class Simulation:
             em, _ = _buf(lam_emission, int(self.params.emission_n) ** 3, np.float32, "adjoint_step lam_emission",
                          device=True)
         self._chk(self.L.dcg_adjoint_step(self.h, li, lo, em), "adjoint_step")
+
+    def adjoint_step_full(self, lam_in, lam_out, lam_emission=None):
+        """dcg_adjoint_step_full: the handle holds the state before a step; the
+        call runs the step and writes into lam_out the adjoint of that state
+        (velocity and scalars, (3 + n_scalars) planes of num_cells) given
+        lam_in, the adjoint of the state after it; lam_emission accumulates
+        the emission map's adjoint."""
+        n = (3 + int(self.params.n_scalars)) * self.num_cells
+        li, _ = _buf(lam_in, n, np.float32, "adjoint_step_full lam_in", device=True)
+        lo, _ = _buf(lam_out, n, np.float32, "adjoint_step_full lam_out", device=True)
+        em = None
+        if lam_emission is not None and self.params.emission_n > 0:
+            em, _ = _buf(lam_emission, int(self.params.emission_n) ** 3, np.float32,
+                         "adjoint_step_full lam_emission", device=True)
+        self._chk(self.L.dcg_adjoint_step_full(self.h, li, lo, em), "adjoint_step_full")
 
     def adjoint_dense(self, lam_dense, lam_cells):
         p = self.params

@@ -482,6 +482,21 @@ int dcg_load_state(dcg_sim *sim, const void *src, int32_t where);
  * lam_cells (device, block-major, accumulated). FP32 scalar storage only. */
 int dcg_adjoint_step(dcg_sim *sim, const float *lam_in, float *lam_out, float *lam_emission);
 int dcg_adjoint_dense(dcg_sim *sim, const float *lam_dense, float *lam_cells);
+/* Full adjoint of one step (extension; no reference counterpart): the whole
+ * state - velocity and every scalar - with buoyancy, the pressure projection
+ * (the transposed cascade: each Jacobi sweep and prolongation transposed, in
+ * reverse order) and the dependence of the semi-Lagrangian sample positions
+ * on the velocity; the block topology is recorded, not differentiated. The
+ * handle must hold the state BEFORE the step: the call runs the step (the
+ * handle then holds the state after it, as after dcg_step(sim, 1)) and applies
+ * the transposes of its stages in reverse order. lam_in / lam_out: device,
+ * (3 + n_scalars) planes of 64*max_blocks cells, block-major: v_x, v_y, v_z,
+ * then the scalars; lam_in = the adjoint of the state after the step, lam_out
+ * receives that of the state before it (may alias lam_in). lam_emission
+ * (device, emission_n^3, may be NULL) accumulates the adjoint of the emission
+ * map. FP32 storage, adaptive grid, no defect correction; not for members of
+ * a batch. */
+int dcg_adjoint_step_full(dcg_sim *sim, const float *lam_in, float *lam_out, float *lam_emission);
 
 /* sizeof of the ABI structs, for binding checks. */
 size_t dcg_sizeof_params(void);

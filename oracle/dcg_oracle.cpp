@@ -1658,6 +1658,295 @@ template <typename R> struct DC : Base {
         }
       }
   }
+  // ---------------- full adjoint of one step ----------------
+  // The whole state (velocity and every scalar): buoyancy, the pressure
+  // projection (every Jacobi sweep and prolongation of the cascade
+  // transposed, in reverse order) and the dependence of the semi-Lagrangian
+  // sample positions on the velocity, with the block topology recorded. The
+  // simulation holds the state before the step; the step runs (replaying the
+  // given adaptation decisions when `moves` is not null) and its stages'
+  // transposes are applied in reverse order in FP64. Afterwards the
+  // simulation holds the state after the step. lam_in / lam_out: (3 + nq)
+  // planes of B*64: v_x, v_y, v_z, the scalars.
+  using VD = std::vector<double>;
+  void adj_restrict(VD &lam) const {
+    for (int level = levels - 2; level >= 0; level--)
+      for (int64_t b = off[level]; b < off[level] + maxL[level]; b++) {
+        if (lvl[b] != level || parent[b] == NF) continue;
+        for (int s = 0; s < 8; s++) {
+          const size_t pc = (size_t)parent[b] * 8 + s;
+          const double lp = lam[pc] * 0.125;
+          for (int i = 0; i < 8; i++) lam[(size_t)b * BV + 8 * s + i] += lp;
+          lam[pc] = 0;
+        }
+      }
+  }
+  void adj_propagate(VD &lam) const {
+    for (int level = 0; level <= levels - 2; level++)
+      for (size_t t = 0; t < touched.size(); t++) {
+        const int64_t b = touched[t];
+        if (b == NF || lvl[b] != level || parent[b] == NF) continue;
+        const int64_t pb = parent[b] / 8;
+        const int64_t *a = &apron[(size_t)pb * AV];
+        for (int c = 0; c < BV; c++) {
+          int lx, ly, lz;
+          local_xyz(c, lx, ly, lz);
+          const int x = bx[b] + lx, y = by[b] + ly, z = bz[b] + lz;
+          const int px = (x / 2) % BW, py = (y / 2) % BW, pz = (z / 2) % BW;
+          const int idx = AA * (1 + px) + AW * (1 + py) + (1 + pz);
+          const int i = x % 2 ? AA : -AA, j = y % 2 ? AW : -AW, k = z % 2 ? 1 : -1;
+          const size_t cell = (size_t)b * BV + c;
+          const double l = lam[cell];
+          lam[cell] = 0;
+          lam[a[idx]] += 27.0 / 64.0 * l;
+          lam[a[idx + k]] += 9.0 / 64.0 * l;
+          lam[a[idx + j]] += 9.0 / 64.0 * l;
+          lam[a[idx + i]] += 9.0 / 64.0 * l;
+          lam[a[idx + j + k]] += 3.0 / 64.0 * l;
+          lam[a[idx + i + k]] += 3.0 / 64.0 * l;
+          lam[a[idx + i + j]] += 3.0 / 64.0 * l;
+          lam[a[idx + i + j + k]] += 1.0 / 64.0 * l;
+        }
+      }
+  }
+  // d(w_c * trilinear_c) / d(fractional coordinate a) of a sample
+  void sample_derivs(const Sample &s, R pxw, R pyw, R pzw, double dW[3][8], double G[3]) const {
+    const R scaleInv = (R)1 / (R)s.scale;
+    const R x = pxw * scaleInv - (R)0.5f, y = pyw * scaleInv - (R)0.5f, z = pzw * scaleInv - (R)0.5f;
+    const double dx = (double)(x - std::floor(x)), dy = (double)(y - std::floor(y)), dz = (double)(z - std::floor(z));
+    G[0] = G[1] = G[2] = 0;
+    for (int c = 0; c < 8; c++) {
+      const double wc = (double)w[s.idx[c]];
+      const double X = (c & 4) ? dx : 1 - dx, Y = (c & 2) ? dy : 1 - dy, Z = (c & 1) ? dz : 1 - dz;
+      const double sx = (c & 4) ? 1 : -1, sy = (c & 2) ? 1 : -1, sz = (c & 1) ? 1 : -1;
+      dW[0][c] = wc * sx * Y * Z;
+      dW[1][c] = wc * X * sy * Z;
+      dW[2][c] = wc * X * Y * sz;
+      for (int a = 0; a < 3; a++) G[a] += dW[a][c];
+    }
+  }
+  // velocity advection + buoyancy transpose, on the state before the step
+  void adj_velocity(VD *lv, VD *out_v, VD *out_q) const {
+    for (int d = 0; d < 3; d++) adj_restrict(lv[d]);
+    const bool buoy = P.buoy_alpha != 0.f || P.buoy_beta != 0.f;
+    for (int64_t b = 0; b < B; b++) {
+      if (lvl[b] == FREE) continue;
+      for (int c = 0; c < BV; c++) {
+        const size_t cell = (size_t)b * BV + c;
+        if (!leaf(cell)) continue;
+        const double l[3] = {lv[0][cell], lv[1][cell], lv[2][cell]};
+        if (l[0] == 0 && l[1] == 0 && l[2] == 0) continue;
+        if (buoy) {
+          out_q[0][cell] += -(double)ph.dt * (double)P.buoy_alpha * l[1];
+          if (nq > 1) out_q[1][cell] += (double)ph.dt * (double)P.buoy_beta * l[1];
+        }
+        R pos[3];
+        back_trace(b, c, pos);
+        Sample s;
+        sample(pos[0], pos[1], pos[2], s);
+        if (s.wAcc < (R)1e-6f) continue;
+        double dW[3][8], G[3];
+        sample_derivs(s, pos[0], pos[1], pos[2], dW, G);
+        double gsum[3] = {0, 0, 0};
+        for (int k = 0; k < 8; k++) {
+          int x, y, z;
+          corner(s, k, x, y, z);
+          R vc[3] = {v[0][s.idx[k]], v[1][s.idx[k]], v[2][s.idx[k]]};
+          ph.vel_bc(vc, x, y, z, s.scale);
+          const bool pass = ph.q_passes(x, y, z, s.scale);
+          for (int comp = 0; comp < 3; comp++) {
+            if (pass) out_v[comp][s.idx[k]] += l[comp] * (double)s.wt[k];
+            for (int a = 0; a < 3; a++) gsum[a] += l[comp] * dW[a][k] * (double)vc[comp];
+          }
+        }
+        double out[3] = {0, 0, 0};
+        for (int k = 0; k < 8; k++)
+          for (int comp = 0; comp < 3; comp++) {
+            int x, y, z;
+            corner(s, k, x, y, z);
+            R vc[3] = {v[0][s.idx[k]], v[1][s.idx[k]], v[2][s.idx[k]]};
+            ph.vel_bc(vc, x, y, z, s.scale);
+            out[comp] += (double)s.wt[k] * (double)vc[comp];
+          }
+        for (int a = 0; a < 3; a++)
+          for (int comp = 0; comp < 3; comp++) gsum[a] -= l[comp] * out[comp] * G[a];
+        const double f = -(double)(ph.dt * ph.rdx) / (double)s.scale / (double)s.wAcc;
+        for (int a = 0; a < 3; a++) out_v[a][cell] += f * gsum[a];
+      }
+    }
+  }
+  int adjoint_step_full(const double *lam_in, double *lam_out, double *lam_em, const int64_t *moves, int64_t nm,
+                        const int64_t *refines, int64_t nr) {
+    if (P.defect_passes) return fail(DCG_E_INVALID, "the full adjoint does not transpose the defect correction");
+    const size_t nc = (size_t)B * BV;
+    DC before = *this;
+    before.ph.P = &before.P;
+    before.ph.em = &before.emis;
+    advect_velocity();
+    int rc = moves ? replay(moves, nm, refines, nr) : adapt();
+    if (rc) return rc;
+    std::vector<R> q0p[3];
+    for (int k = 0; k < nq; k++) q0p[k] = q[k];
+    project();
+    advect_scalars();
+    steps++;
+    // phase A on the state after the step
+    VD lv[3], lq[3], out_v[3], out_q[3];
+    for (int d = 0; d < 3; d++) {
+      lv[d].assign(lam_in + d * nc, lam_in + (d + 1) * nc);
+      out_v[d].assign(nc, 0.0);
+    }
+    for (int k = 0; k < nq; k++) {
+      lq[k].assign(lam_in + (3 + k) * nc, lam_in + (4 + k) * nc);
+      out_q[k].assign(nc, 0.0);
+      adj_restrict(lq[k]);
+    }
+    for (int64_t b = 0; b < B; b++) {  // scalar advection (+ emission, sources cut)
+      if (lvl[b] == FREE) continue;
+      const int scale0 = 1 << lvl[b];
+      for (int c = 0; c < BV; c++) {
+        const size_t cell = (size_t)b * BV + c;
+        if (!leaf(cell)) continue;
+        bool any = false;
+        for (int k = 0; k < nq; k++) any |= lq[k][cell] != 0;
+        if (!any) continue;
+        int x, y, z;
+        local_xyz(c, x, y, z);
+        if (ph.in_source(bx[b] + x, by[b] + y, bz[b] + z, scale0)) continue;
+        if (P.emission_n > 0 && lam_em && lq[0][cell] != 0)
+          ph.emission_adjoint(bx[b] + x, by[b] + y, bz[b] + z, scale0, (double)ph.dt * lq[0][cell], lam_em);
+        R pos[3];
+        back_trace(b, c, pos);
+        Sample s;
+        sample(pos[0], pos[1], pos[2], s);
+        if (s.wAcc < (R)1e-6f) continue;
+        double dW[3][8], G[3];
+        sample_derivs(s, pos[0], pos[1], pos[2], dW, G);
+        double gsum[3] = {0, 0, 0};
+        for (int k = 0; k < nq; k++) {
+          const double l = lq[k][cell];
+          if (l == 0) continue;
+          double out = 0, H[3] = {0, 0, 0};
+          for (int cc = 0; cc < 8; cc++) {
+            int cx, cy, cz;
+            corner(s, cc, cx, cy, cz);
+            const double val = (double)ph.q_bc(q0p[k][s.idx[cc]], k, cx, cy, cz, s.scale);
+            out += (double)s.wt[cc] * val;
+            for (int a = 0; a < 3; a++) H[a] += dW[a][cc] * val;
+            if (ph.q_passes(cx, cy, cz, s.scale)) out_q[k][s.idx[cc]] += l * (double)s.wt[cc];
+          }
+          for (int a = 0; a < 3; a++) gsum[a] += l * (H[a] - out * G[a]) / (double)s.wAcc;
+        }
+        const double f = -(double)(ph.dt * ph.rdx) / (double)s.scale;
+        for (int a = 0; a < 3; a++) lv[a][cell] += f * gsum[a];
+      }
+    }
+    for (int d = 0; d < 3; d++) adj_restrict(lv[d]);
+    VD lp[2] = {VD(nc, 0.0), VD(nc, 0.0)}, ld(nc, 0.0);
+    for (int64_t b = 0; b < B; b++) {  // pressure gradient
+      if (lvl[b] == FREE) continue;
+      const double alpha = (double)((R)0.5f * ph.rdx / (R)(1 << lvl[b]));
+      for (int c = 0; c < BV; c++) {
+        const size_t cell = (size_t)b * BV + c;
+        if (!leaf(cell)) continue;
+        int lx, ly, lz;
+        local_xyz(c, lx, ly, lz);
+        const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+        for (int a = 0; a < 3; a++) {
+          const double l = lv[a][cell];
+          if (l == 0) continue;
+          const size_t L = apr(b, ax - (a == 0), ay - (a == 1), az - (a == 2));
+          const size_t Rr = apr(b, ax + (a == 0), ay + (a == 1), az + (a == 2));
+          const double wL = (double)w[L], wR = (double)w[Rr];
+          lp[0][Rr] += -alpha * wR * l;
+          lp[0][cell] += -alpha * (wL - wR) * l;
+          lp[0][L] += alpha * wL * l;
+        }
+      }
+    }
+    const int sweeps = P.jacobi_iters;
+    for (int level = 0; level < levels; level++) {  // the cascade, transposed
+      const int s = 1 << level;
+      const double alpha = (double)((R)(s * s) * ph.dx * ph.dx);
+      for (int it = sweeps - 1; it >= 0; it--) {
+        VD &ldst = lp[(it & 1) ? 0 : 1], &lsrc = lp[(it & 1) ? 1 : 0];
+#pragma omp parallel for schedule(static)
+        for (int64_t b = off[level]; b < off[level] + maxL[level]; b++) {
+          if (lvl[b] != level) continue;
+          for (int c = 0; c < BV; c++) {
+            const size_t cell = (size_t)b * BV + c;
+            const double l = ldst[cell];
+            if (l == 0) continue;
+            ldst[cell] = 0;
+            int lx, ly, lz;
+            local_xyz(c, lx, ly, lz);
+            const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+            const size_t nb[6] = {apr(b, ax - 1, ay, az), apr(b, ax + 1, ay, az), apr(b, ax, ay - 1, az),
+                                  apr(b, ax, ay + 1, az), apr(b, ax, ay, az - 1), apr(b, ax, ay, az + 1)};
+            for (int n = 0; n < 6; n++) {
+#pragma omp atomic
+              lsrc[nb[n]] += l / 6.0;
+            }
+            ld[cell] += -alpha * l / 6.0;
+          }
+        }
+      }
+      if (level == levels - 1) break;
+      for (int64_t b = off[level]; b < off[level] + maxL[level]; b++) {  // prolongation
+        if (lvl[b] != level || parent[b] == NF) continue;
+        const int64_t pb = parent[b] / 8;
+        const int64_t *a = &apron[(size_t)pb * AV];
+        for (int c = 0; c < BV; c++) {
+          const size_t cell = (size_t)b * BV + c;
+          const double l = lp[0][cell];
+          lp[0][cell] = 0;
+          if (l == 0) continue;
+          int lx, ly, lz;
+          local_xyz(c, lx, ly, lz);
+          const int x = bx[b] + lx, y = by[b] + ly, z = bz[b] + lz;
+          const int px = (x / 2) % BW, py = (y / 2) % BW, pz = (z / 2) % BW;
+          const int idx = AA * (1 + px) + AW * (1 + py) + (1 + pz);
+          const int i = x % 2 ? AA : -AA, j = y % 2 ? AW : -AW, k = z % 2 ? 1 : -1;
+          lp[0][a[idx]] += 27.0 / 64.0 * l;
+          lp[0][a[idx + k]] += 9.0 / 64.0 * l;
+          lp[0][a[idx + j]] += 9.0 / 64.0 * l;
+          lp[0][a[idx + i]] += 9.0 / 64.0 * l;
+          lp[0][a[idx + j + k]] += 3.0 / 64.0 * l;
+          lp[0][a[idx + i + k]] += 3.0 / 64.0 * l;
+          lp[0][a[idx + i + j]] += 3.0 / 64.0 * l;
+          lp[0][a[idx + i + j + k]] += 1.0 / 64.0 * l;
+        }
+      }
+    }
+    adj_restrict(ld);
+    for (int64_t b = 0; b < B; b++) {  // divergence
+      if (lvl[b] == FREE) continue;
+      const int scale = 1 << lvl[b];
+      const double alpha = (double)((R)0.5f * ph.rdx / (R)scale);
+      for (int c = 0; c < BV; c++) {
+        const size_t cell = (size_t)b * BV + c;
+        if (!leaf(cell) || ld[cell] == 0) continue;
+        int lx, ly, lz;
+        local_xyz(c, lx, ly, lz);
+        const int ax = lx + 1, ay = ly + 1, az = lz + 1;
+        const int x = bx[b] + lx, y = by[b] + ly, z = bz[b] + lz;
+        for (int a = 0; a < 3; a++)
+          for (int sg = -1; sg <= 1; sg += 2) {
+            const int da = a == 0 ? sg : 0, db = a == 1 ? sg : 0, dc = a == 2 ? sg : 0;
+            if (!ph.q_passes(x + da, y + db, z + dc, scale)) continue;
+            const size_t n = apr(b, ax + da, ay + db, az + dc);
+            lv[a][n] += (double)sg * alpha * (double)w[n] * ld[cell];
+          }
+      }
+    }
+    for (int d = 0; d < 3; d++) adj_propagate(lv[d]);
+    for (int k = 0; k < nq; k++) adj_propagate(out_q[k]);
+    // phase B on the state before the step
+    before.adj_velocity(lv, out_v, out_q);
+    for (int d = 0; d < 3; d++) std::copy(out_v[d].begin(), out_v[d].end(), lam_out + d * nc);
+    for (int k = 0; k < nq; k++) std::copy(out_q[k].begin(), out_q[k].end(), lam_out + (3 + k) * nc);
+    return DCG_OK;
+  }
   // transpose of get_dense: lam_cells[leaf covering (x,y,z)] += lam_dense[x,y,z]
   void adjoint_dense(const double *lam_dense, double *lam_cells) const {
     for (int z = 0; z < gz; z++)
@@ -2438,6 +2727,11 @@ int dcgo_adjoint_step(dcgo_sim *s, const double *lam_in, double *lam_out, double
     d.adjoint_step(lam_in, lam_out, lam_em);
     return DCG_OK;
   });
+}
+int dcgo_adjoint_step_full(dcgo_sim *s, const double *lam_in, double *lam_out, double *lam_em, const int64_t *moves,
+                           int64_t n_moves, const int64_t *refines, int64_t n_refines) {
+  if (!s || !lam_in || !lam_out) return DCG_E_INVALID;
+  return with_dc(s, [&](auto &d) { return d.adjoint_step_full(lam_in, lam_out, lam_em, moves, n_moves, refines, n_refines); });
 }
 int dcgo_adjoint_dense(dcgo_sim *s, const double *lam_dense, double *lam_cells) {
   if (!lam_dense || !lam_cells) return DCG_E_INVALID;

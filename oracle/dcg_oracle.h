@@ -81,6 +81,14 @@ int dcgo_render(dcgo_sim *s, const dcg_render_params *rp, double *rgba);
  * the current state (flow and topology fixed); lam_em (emission_n^3) is
  * accumulated and may be NULL. */
 int dcgo_adjoint_step(dcgo_sim *s, const double *lam_in, double *lam_out, double *lam_em);
+/* FP64 host adjoint of one whole step (velocity and scalars, buoyancy, the
+ * transposed pressure cascade, sample positions' dependence on the velocity):
+ * the simulation holds the state before the step; the step runs, replaying
+ * the given adaptation decisions (dcg_get_last_adapt layout) when moves is not
+ * NULL, and lam_out receives the adjoint of the state before it given lam_in,
+ * that of the state after it; (3 + n_scalars) planes of 64*max_blocks. */
+int dcgo_adjoint_step_full(dcgo_sim *s, const double *lam_in, double *lam_out, double *lam_em,
+                           const int64_t *moves, int64_t n_moves, const int64_t *refines, int64_t n_refines);
 /* transpose of dcgo_get_dense, accumulated into lam_cells */
 int dcgo_adjoint_dense(dcgo_sim *s, const double *lam_dense, double *lam_cells);
 /* dst takes src's whole state; both created with the same parameters and

@@ -58,6 +58,7 @@ def lib():
         L.dcgo_render.argtypes = [vp, C.POINTER(capi.DcgRenderParams), vp]
         L.dcgo_adjoint_step.argtypes = [vp, vp, vp, vp]
         L.dcgo_adjoint_dense.argtypes = [vp, vp, vp]
+        L.dcgo_adjoint_step_full.argtypes = [vp, vp, vp, vp, vp, C.c_int64, vp, C.c_int64]
         L.dcgo_copy_state.argtypes = [vp, vp]
         _lib = L
     return _lib
@@ -226,6 +227,23 @@ class OracleSim:
         a = np.ascontiguousarray(lam_in, np.float64)
         out = np.empty_like(a)
         self._chk(self.L.dcgo_adjoint_step(self.h, _ptr(a), _ptr(out), _ptr(lam_em)), "adjoint_step")
+        return out
+
+    def adjoint_step_full(self, lam_in, lam_em=None, moves=None, refines=None):
+        """FP64 adjoint of one whole step from the state held now (which the
+        call advances by the step, replaying `moves` / `refines` when given);
+        returns the adjoint of the state before the step ((3 + n_scalars)
+        planes) given lam_in, that of the state after it."""
+        a = np.ascontiguousarray(lam_in, np.float64)
+        out = np.empty_like(a)
+        if moves is None:
+            mv, nm, rf, nr = None, 0, None, 0
+        else:
+            mv = np.ascontiguousarray(moves, np.int64).reshape(-1)
+            rf = np.ascontiguousarray(refines, np.int64).reshape(-1)
+            nm, nr = len(mv) // 2, len(rf) // 2
+        self._chk(self.L.dcgo_adjoint_step_full(self.h, _ptr(a), _ptr(out), _ptr(lam_em), _ptr(mv), nm, _ptr(rf),
+                                                nr), "adjoint_step_full")
         return out
 
     def adjoint_dense(self, lam_dense, lam_cells):

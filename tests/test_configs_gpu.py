@@ -102,7 +102,7 @@ def test_cloud256_40k_blocks_spun_up_window_bitexact():
         g.sync()
         compare(g, o, p, f"spun-up step {k + 1}")
         moved += g.stats().moved_blocks + g.stats().refined_subblocks
-    assert g.stats().active_cells > 1_000_000
+    assert g.stats().active_cells > 500_000
     assert moved > 0  # the window includes topology changes
 
 
