@@ -277,6 +277,27 @@ def density_error_fp16(params, steps=10):
     return out
 
 
+def reference_gpu_comparator(steps=3):
+    """The reference's own kernels, compiled from its unmodified sources into
+    oracle/_ref (cubins; the reference's host orchestration restated around
+    them), against this library stage by stage on the same input: the
+    reference's default scene at 64x128x64 (3000 blocks) and 256^3 (40000
+    blocks), derived level counts, 10 (the reference's) and 100 Jacobi sweeps
+    per level. A measurement of the reference, never a path of this library."""
+    cubin = os.path.join(ROOT, "oracle", "_ref", "ref_dcgrid.cubin")
+    if not os.path.exists(cubin):
+        return {"unavailable": "the reference's cubins are not built (its sources were absent when build() ran)"}
+    from oracle import ref_gpu_timing
+    runs = []
+    for size, blocks in [((64, 128, 64), 3000), ((256, 256, 256), 40000)]:
+        for sweeps in (10, 100):
+            runs.append(ref_gpu_timing.stage_compare(size, blocks, sweeps, steps=steps))
+    return {"runs": runs,
+            "note": "per stage: CUDA events on each side's stream after an L2 flush, mean of "
+                    f"{steps} steps; ratio = reference ms / ours ms; adaptTopology on the reference side "
+                    "includes its host ranking (D2H, sort, H2D) as in the reference application"}
+
+
 # ------------------------------------------------------------------ batch
 def run_batch(args, ctx):
     import numpy as np
@@ -452,6 +473,8 @@ def run_batch(args, ctx):
             "launches_per_step": info["launches_per_step"], "roofline": roofline, "e2e": e2e}
     if clk:
         line["clocks"] = clk
+    if ctx.rank == 0 and not args.no_ref_gpu:
+        line["comparison"]["reference_gpu"] = reference_gpu_comparator()
     if ctx.rank == 0 and not args.no_cpu:
         # the largest member over the headline's horizon: spin-up, warm-up and timed steps
         line["comparison"]["rel_err_fp16_vs_fp64"] = density_error_fp16(
@@ -666,6 +689,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch", choices=["batch", "cloud", "large"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and FP64 error legs")
+    ap.add_argument("--no-ref-gpu", action="store_true", help="skip the reference-kernel GPU comparator")
     ap.add_argument("--profile", action="store_true",
                     help="batch workload: time the headline leg only (for profiler runs)")
     ap.add_argument("--tuning", default=None,

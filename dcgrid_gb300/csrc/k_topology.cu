@@ -876,10 +876,17 @@ struct AdaptLauncher {
   const AdaptMember *m;
   int n;
   unsigned gs;  // grid-stride CTAs per member
+  int sms;
   cudaStream_t st;
+  // grid-barrier words and error word of the single-launch sorts (null: one
+  // launch per sort phase)
+  uint32_t *sort_bar = nullptr, *err = nullptr;
+  void sort(const SortSeg *seg, int ns) {
+    if (!(sort_bar && launch_radix_sort_coop(seg, ns, sort_bar, err, sms, st))) launch_radix_sort_batch(seg, ns, st);
+  }
   AdaptBatchP P{};
 
-  AdaptLauncher(const AdaptMember *mm, int nn, int sms, cudaStream_t s) : m(mm), n(nn), st(s) {
+  AdaptLauncher(const AdaptMember *mm, int nn, int sms_, cudaStream_t s) : m(mm), n(nn), sms(sms_), st(s) {
     P.n = n;
     for (int i = 0; i < n; i++) P.d[i] = m[i].D;
     const int total = sms > 0 ? sms * 4 : 512;
@@ -952,7 +959,7 @@ struct AdaptLauncher {
         seg[ns++] = SortSeg{m[i].keys, m[i].vals, m[i].D.g.budget[L], act, m[i].S2, m[i].D.load + L, 1};
         seg[ns++] = SortSeg{m[i].keys2, m[i].vals2, 8 * m[i].D.g.budget[L + 1], act, m[i].S, m[i].D.load + L + 1, 8};
       }
-      launch_radix_sort_batch(seg, ns, st);
+      sort(seg, ns);
       for (int i = 0; i < n; i++) {
         P.p0[i] = m[i].vals;
         P.p1[i] = m[i].vals2;
@@ -996,7 +1003,7 @@ struct AdaptLauncher {
         if (score[i])
           seg[ns++] = SortSeg{m[i].keys, m[i].vals2, 8 * m[i].D.g.budget[L], m[i].D.ctr + C_SELECT, m[i].S,
                               m[i].D.ctr + C_NCAND, 1};  // the compacted candidates only, when selecting
-      launch_radix_sort_batch(seg, ns, st);
+      sort(seg, ns);
       for (int i = 0; i < n; i++) {
         P.p0[i] = m[i].keys2;
         P.nn[i] = 2 * B(i);  // 8*B selection bytes as words
@@ -1026,9 +1033,13 @@ struct AdaptLauncher {
 };
 }  // namespace
 
-void launch_adapt_batch(const AdaptMember *m, int n, int sms, cudaStream_t st) {
+void launch_adapt_batch(const AdaptMember *m, int n, int sms, cudaStream_t st, uint32_t *sort_bar,
+                        uint32_t *err) {
   if (n <= 0 || n > BMAX) return;
-  AdaptLauncher(m, n, sms, st).run();
+  AdaptLauncher L(m, n, sms, st);
+  L.sort_bar = sort_bar;
+  L.err = err;
+  L.run();
 }
 
 // ------------------------------------------------------------------ stats

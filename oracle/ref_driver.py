@@ -254,15 +254,18 @@ class RefDCGrid:
         self.d.sync()
 
     def project(self):
+        # the reference hard-wires 5 pairs of sweeps per level (cu:274-290);
+        # other sweep counts come from params.jacobi_iters (10 = the reference)
+        pairs = max(self.p.jacobi_iters, 0) // 2
         self.d.launch("k_dcgrid_calc_divergence", self.B, 64, self.g)
         self._accumulate("k_dcgrid_accumulate_divergence")
         top = self.levels - 1
-        for _ in range(5):
+        for _ in range(pairs):
             self.d.launch("k_dcgrid_jacobi", self.maxL[top], 64, self.g, C.c_uint8(top))
             self.d.launch("k_dcgrid_jacobi_inv", self.maxL[top], 64, self.g, C.c_uint8(top))
         for level in range(self.levels - 2, -1, -1):
             self.d.launch("k_dcgrid_prolongate", self.maxL[level], 64, self.g, C.c_uint8(level))
-            for _ in range(5):
+            for _ in range(pairs):
                 self.d.launch("k_dcgrid_jacobi", self.maxL[level], 64, self.g, C.c_uint8(level))
                 self.d.launch("k_dcgrid_jacobi_inv", self.maxL[level], 64, self.g, C.c_uint8(level))
         self.d.launch("k_dcgrid_apply_pressure", self.B, 64, self.g)

@@ -88,12 +88,82 @@ def run(size, blocks, steps, warmup=3):
             "speedup_vs_ref_kernels": (t_kern / steps) / ours_ms, "same_block_count": same_topology}
 
 
+def stage_compare(size, blocks, sweeps, steps=3, warmup=2):
+    """Stage-matched GPU times of the reference's kernels and this library on
+    the same state (the reference's default scene): advectVelocity,
+    adaptTopology (the reference's kernels plus its host ranking),
+    project (divergence, cascade, gradient) and advectDensity, each bracketed
+    by CUDA events on its side's stream after an L2 flush, averaged over
+    `steps` steps; and the whole step (ours: dcg_step's graph). Both sides
+    start from the same parameters and make the same decisions, so they hold
+    identical states throughout."""
+    import torch
+    from dcgrid_gb300 import Simulation, capi
+    from oracle.ref_driver import Driver, RefDCGrid, REF_DIR
+    p = capi.default_params(*size, blocks)
+    p.jacobi_iters = sweeps
+    drv = Driver(os.path.join(REF_DIR, "ref_dcgrid.cubin"))
+    ref = RefDCGrid(drv, p)
+    ours = Simulation(p)
+    st = torch.cuda.Stream()
+    ours.set_stream(st.cuda_stream)
+    # the reference launches on the legacy default stream
+    streams = (torch.cuda.default_stream(), st)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(warmup):
+        ref.step(1)
+        ours.step(1)
+    ours.sync()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    names = ["advectVelocity", "adaptTopology", "project", "advectDensity"]
+    ours_fn = [ours.advect_velocity, ours.adapt, ours.project, ours.advect_scalars]
+    ref_fn = [ref.advectVelocity, ref.adaptTopology, ref.project, ref.advectDensity]
+    acc = {n: [0.0, 0.0] for n in names}
+    for _ in range(steps):
+        for k, n in enumerate(names):
+            for side, fn in ((0, ref_fn[k]), (1, ours_fn[k])):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                e0.record(streams[side])
+                fn()
+                e1.record(streams[side])
+                torch.cuda.synchronize()
+                acc[n][side] += e0.elapsed_time(e1)
+    ours.sync()
+    stages = {}
+    for n in names:
+        r, o = acc[n][0] / steps, acc[n][1] / steps
+        stages[n] = {"reference_ms": r, "ours_ms": o, "ratio": r / o}
+    # whole steps: ours through the captured graph
+    step_ms = 0.0
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0.record(st)
+        ours.step(1)
+        e1.record(st)
+        torch.cuda.synchronize()
+        step_ms += e0.elapsed_time(e1)
+    ref_step = sum(v["reference_ms"] for v in stages.values())
+    return {"size": list(size), "max_blocks": blocks, "levels": ref.levels, "sweeps_per_level": sweeps,
+            "steps": steps, "stages": stages, "reference_step_ms": ref_step, "ours_graph_step_ms": step_ms / steps,
+            "step_ratio": ref_step / (step_ms / steps),
+            "same_block_count": bool((ref.snapshot()["level"] != 255).sum() ==
+                                     (ours.get_topology()["pos"][:, 3] >= 0).sum())}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--stages", action="store_true", help="stage-matched times at 10 and 100 sweeps per level")
     args = ap.parse_args()
     for size, blocks in [((64, 128, 64), 3000), ((256, 256, 256), 40000)]:
-        print(json.dumps(run(size, blocks, args.steps)), flush=True)
+        if args.stages:
+            for sweeps in (10, 100):
+                print(json.dumps(stage_compare(size, blocks, sweeps, args.steps)), flush=True)
+        else:
+            print(json.dumps(run(size, blocks, args.steps)), flush=True)
 
 
 if __name__ == "__main__":

@@ -140,3 +140,67 @@ def test_full_step_adjoint_of_the_pressure_path_alone():
     an = float(np.dot(adj, d))
     assert abs(fd) > 1e-8  # buoyancy couples the scalars into the velocity
     assert abs(fd - an) <= 1e-6 * max(abs(fd), 1.0), (fd, an)
+
+
+def test_buoyant_rollout_adjoint_matches_fp64_central_differences():
+    """A buoyant rollout (temperature source, alpha = 0.1, beta = 0.3, an
+    emission map): the gradient of a dense density loss with respect to the
+    emission map through 8 steps of the full FP64 host adjoint equals FP64
+    central differences along unit directions. In FP64 a step of 1e-6 along a
+    unit direction moves no sample across a cell face or a level interface
+    (where the semi-Lagrangian sample is not differentiable)."""
+    from oracle.pyoracle import OracleSim
+    g, steps, em_n = 32, 8, 8
+    p = scenarios.differentiable(g, 2, iters=20, em_n=em_n)
+    p.n_scalars = 3
+    p.buoy_alpha, p.buoy_beta = 0.1, 0.3
+    p.src_enabled = 1
+    p.src_center[0], p.src_center[1], p.src_center[2] = g / 2.0, g / 8.0, g / 2.0
+    p.src_radius = 3.0
+    p.src_density, p.src_temperature, p.src_vapor = 0.0, 10.0, 0.0
+    rng = np.random.default_rng(2)
+    E0 = 0.05 * rng.random(em_n ** 3)
+    base = OracleSim(p, precision="double")
+    base.add_velocity_noise(0, 0.5)
+    probe = _clone(base, p)
+    probe.set_emission(E0)
+    decisions = []
+    for _ in range(steps):
+        probe.advect_velocity()
+        probe.adapt()
+        decisions.append(probe.get_last_adapt())
+        probe.project()
+        probe.advect_scalars()
+    target = 0.5 * probe.get_dense("density").reshape(-1)
+
+    def run(E):
+        o = _clone(base, p)
+        o.set_emission(E)
+        states = []
+        for t in range(steps):
+            states.append(_clone(o, p))
+            _step(o, *decisions[t])
+        return o, states
+
+    def loss(E):
+        o, _ = run(E)
+        r = o.get_dense("density").reshape(-1) - target
+        return float(r @ r)
+
+    o, states = run(E0)
+    nq, nc = p.n_scalars, o.num_cells
+    lam = np.zeros((3 + nq) * nc)
+    lrho = np.zeros(nc)
+    o.adjoint_dense(2.0 * (o.get_dense("density").reshape(-1) - target), lrho)
+    lam[3 * nc:4 * nc] = lrho
+    lam_e = np.zeros(em_n ** 3)
+    for t in range(steps - 1, -1, -1):
+        mv, rf = decisions[t]
+        lam = states[t].adjoint_step_full(lam, lam_e, moves=mv, refines=rf)
+    eps = 1e-6
+    for _ in range(4):
+        d = rng.standard_normal(em_n ** 3)
+        d /= np.linalg.norm(d)
+        fd = (loss(E0 + eps * d) - loss(E0 - eps * d)) / (2 * eps)
+        an = float(lam_e @ d)
+        assert abs(fd - an) <= 1e-5 * abs(fd), (fd, an)
