@@ -129,7 +129,6 @@ class DcgTuning(C.Structure):
         ("tile", C.c_int32 * 4), ("solve_cache", C.c_int32),
         ("solve_ctas_per_sm", C.c_int32), ("solve_barrier", C.c_int32), ("persistent", C.c_int32),
         ("round_ctas_per_sm", C.c_int16 * 4), ("round_cache", C.c_int8 * 4), ("round_barrier", C.c_int8 * 4), ("solve_ms", C.c_float), ("cells_ms", C.c_float * 4),
-        ("adapt_sort", C.c_int32),
     ]
 
 

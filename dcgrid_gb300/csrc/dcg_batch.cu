@@ -36,9 +36,7 @@ struct dcg_batch {
   // planes the cascade runs on: 0 = p, p~, div; 1 = e, e~, r (the correction)
   int planes = 0;
   uint32_t *binfo = nullptr;  // block descriptions of a cascade round, 13 words per block
-  uint32_t *epoch = nullptr;  // epoch-ordered solve variants: per arena block
   uint32_t *bar = nullptr, *errw = nullptr;
-  uint32_t *sort_bar = nullptr;  // grid-barrier words of the adaptation's single-launch sorts
   // concurrent cascades (solve_barrier bit 2): members with two different level
   // counts solved by two cooperative launch chains on parallel graph branches,
   // each with its own barrier words and block-description table
@@ -102,12 +100,10 @@ struct dcg_batch {
       return fail(DCG_E_INVALID, "solve_barrier must be 0..7 (bit 0 two-level barrier, bit 1 coarsest-aligned rounds, "
                                  "bit 2 concurrent cascades of the two level counts)");
     if (!solve_variant_valid(tune.solve_cache))
-      return fail(DCG_E_INVALID, "solve_cache must be 0, 3, 4, 8 or a pipelined variant 16, 18, 19, 32, 34, 35, 64, "
-                                 "66, 128, 130, 131, 160, 163");
+      return fail(DCG_E_INVALID, "solve_cache must be 0, 3, 4, 8 or a pipelined variant 16, 18, 19, 32, 34, 35, 64, 66");
     for (int k = 0; k < 4; k++)
-      if (tune.tile[k] != 1 && tune.tile[k] != 2 && tune.tile[k] != 4 && tune.tile[k] != 8 && tune.tile[k] != 16)
-        return fail(DCG_E_INVALID, "tiles must be 1 (staged), 16 (staged, interleaved tiles), 2, 4 or 8 blocks");
-    if (tune.adapt_sort != 0 && tune.adapt_sort != 1) return fail(DCG_E_INVALID, "adapt_sort must be 0 or 1");
+      if (tune.tile[k] != 1 && tune.tile[k] != 2 && tune.tile[k] != 4 && tune.tile[k] != 8)
+        return fail(DCG_E_INVALID, "tiles must be 1 (staged), 2, 4 or 8 blocks");
     solve_grid = batch_solve_grid(sms, tune.solve_cache, tune.solve_ctas_per_sm);
     if (solve_grid <= 0) return fail(DCG_E_CUDA, "cooperative level solve cannot be resident");
     for (int r = 0; r < 4; r++) {
@@ -218,7 +214,6 @@ struct dcg_batch {
       P.binfo = gi ? binfo2 : binfo;
       P.bar = gi ? bar2 : bar;
       P.err = errw;
-      P.epoch = epoch;
       for (int i = 0; i < P.n; i++) {
         P.d[i] = m[mem[i]]->D;
         P.arena[i] = arena_off[mem[i]];
@@ -267,7 +262,6 @@ struct dcg_batch {
         P.binfo = binfo;
         P.bar = bar;
         P.err = errw;
-        P.epoch = epoch;
         for (int i = 0; i < P.n; i++) {
           P.d[i] = m[g * BMAX + i]->D;
           P.arena[i] = arena_off[g * BMAX + i];
@@ -298,7 +292,7 @@ struct dcg_batch {
         const dcg_sim *s = m[g * BMAX + i];
         A[i] = AdaptMember{s->D, s->S, S2[g * BMAX + i], s->keys, s->vals, s->keys2, s->vals2};
       }
-      launch_adapt_batch(A, k, sms, stream, tune.adapt_sort == 0 ? sort_bar : nullptr, errw);
+      launch_adapt_batch(A, k, sms, stream);
     }
   }
   // Simulation::updateSimulation (simulation.cpp:104-112) for every member
@@ -398,7 +392,6 @@ struct dcg_batch {
     if ((rc = cuda(cudaStreamSynchronize(stream), "sync"))) return rc;
     cudaMemsetAsync(bar, 0, 4 * (64 + 32 * 18), stream);
     if (bar2) cudaMemsetAsync(bar2, 0, 4 * (64 + 32 * 18), stream);
-    cudaMemsetAsync(sort_bar, 0, 4 * 64, stream);
     cudaMemsetAsync(errw, 0, 4, stream);
     for (dcg_sim *s : m)
       if ((rc = s->reset_adaptive())) return fail(rc, "member reset: " + s->err);
@@ -459,7 +452,7 @@ struct dcg_batch {
     // cell stages: every tile of each stage, launched one CTA per block or
     // persistent; the launch form that gives the lower total is kept. Tile 1:
     // one warp per block through shared tiles (staged)
-    const int tiles[5] = {1, 2, 4, 8, 16};
+    const int tiles[4] = {1, 2, 4, 8};
     dcg_tuning best = tune;
     float total[2] = {0.f, 0.f};
     int tile_of[2][4];
@@ -469,7 +462,6 @@ struct dcg_batch {
       for (int stage = 0; stage < 4; stage++) {
         float best_ms = 1e30f;
         for (int tile : tiles) {
-          if (tile == 16 && stage >= 2) continue;  // the interleaved tiles serve the advections
           tune.tile[stage] = tile;
           const float ms = time_ms(reps, [&] { cells(stage); });
           if (ms < best_ms) {
@@ -491,7 +483,7 @@ struct dcg_batch {
     }
     // level solve: cache depth x CTAs per SM x barrier kind
     float best_solve = 1e30f;
-    for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66, 128, 130, 131, 160, 163}) {
+    for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66}) {
       const int occ = batch_solve_grid(sms, cache, 0) / std::max(1, sms);
       for (int k = 1; k <= occ; k++)
         for (int tb = 0; tb < 8; tb++) {  // bit 0: two-level barrier; bit 1: coarsest-aligned rounds;
@@ -518,7 +510,7 @@ struct dcg_batch {
       });
       float bms = base;
       best.round_ctas_per_sm[r] = 0;
-      for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66, 128, 130, 131, 160, 163}) {
+      for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66}) {
         const int occ = batch_solve_grid(sms, cache, 0) / std::max(1, sms);
         std::vector<int> ks = {-8, -4, -2};  // k < 0: one CTA per -k SMs (small rounds)
         for (int k = 1; k <= occ; k++) ks.push_back(k);
@@ -651,13 +643,11 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
   }
   if ((rc = b->alloc(&b->p_arena, cells)) || (rc = b->alloc(&b->pt_arena, cells)) ||
       (rc = b->alloc(&b->div_arena, cells)) || (rc = b->alloc(&b->binfo, 13 * (cells / BV))) ||
-      (rc = b->alloc(&b->epoch, cells / BV)) ||
-      (rc = b->alloc(&b->bar, 64 + 32 * 18)) || (rc = b->alloc(&b->errw, 4)) || (rc = b->alloc(&b->sort_bar, 64))) {
+      (rc = b->alloc(&b->bar, 64 + 32 * 18)) || (rc = b->alloc(&b->errw, 4))) {
     delete b;
     return rc;
   }
   cudaMemset(b->bar, 0, 4 * (64 + 32 * 18));
-  cudaMemset(b->sort_bar, 0, 4 * 64);
   for (int i = 0; i < n; i++)
     if (params[i].emission_n > 0)
       b->emis_floats += (size_t)params[i].emission_n * params[i].emission_n * params[i].emission_n;

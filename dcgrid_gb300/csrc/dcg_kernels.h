@@ -37,10 +37,6 @@ struct SortSeg {
   int nmul;
 };
 void launch_radix_sort_batch(const SortSeg *seg, int nseg, cudaStream_t st);
-// the same sort as one cooperative launch (grid barriers on bar, bounded waits
-// flagging err); false when the cooperative grid cannot be formed (nothing
-// launched)
-bool launch_radix_sort_coop(const SortSeg *seg, int nseg, uint32_t *bar, uint32_t *err, int sms, cudaStream_t st);
 
 // k_fluid.cu
 void launch_advect_velocity(const Dev &D, cudaStream_t st);
@@ -84,7 +80,6 @@ struct SolveBatch {
   const float *div;  // divergence arena (same layout as p)
   uint32_t *binfo;   // block descriptions of the round's level, 13 words per level block
   uint32_t *bar, *err;
-  uint32_t *epoch;   // epoch-ordered variants: sweeps completed, per arena block (cell / 64)
   unsigned long long arena[BMAX];  // first cell of member s in the arenas
   Dev d[BMAX];
 };
@@ -130,10 +125,7 @@ struct AdaptMember {
   SortScratch S, S2;
   uint32_t *keys, *vals, *keys2, *vals2;
 };
-// sort_bar (grid-barrier words, 64 u32) and err: the sorts run as single
-// cooperative launches; sort_bar null: one launch per sort phase
-void launch_adapt_batch(const AdaptMember *m, int n, int sms, cudaStream_t st, uint32_t *sort_bar = nullptr,
-                        uint32_t *err = nullptr);
+void launch_adapt_batch(const AdaptMember *m, int n, int sms, cudaStream_t st);
 void launch_stats(const Dev &D, cudaStream_t st);
 void launch_fields_to_dense(const Dev &D, const void *src, int mode, float *dst, cudaStream_t st);
 void launch_h16_to_f32(const uint16_t *src, float *dst, long long n, int mode, cudaStream_t st);

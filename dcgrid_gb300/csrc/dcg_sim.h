@@ -513,7 +513,6 @@ struct dcg_sim {
     SB.binfo = D.binfo;
     SB.bar = D.bar;
     SB.err = D.err;
-    SB.epoch = D.epoch;
     SB.arena[0] = 0;
     SB.d[0] = D;
     if (pp) {  // the prolongation and the cached alpha*div read these through D

@@ -839,21 +839,7 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
 // The copies read the previous sweep's results written by other SMs; the grid
 // barrier's fences order them. Block descriptions come from the launch's
 // shared cache when they fit, else from the global table, through shuffles.
-// EP = 1: the sweeps are ordered block by block instead of by grid barriers.
-// Warp w takes the CTA's blocks w, w + 8, ... in every sweep (no claims); a
-// block's copies for sweep `it` wait until each same-level face neighbour has
-// completed sweep it - 1 (its epoch word, P.epoch[arena block], reached it),
-// so the values read are that sweep's and no neighbour still reads the
-// buffer being written; coarser neighbours are constant during the level and
-// need no wait. After its store the warp publishes the block's epoch it + 1
-// (__syncwarp, then a release store by lane 0: the warp's writes are ordered
-// before it); the waits are acquire loads followed by __syncwarp, which order
-// the warp's later copies after them. Every warp always waits only for sweep
-// it - 1 of others, and the warp with the smallest sweep always proceeds, so
-// the ordering cannot deadlock; a wait still gives up after 2^22 polls and
-// records DCG_DEVERR_TIMEOUT. The copy pipeline drains at the end of each
-// sweep (a warp never waits on a block it has not yet finished).
-template <int CACHE, int NB, int EP = 0>
+template <int CACHE, int NB>
 __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long long *s_end, const int *s_lev,
                                                 uint32_t *s_cache, long long total, unsigned nctas, int sweeps,
                                                 int tree) {
@@ -896,19 +882,6 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
     if (tree & 1) grid_barrier_tree(P.bar, P.err, nctas);
     else grid_barrier(P.bar, P.err, nctas);
   };
-  // arena index of the first cell of CTA-local block k (its description's word 0)
-  auto own_of = [&](int k) -> uint32_t {
-    if (cached) return s_cache[k * BI_WORDS];
-    const long long gb = ((long long)(k >> 3) * nctas + blockIdx.x) * W + (k & 7);
-    return __ldcg(P.binfo + gb * BI_WORDS);
-  };
-  if constexpr (EP) {
-    // the epochs of this launch start at 0 for every block, visible to all
-    // CTAs after one grid barrier
-    if (lane == 0)
-      for (int k = w; k < kcount; k += W) st_relaxed(P.epoch + (own_of(k) >> 6), 0u);
-    barrier();
-  }
   // per buffer: arena index of the block's first cell and alpha (bits); own = ~0u: no block
   uint32_t b_own[NB], b_alpha[NB];
   // shared-memory addresses of the lane's copy targets in buffer 0 (buffer b: + b * TILE * 4)
@@ -923,19 +896,12 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
     float *dst = (it & 1) ? P.p : P.pt;
     const float *srcl = src + 2 * lane;
     float2 *dstl = reinterpret_cast<float2 *>(dst) + lane;
-    if (!EP && t == 0) s_next[(it + 1) & 1] = 0u;  // the next sweep's counter; its last use ended before the barrier
+    if (t == 0) s_next[(it + 1) & 1] = 0u;  // the next sweep's counter; its last use ended before the barrier
     unsigned *cnt = &s_next[it & 1];
-    int j_next = 0;  // EP: the warp's next block of this sweep is CTA-local block j_next * W + w
     auto issue = [&](int buf) {
-      int k;
-      if constexpr (EP) {
-        k = j_next * W + w;
-        j_next++;
-      } else {
-        unsigned kk = 0;
-        if (lane == 0) kk = atomicAdd(cnt, 1u);
-        k = (int)__shfl_sync(full, kk, 0);
-      }
+      unsigned kk = 0;
+      if (lane == 0) kk = atomicAdd(cnt, 1u);
+      const int k = (int)__shfl_sync(full, kk, 0);
       const bool act = k < kcount;  // warp-uniform; a warp's claims only grow
       uint32_t biw = 0;
       if (act && lane < BI_WORDS) {
@@ -949,26 +915,6 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
       const uint32_t own = __shfl_sync(full, biw, 0);
       const uint32_t alpha = __shfl_sync(full, biw, 1);
       const uint32_t c11 = __shfl_sync(full, biw, 11), c12 = __shfl_sync(full, biw, 12);
-      if constexpr (EP) {
-        // lane f < 6 waits for face f's block when it is a same-level neighbour
-        const uint32_t fbase = __shfl_sync(full, biw, 5 + (lane < 6 ? lane : 0));
-        if (act && it > 0 && lane < 6) {
-          const uint32_t code = ((lane < 4 ? c11 : c12) >> (8 * (lane & 3))) & 0xFFu;
-          if (code == 0u) {
-            const unsigned *ep = P.epoch + (fbase >> 6);
-            volatile uint32_t *errv = P.err;
-            unsigned spins = 0;
-            while (ld_acquire(ep) < (unsigned)it) {
-              if (++spins > kPollLimit || (*errv & 8u)) {
-                atomicOr(P.err, 8u);
-                break;
-              }
-              __nanosleep(32);
-            }
-          }
-        }
-        __syncwarp();
-      }
       uint32_t fb[3];
 #pragma unroll
       for (int q = 0; q < 3; q++) fb[q] = __shfl_sync(full, biw, 5 + (int)(hax[q] >> 12));
@@ -1031,15 +977,11 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
         res.x = div6(L.x + R.x + Dn.x + Up.x + Bk + ab.y - adA);
         res.y = div6(L.y + R.y + Dn.y + Up.y + ab.x + Fw - adB);
         dstl[own >> 1] = res;
-        if constexpr (EP) {
-          __syncwarp();  // the warp's stores, then the block's epoch
-          if (lane == 0) st_release_u32(P.epoch + (own >> 6), (uint32_t)it + 1u);
-        }
       }
       __syncwarp();  // buffer `buf` may be refilled by the next issue
     }
     cp_async_wait<0>();
-    if (!EP && it + 1 < sweeps) barrier();
+    if (it + 1 < sweeps) barrier();
   }
 }
 
@@ -1054,7 +996,7 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
 // store per cell. Larger levels are swept one block per warp through a 6^3
 // shared-memory tile holding the block and its face halo. Arithmetic is that
 // of k_jacobi (identical results).
-template <int CACHE, int NB = 0, int MB = DCG_PIPE_MINB, int EP = 0>
+template <int CACHE, int NB = 0, int MB = DCG_PIPE_MINB>
 __global__ void __launch_bounds__(256, NB ? MB : DCG_SOLVE_MINB)
     k_level_solve_batch(const __grid_constant__ SolveBatch P, int round, int sweeps, int tree) {
   __shared__ long long s_end[BMAX];
@@ -1126,7 +1068,7 @@ __global__ void __launch_bounds__(256, NB ? MB : DCG_SOLVE_MINB)
       if (it + 1 < sweeps) barrier();
     }
   } else if constexpr (NB > 0) {
-    solve_pipelined<CACHE, NB, EP>(P, s_end, s_lev, s_cache, total, nctas, sweeps, tree);
+    solve_pipelined<CACHE, NB>(P, s_end, s_lev, s_cache, total, nctas, sweeps, tree);
   } else {
     // staged sweeps, one warp per block: per round each of the CTA's 8 warps
     // takes one block; its 64 cells and 96 face-halo cells go into a 6^3 tile
@@ -1714,201 +1656,6 @@ __global__ void __launch_bounds__(256, DCG_ADV_MINB) k_advect_staged(const __gri
     pair_sync();  // the tiles are refilled for the next block
   }
 }
-// The same advection with one interleaved tile per block: each apron cell's
-// fluidity and sampled values (velocity x, y, z, or up to three scalars) sit
-// together in one float4, so a cell reads each stencil corner with one
-// 128-bit shared load (8 per cell instead of 32) and a tile cell is written
-// with one 128-bit store. Strides AX4 = 60, AY4 = 10 (float4 units) put the
-// 2x2x2 cells of a quarter warp, and each of their corners, in distinct bank
-// quads. Arithmetic as in k_advect_staged (identical results).
-constexpr int AX4 = 60, AY4 = 10, TILE4 = 5 * AX4 + 5 * AY4 + 6;
-// resident CTAs per SM the register allocation targets (3: the eight corner
-// values stay in registers)
-#ifndef DCG_ADV4_MINB
-#define DCG_ADV4_MINB 3
-#endif
-template <int STAGE, int MODE, int NQ>
-__global__ void __launch_bounds__(256, DCG_ADV4_MINB) k_advect_staged4(const __grid_constant__ CellBatch P) {
-  constexpr int NBK = 4;
-  __shared__ long long s_end[BMAX * MAXL];
-  __shared__ __align__(16) float4 s_t4[NBK][TILE4];
-  __shared__ uint32_t s_slot[2][3][64];  // apron slots a = c + 64 r of thread c (pk ~0u: none)
-  const int nseg = P.n * MAXL;
-  for (int i = threadIdx.x; i < nseg; i += blockDim.x) {
-    const Dev &D = P.d[i / MAXL];
-    const int l = i % MAXL;
-    const bool mine = STAGE == 0 || (D.g.mixed == MODE && D.g.nq == NQ);
-    s_end[i] = (mine && l < D.g.levels) ? __ldcg(D.load + l) : 0;
-  }
-  if (threadIdx.x < 64) {
-    const int c = threadIdx.x;
-#pragma unroll 1
-    for (int r = 0; r < 3; r++) s_slot[0][r][c] = ~0u, s_slot[1][r][c] = 0u;
-    int cnt = 0;
-    for (int idx = 0; idx < AW * AW * AW; idx++) {
-      const int ax = idx / 36, ay = (idx / 6) % 6, az = idx % 6;
-      if (ax > 0 && ax < AW - 1 && ay > 0 && ay < AW - 1 && az > 0 && az < AW - 1) continue;
-      if ((cnt & 63) == c) {
-        const int same = local_of((ax - 1) & 3, (ay - 1) & 3, (az - 1) & 3);
-        const int self = local_of(clampi(ax, 1, BW) - 1, clampi(ay, 1, BW) - 1, clampi(az, 1, BW) - 1);
-        const int quirk = local_of(clampi(ax, 1, BW) & 3, clampi(ay, 1, BW) & 3, clampi(az, 1, BW) & 3);
-        const int d = dir_of(ax) * 9 + dir_of(ay) * 3 + dir_of(az);
-        s_slot[0][cnt >> 6][c] = (uint32_t)(ax * AX4 + ay * AY4 + az) | ((uint32_t)same << 9) |
-                                 ((uint32_t)self << 15) | ((uint32_t)quirk << 21);
-        s_slot[1][cnt >> 6][c] = (uint32_t)ax | ((uint32_t)ay << 4) | ((uint32_t)az << 8) | ((uint32_t)d << 12);
-      }
-      cnt++;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0)
-    for (int i = 1; i < nseg; i++) s_end[i] += s_end[i - 1];
-  __syncthreads();
-  const long long total = s_end[nseg - 1];
-  const int k = threadIdx.x >> 6, c = threadIdx.x & 63, lane = threadIdx.x & 31;
-  int lx, ly, lz;
-  local_xyz(c, lx, ly, lz);
-  const int oC = (lx + 1) * AX4 + (ly + 1) * AY4 + (lz + 1);
-  const unsigned full = 0xffffffffu;
-  auto pair_sync = [&]() { asm volatile("bar.sync %0, 64;" ::"r"(1 + k) : "memory"); };
-  float4 *T = s_t4[k];
-  int seg = 0;
-  for (long long t = (long long)blockIdx.x * NBK + k; t < total; t += (long long)gridDim.x * NBK) {
-    while (t >= s_end[seg]) seg++;
-    const Dev &D = P.d[seg / MAXL];
-    const int l = seg % MAXL;
-    const uint32_t b = (uint32_t)(D.g.off[l] + (t - (seg ? s_end[seg - 1] : 0)));
-    const int4 bp = D.pos[b];
-    const size_t own = (size_t)b * BV;
-    const size_t cell = own + c;
-    const uint32_t e = lane < 27 ? D.nbr[27u * b + lane] : OUT;   // each warp keeps a copy
-    const uint32_t ch = lane < 8 ? D.child[8u * b + lane] : NONE;  // the block's subblock children
-    const float va = D.v[0][cell], vb = D.v[1][cell], vc = D.v[2][cell];
-    float qa = 0.f, qb = 0.f;  // own density / temperature (buoyancy)
-    if constexpr (STAGE == 0) {
-      T[oC] = make_float4(D.w[cell], va, vb, vc);
-      if (D.ph.buoy_a != 0.f || D.ph.buoy_b != 0.f) {
-        qa = q_ld(D, 0, cell);
-        if (D.g.nq > 1) qb = q_ld(D, 1, cell);
-      }
-    } else {
-      T[oC] = make_float4(D.w[cell], q_ldm<MODE>(D, 0, cell), NQ > 1 ? q_ldm<MODE>(D, 1, cell) : 0.f,
-                          NQ > 2 ? q_ldm<MODE>(D, 2, cell) : 0.f);
-    }
-#pragma unroll
-    for (int r = 0; r < 3; r++) {
-      const uint32_t pk = s_slot[0][r][c], ga = s_slot[1][r][c];
-      const uint32_t ed = __shfl_sync(full, e, (int)((ga >> 12) & 31u));
-      if (pk != ~0u) {
-        const size_t ac = halo_cell(D, b, bp, ed, pk, ga);
-        const uint32_t at = pk & 511u;
-        if constexpr (STAGE == 0) {
-          T[at] = make_float4(D.w[ac], D.v[0][ac], D.v[1][ac], D.v[2][ac]);
-        } else {
-          T[at] = make_float4(D.w[ac], q_ldm<MODE>(D, 0, ac), NQ > 1 ? q_ldm<MODE>(D, 1, ac) : 0.f,
-                              NQ > 2 ? q_ldm<MODE>(D, 2, ac) : 0.f);
-        }
-      }
-    }
-    pair_sync();
-    const bool leaf = __shfl_sync(full, ch, c >> 3) == NONE;
-    float px = 0.f, py = 0.f, pz = 0.f;
-    bool fast = false;
-    int sub = 0;
-    if (leaf) {
-      const float scale = (float)(1 << bp.w);
-      const float alpha = D.ph.dt * D.ph.rdx;
-      px = ((float)(bp.x + lx) + 0.5f) * scale - va * alpha;
-      py = ((float)(bp.y + ly) + 0.5f) * scale - vb * alpha;
-      pz = ((float)(bp.z + lz) + 0.5f) * scale - vc * alpha;
-      fast = sample_in_own(D, bp, px, py, pz, sub);
-    }
-    const bool sub_leaf = __shfl_sync(full, ch, sub) == NONE;
-    fast = fast && (bp.w == 0 || sub_leaf);
-    if (leaf && !fast) {
-      if constexpr (STAGE == 0) advect_velocity_cell_ool(D, b, c);
-      else advect_scalars_cell_ool<MODE, NQ>(D, b, c);
-    } else {
-      float o[3] = {0.f, 0.f, 0.f};
-      if (leaf) {
-        // sample_tile's weights (same operations), the corner values kept
-        const int lev = bp.w, scl = 1 << lev;
-        const float scaleInv = __int_as_float((127 - lev) << 23);
-        const float x = px * scaleInv - 0.5f, y = py * scaleInv - 0.5f, z = pz * scaleInv - 0.5f;
-        const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
-        const float dx = x - xf, dy = y - yf, dz = z - zf;
-        const int x0 = (int)xf, y0 = (int)yf, z0 = (int)zf;
-        const int i = clampi(x0 + 1 - bp.x, 0, AW - 2), j = clampi(y0 + 1 - bp.y, 0, AW - 2),
-                  kz = clampi(z0 + 1 - bp.z, 0, AW - 2);
-        const float4 *Tc = T + (i * AX4 + j * AY4 + kz);
-        const float Dx = 1.f - dx, Dy = 1.f - dy, Dz = 1.f - dz;
-        float wt[8], val[8][3];
-#pragma unroll
-        for (int kk = 0; kk < 8; kk++) {
-          const float4 cv = Tc[tile_delta<AX4, AY4>(kk)];
-          const float X = (kk & 4) ? dx : Dx, Y = (kk & 2) ? dy : Dy, Z = (kk & 1) ? dz : Dz;
-          wt[kk] = cv.x * X * Y * Z;
-          val[kk][0] = cv.y;
-          val[kk][1] = cv.z;
-          val[kk][2] = cv.w;
-        }
-        const float wAcc = wt[0] + wt[1] + wt[2] + wt[3] + wt[4] + wt[5] + wt[6] + wt[7];
-        const float wInv = 1.f / wAcc;
-#pragma unroll
-        for (int kk = 0; kk < 8; kk++) wt[kk] = wt[kk] * wInv;
-        if (!(wAcc < 1e-6f)) {
-          const bool inside = x0 >= 0 && y0 >= 0 && z0 >= 0 && (x0 + 1) * scl < D.g.gx && (y0 + 1) * scl < D.g.gy &&
-                              (z0 + 1) * scl < D.g.gz;
-#pragma unroll
-          for (int kk = 0; kk < 8; kk++) {
-            const int cx = (kk & 4) ? x0 + 1 : x0, cy = (kk & 2) ? y0 + 1 : y0, cz = (kk & 1) ? z0 + 1 : z0;
-            if constexpr (STAGE == 0) {
-              float vx = val[kk][0], vy = val[kk][1], vz = val[kk][2];
-              if (!inside) vel_bc(D.g, D.ph, vx, vy, vz, cx, cy, cz, scl);
-              if (kk == 0) {
-                o[0] = vx * wt[0]; o[1] = vy * wt[0]; o[2] = vz * wt[0];
-              } else {
-                o[0] = o[0] + vx * wt[kk]; o[1] = o[1] + vy * wt[kk]; o[2] = o[2] + vz * wt[kk];
-              }
-            } else {
-              const int mode = inside ? 0 : q_bc_mode(D.g, D.ph, cx, cy, cz, scl);
-#pragma unroll
-              for (int kq = 0; kq < NQ; kq++) {
-                const float qc = mode == 0 ? val[kk][kq] : (mode == 1 && kq == 0 ? D.ph.d_emit : 0.f);
-                o[kq] = (kk == 0) ? qc * wt[0] : o[kq] + qc * wt[kk];
-              }
-            }
-          }
-        }
-        if constexpr (STAGE == 0) {
-          if (D.ph.buoy_a != 0.f || D.ph.buoy_b != 0.f) {
-            float f = -D.ph.buoy_a * qa;
-            if (D.g.nq > 1) f = f + D.ph.buoy_b * (qb - D.ph.t_amb);
-            o[1] = o[1] + D.ph.dt * f;
-          }
-        } else {
-          if (D.ph.em_n > 0)
-            o[0] = o[0] + D.ph.dt * emission_at(D.g, D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w);
-          if (D.ph.src) {
-            if (in_source(D.ph, bp.x + lx, bp.y + ly, bp.z + lz, 1 << bp.w))
-#pragma unroll
-              for (int kq = 0; kq < NQ; kq++) o[kq] = src_value_at(D.ph, kq, bp.x + lx, bp.y + ly, bp.z + lz, bp.w);
-          }
-        }
-      }
-      if constexpr (STAGE == 0) {
-        D.tv[0][cell] = o[0];
-        D.tv[1][cell] = o[1];
-        D.tv[2][cell] = o[2];
-      } else {
-#pragma unroll
-        for (int kq = 0; kq < NQ; kq++) tq_stm<MODE>(D, kq, cell, o[kq]);
-      }
-    }
-    pair_sync();  // the tile is refilled for the next block
-  }
-}
-
 template <int STAGE, int MODE, int NQ> static unsigned advect_grid() {
   static unsigned g = 0;
   if (!g) {
@@ -1919,31 +1666,6 @@ template <int STAGE, int MODE, int NQ> static unsigned advect_grid() {
     g = (unsigned)(sms * (occ > 0 ? occ : 1));
   }
   return g;
-}
-template <int STAGE, int MODE, int NQ> static unsigned advect4_grid() {
-  static unsigned g = 0;
-  if (!g) {
-    int dev = 0, sms = 0, occ = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_advect_staged4<STAGE, MODE, NQ>, 256, 0);
-    g = (unsigned)(sms * (occ > 0 ? occ : 1));
-  }
-  return g;
-}
-static void launch_advect_staged4(int stage, const CellBatch &P, cudaStream_t st) {
-  if (stage == 0) {
-    k_advect_staged4<0, 0, 1><<<advect4_grid<0, 0, 1>(), 256, 0, st>>>(P);
-    return;
-  }
-  bool has[3][2] = {};
-  for (int i = 0; i < P.n; i++) has[P.d[i].g.mixed][P.d[i].g.nq == 3 ? 1 : 0] = true;
-  if (has[0][0]) k_advect_staged4<1, 0, 1><<<advect4_grid<1, 0, 1>(), 256, 0, st>>>(P);
-  if (has[0][1]) k_advect_staged4<1, 0, 3><<<advect4_grid<1, 0, 3>(), 256, 0, st>>>(P);
-  if (has[1][0]) k_advect_staged4<1, 1, 1><<<advect4_grid<1, 1, 1>(), 256, 0, st>>>(P);
-  if (has[1][1]) k_advect_staged4<1, 1, 3><<<advect4_grid<1, 1, 3>(), 256, 0, st>>>(P);
-  if (has[2][0]) k_advect_staged4<1, 2, 1><<<advect4_grid<1, 2, 1>(), 256, 0, st>>>(P);
-  if (has[2][1]) k_advect_staged4<1, 2, 3><<<advect4_grid<1, 2, 3>(), 256, 0, st>>>(P);
 }
 static void launch_advect_staged(int stage, const CellBatch &P, cudaStream_t st) {
   if (stage == 0) {
@@ -2043,11 +1765,6 @@ static void cells_batch_tb(int stage, const CellBatch &P, unsigned grid, cudaStr
   }
 }
 void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st, bool persistent) {
-  if (tile == 16 && stage < 2) {  // staged advection, interleaved float4 tiles
-    launch_advect_staged4(stage, P, st);
-    return;
-  }
-  if (tile == 16) tile = 1;
   if (tile == 1) {  // staged, one warp per block
     if (stage < 2) launch_advect_staged(stage, P, st);
     else if (stage == 2) k_cells_staged<2><<<staged_grid(2), 256, 0, st>>>(P);
@@ -2081,24 +1798,22 @@ void launch_restrict_batch(RestrictBatch &P, cudaStream_t st) {
   if (acc > 0) k_restrict_batch<<<(unsigned)acc, 256, 0, st>>>(P);
 }
 
-template <int C, int NB, int MB = DCG_PIPE_MINB, int EP = 0>
+template <int C, int NB, int MB = DCG_PIPE_MINB>
 static int solve_batch_occupancy() {
   // static + dynamic shared memory above 48 KB needs the opt-in
   const int smem = C * 8 * 256 * 4;
-  if (smem > 0 && cudaFuncSetAttribute(k_level_solve_batch<C, NB, MB, EP>,
+  if (smem > 0 && cudaFuncSetAttribute(k_level_solve_batch<C, NB, MB>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
     return 0;
   int a = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_level_solve_batch<C, NB, MB, EP>, 256, smem) !=
-      cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_level_solve_batch<C, NB, MB>, 256, smem) != cudaSuccess)
     return 0;
   return a;
 }
 // solve variants: cache depth 0, 3, 4 or 8 (cells per thread of the small-level
 // path; 8 KB of dynamic shared memory each); 16 + c: pipelined staged sweeps
 // with two tile buffers per warp (registers for 4 CTAs per SM), 32 + c: three
-// buffers, 64 + c: two buffers with registers for 5 CTAs per SM; 128 + c and
-// 160 + c: two and three buffers, sweeps ordered by block epochs
+// buffers, 64 + c: two buffers with registers for 5 CTAs per SM
 static int solve_occupancy(int cache) {
   switch (cache) {
     case 8: return solve_batch_occupancy<8, 0>();
@@ -2113,18 +1828,12 @@ static int solve_occupancy(int cache) {
     case 32 + 3: return solve_batch_occupancy<3, 3>();
     case 64: return solve_batch_occupancy<0, 2, 5>();
     case 64 + 2: return solve_batch_occupancy<2, 2, 5>();
-    case 128: return solve_batch_occupancy<0, 2, DCG_PIPE_MINB, 1>();
-    case 128 + 2: return solve_batch_occupancy<2, 2, DCG_PIPE_MINB, 1>();
-    case 128 + 3: return solve_batch_occupancy<3, 2, DCG_PIPE_MINB, 1>();
-    case 160: return solve_batch_occupancy<0, 3, DCG_PIPE_MINB, 1>();
-    case 160 + 3: return solve_batch_occupancy<3, 3, DCG_PIPE_MINB, 1>();
     default: return 0;
   }
 }
 bool solve_variant_valid(int cache) {
   return cache == 0 || cache == 3 || cache == 4 || cache == 8 || cache == 16 || cache == 18 || cache == 19 ||
-         cache == 32 || cache == 34 || cache == 35 || cache == 64 || cache == 66 || cache == 128 || cache == 130 ||
-         cache == 131 || cache == 160 || cache == 163;
+         cache == 32 || cache == 34 || cache == 35 || cache == 64 || cache == 66;
 }
 int batch_solve_grid(int sms, int cache, int ctas_per_sm) {
   const int occ = solve_occupancy(cache);
@@ -2158,11 +1867,6 @@ void launch_level_solve_batch(const SolveBatch &P, int round, int sweeps, int gr
     case 35: cudaLaunchKernelEx(&cfg, k_level_solve_batch<3, 3>, P, round, sweeps, tree); break;
     case 64: cudaLaunchKernelEx(&cfg, k_level_solve_batch<0, 2, 5>, P, round, sweeps, tree); break;
     case 66: cudaLaunchKernelEx(&cfg, k_level_solve_batch<2, 2, 5>, P, round, sweeps, tree); break;
-    case 128: cudaLaunchKernelEx(&cfg, k_level_solve_batch<0, 2, DCG_PIPE_MINB, 1>, P, round, sweeps, tree); break;
-    case 130: cudaLaunchKernelEx(&cfg, k_level_solve_batch<2, 2, DCG_PIPE_MINB, 1>, P, round, sweeps, tree); break;
-    case 131: cudaLaunchKernelEx(&cfg, k_level_solve_batch<3, 2, DCG_PIPE_MINB, 1>, P, round, sweeps, tree); break;
-    case 160: cudaLaunchKernelEx(&cfg, k_level_solve_batch<0, 3, DCG_PIPE_MINB, 1>, P, round, sweeps, tree); break;
-    case 163: cudaLaunchKernelEx(&cfg, k_level_solve_batch<3, 3, DCG_PIPE_MINB, 1>, P, round, sweeps, tree); break;
     default: cudaLaunchKernelEx(&cfg, k_level_solve_batch<0, 0>, P, round, sweeps, tree); break;
   }
 }

@@ -7,7 +7,6 @@
 // __match_any_sync inside a warp and a per-digit running offset across warps
 // and rounds, so the order of equal keys is preserved (ties stay in index
 // order, which the selection relies on).
-#include <algorithm>
 #include <utility>
 
 #include "dcg_kernels.h"
@@ -187,102 +186,6 @@ template <int OP> __global__ void __launch_bounds__(RS_THREADS) k_rs_batch(const
   if constexpr (OP == 3)
     rs_scatter_body(P.kin[s], P.vin[s], P.kout[s], P.vout[s], eff_n(P.n[s], P.ndev[s], P.nmul[s]), P.shift,
                     P.hist[s], P.totals[s], P.nt[s], P.active[s], bx, gx);
-}
-
-// All four passes of a batched sort in one cooperative launch: the four phases
-// of each pass (tile histograms, column scans, digit bases, stable scatter)
-// are separated by grid barriers, and every CTA loops over the phase's work
-// items of all segments. Same bodies and order as the launch-per-phase form,
-// so the same result; one launch instead of sixteen. Data written by other
-// CTAs in the launch is read through L2 (the bodies load with __ldcg).
-struct SortCoopP {
-  int nseg, pad;
-  long long end[SORT_SEGS];  // cumulative tile counts
-  uint32_t *k0[SORT_SEGS], *v0[SORT_SEGS], *k1[SORT_SEGS], *v1[SORT_SEGS];
-  uint32_t *hist[SORT_SEGS], *totals[SORT_SEGS];
-  const long long *active[SORT_SEGS];
-  long long n[SORT_SEGS], nt[SORT_SEGS];
-  const long long *ndev[SORT_SEGS];
-  int nmul[SORT_SEGS];
-};
-__global__ void __launch_bounds__(RS_THREADS) k_rs_coop(const __grid_constant__ SortCoopP P, uint32_t *bar,
-                                                        uint32_t *err) {
-  const unsigned G = gridDim.x;
-  const long long tiles = P.end[P.nseg - 1];
-  auto seg_of = [&](long long t) {
-    int s = 0;
-    while (s < P.nseg - 1 && t >= P.end[s]) s++;
-    return s;
-  };
-  for (int pass = 0; pass < 4; pass++) {
-    const int shift = 8 * pass;
-    const bool odd = pass & 1;
-    for (long long t = blockIdx.x; t < tiles; t += G) {
-      const int s = seg_of(t);
-      const unsigned bx = (unsigned)(t - (s ? P.end[s - 1] : 0));
-      rs_hist_body(odd ? P.k1[s] : P.k0[s], eff_n(P.n[s], P.ndev[s], P.nmul[s]), shift, P.hist[s], P.nt[s],
-                   P.active[s], bx, 0);
-    }
-    grid_barrier(bar, err, G);
-    for (long long q = blockIdx.x; q < (long long)P.nseg * 256; q += G) {
-      const int s = (int)(q >> 8);
-      if (P.n[s] > 0) rs_scan_cols_body(P.hist[s], P.nt[s], P.totals[s], P.active[s], (unsigned)(q & 255), 0);
-    }
-    grid_barrier(bar, err, G);
-    for (int s = blockIdx.x; s < P.nseg; s += G)
-      if (P.n[s] > 0) rs_scan_totals_body(P.totals[s], P.active[s], 0, 0);
-    grid_barrier(bar, err, G);
-    for (long long t = blockIdx.x; t < tiles; t += G) {
-      const int s = seg_of(t);
-      const unsigned bx = (unsigned)(t - (s ? P.end[s - 1] : 0));
-      rs_scatter_body(odd ? P.k1[s] : P.k0[s], odd ? P.v1[s] : P.v0[s], odd ? P.k0[s] : P.k1[s],
-                      odd ? P.v0[s] : P.v1[s], eff_n(P.n[s], P.ndev[s], P.nmul[s]), shift, P.hist[s], P.totals[s],
-                      P.nt[s], P.active[s], bx, 0);
-    }
-    if (pass < 3) grid_barrier(bar, err, G);
-  }
-}
-static int coop_sort_grid(int sms) {
-  static int per_sm = -1;
-  if (per_sm < 0) {
-    int a = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_rs_coop, RS_THREADS, 0) != cudaSuccess) a = 0;
-    per_sm = a;
-  }
-  return per_sm > 0 ? std::min(per_sm, 2) * sms : 0;
-}
-bool launch_radix_sort_coop(const SortSeg *seg, int nseg, uint32_t *bar, uint32_t *err, int sms, cudaStream_t st) {
-  const int grid = coop_sort_grid(sms);
-  if (grid <= 0 || !bar || !err) return false;
-  SortCoopP P{};
-  P.nseg = nseg;
-  long long e = 0;
-  for (int i = 0; i < nseg; i++) {
-    P.n[i] = seg[i].n > 0 ? seg[i].n : 0;
-    P.nt[i] = sort_tiles(P.n[i]);
-    P.hist[i] = seg[i].s.hist;
-    P.totals[i] = seg[i].s.totals;
-    P.active[i] = seg[i].active;
-    P.ndev[i] = seg[i].ndev;
-    P.nmul[i] = seg[i].nmul;
-    P.k0[i] = seg[i].keys;
-    P.v0[i] = seg[i].vals;
-    P.k1[i] = seg[i].s.k1;
-    P.v1[i] = seg[i].s.v1;
-    if (P.n[i] > 0) e += P.nt[i];
-    P.end[i] = e;
-  }
-  if (e == 0) return true;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3(RS_THREADS);
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeCooperative;
-  attr[0].val.cooperative = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_rs_coop, P, bar, err) == cudaSuccess;
 }
 
 void launch_radix_sort_batch(const SortSeg *seg, int nseg, cudaStream_t st) {

@@ -876,17 +876,11 @@ struct AdaptLauncher {
   const AdaptMember *m;
   int n;
   unsigned gs;  // grid-stride CTAs per member
-  int sms;
   cudaStream_t st;
-  // grid-barrier words and error word of the single-launch sorts (null: one
-  // launch per sort phase)
-  uint32_t *sort_bar = nullptr, *err = nullptr;
-  void sort(const SortSeg *seg, int ns) {
-    if (!(sort_bar && launch_radix_sort_coop(seg, ns, sort_bar, err, sms, st))) launch_radix_sort_batch(seg, ns, st);
-  }
+  void sort(const SortSeg *seg, int ns) { launch_radix_sort_batch(seg, ns, st); }
   AdaptBatchP P{};
 
-  AdaptLauncher(const AdaptMember *mm, int nn, int sms_, cudaStream_t s) : m(mm), n(nn), sms(sms_), st(s) {
+  AdaptLauncher(const AdaptMember *mm, int nn, int sms, cudaStream_t s) : m(mm), n(nn), st(s) {
     P.n = n;
     for (int i = 0; i < n; i++) P.d[i] = m[i].D;
     const int total = sms > 0 ? sms * 4 : 512;
@@ -1033,13 +1027,9 @@ struct AdaptLauncher {
 };
 }  // namespace
 
-void launch_adapt_batch(const AdaptMember *m, int n, int sms, cudaStream_t st, uint32_t *sort_bar,
-                        uint32_t *err) {
+void launch_adapt_batch(const AdaptMember *m, int n, int sms, cudaStream_t st) {
   if (n <= 0 || n > BMAX) return;
-  AdaptLauncher L(m, n, sms, st);
-  L.sort_bar = sort_bar;
-  L.err = err;
-  L.run();
+  AdaptLauncher(m, n, sms, st).run();
 }
 
 // ------------------------------------------------------------------ stats

@@ -345,18 +345,12 @@ typedef struct dcg_batch dcg_batch;
 typedef struct {
   int32_t tile[4];           /* blocks of 64 cells per CTA (2, 4 or 8) for advect velocity,
                                 advect scalars, divergence, apply pressure; 1: one warp per
-                                block through shared tiles of the block and its apron;
-                                16 (advections): as 1 with one interleaved float4 tile per
-                                block (fluidity and the sampled values of a cell together) */
+                                block through shared tiles of the block and its apron      */
   int32_t solve_cache;       /* cells per thread whose stencil the level solve keeps in
                                 shared memory: 0, 3, 4 or 8 (8 KB of shared memory each);
                                 16 + c (c = 0, 2, 3): pipelined staged sweeps, asynchronous
                                 copies into two tile buffers per warp; 32 + c: three;
-                                64 + c (c = 0, 2): two, registers for 5 CTAs per SM;
-                                128 + c (c = 0, 2, 3) / 160 + c (c = 0, 3): two / three
-                                buffers, sweeps ordered by per-block epochs (each block waits
-                                for its same-level face neighbours' previous sweep) instead of
-                                grid barriers                                               */
+                                64 + c (c = 0, 2): two, registers for 5 CTAs per SM      */
   int32_t solve_ctas_per_sm; /* CTAs per SM of the cooperative solve (0 = occupancy limit) */
   int32_t solve_barrier;     /* bit 0: grid barrier between sweeps, 0 flat, 1 two-level;
                                 bit 1: cascade round r solves every member's level
@@ -374,9 +368,6 @@ typedef struct {
   int8_t round_barrier[4];
   float solve_ms;            /* autotune: measured time of the whole cascade (all rounds)  */
   float cells_ms[4];         /* autotune: measured time of each cell stage at its tile     */
-  int32_t adapt_sort;        /* adaptation's radix sorts: 0 = each sort one cooperative launch
-                                (all passes, phases separated by grid barriers), 1 = one launch
-                                per phase and pass (16 per sort); the results are the same   */
 } dcg_tuning;
 
 int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out);

@@ -94,20 +94,10 @@ def test_results_do_not_depend_on_tuning():
     piped_rounds.round_ctas_per_sm[0], piped_rounds.round_cache[0], piped_rounds.round_barrier[0] = -4, 18, 1
     mixed_tiles = tuning(4, 4, 0, 1, 0)
     mixed_tiles.tile[0], mixed_tiles.tile[3] = 1, 1
-    phase_sorts = tuning(4, 4, 0, 1)
-    phase_sorts.adapt_sort = 1  # the adaptation's sorts as one launch per phase
-    # sweeps ordered by block epochs: two and three buffers, cached and global
-    # block descriptions, per-round schedules with sub-SM grids
-    interleaved = tuning(1, 131, 1, 2, 1)
-    interleaved.tile[0], interleaved.tile[1] = 16, 16  # the advections through interleaved float4 tiles
-    epochs_rounds = tuning(1, 131, 1, 2, 1)
-    epochs_rounds.round_ctas_per_sm[0], epochs_rounds.round_cache[0], epochs_rounds.round_barrier[0] = -4, 130, 0
     for t in [tuning(2, 0, 1, 0), tuning(8, 8, 2, 1, 1), tuning(2, 8, 1, 0, 1), tuning(8, 0, 0, 1),
               tuning(4, 3, 0, 0, 1), rounds, staged, mixed_tiles, piped2, piped3, piped_rounds, piped_global2,
               piped_global3, tuning(1, 19, 0, 2, 1), tuning(2, 16, 1, 3, 1), tuning(1, 66, 1, 2, 1),
-              tuning(1, 64, 1, 1, 1), tuning(1, 19, 1, 4, 1), tuning(4, 16, 2, 5, 1), phase_sorts,
-              tuning(1, 131, 0, 2, 1), tuning(2, 128, 1, 1, 1), tuning(1, 163, 1, 4, 1), tuning(4, 160, 2, 0, 0),
-              epochs_rounds, interleaved]:
+              tuning(1, 64, 1, 1, 1), tuning(1, 19, 1, 4, 1), tuning(4, 16, 2, 5, 1)]:
         b = batch_run(params, 5, t)
         for i, p in enumerate(params):
             compare(b[i], ref[i], p, f"tiles {list(t.tile)} cache {t.solve_cache} member {i}")
@@ -125,8 +115,8 @@ def test_autotune_resets_and_keeps_results():
     params = small_batch(4, 17)
     b = Batch(params)
     t = b.autotune(spinup_steps=3, reps=2)
-    assert all(x in (1, 2, 4, 8, 16) for x in t["tile"])
-    assert t["solve_cache"] in (0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66, 128, 130, 131, 160, 163) and 0 <= t["solve_barrier"] <= 7
+    assert all(x in (1, 2, 4, 8) for x in t["tile"])
+    assert t["solve_cache"] in (0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66) and 0 <= t["solve_barrier"] <= 7
     assert t["solve_ms"] > 0
     fresh = Batch(params)
     for i, p in enumerate(params):
