@@ -20,13 +20,16 @@ Workloads (--workload):
   large — the 512^3 4-level fire plume with a 100 GB block budget: FP16
     storage, FP32, and the uniform grid at the largest cube that fits 100 GB
     (no CPU baseline or end-to-end leg at this size).
+  precision — not a timing: the cloud scene over 200 steps in FP32, FP16 and
+    BF16 scalar storage, per-field relative L2 error against the FP64 oracle
+    every 50 steps.
 
 Synthetic inputs throughout (seeded sources, terrain, noise, emission maps);
 scenes are spun up untimed before warm-up so the refined topology has
 developed.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                       [--workload batch|cloud]
+                       [--workload batch|cloud|large|precision]
 Under torchrun with N > 1 every rank runs an independent replica of the
 workload (no data exchange); value sums the ranks' cell-steps over the
 slowest rank's time.
@@ -628,6 +631,71 @@ def run_large(args, ctx):
     return line
 
 
+# ------------------------------------------------------------------ precision
+PRECISION_STEPS = 200
+PRECISION_EVERY = 50
+
+
+def run_precision(args, ctx):
+    """Per-field error of each storage precision against the FP64 oracle on
+    the 3-level cloud scene at effective 256^3 with a 40000-block budget over
+    200 steps: FP32, FP16 scalar storage and BF16 scalar storage, each driving
+    its own FP64 oracle with the GPU's adaptation decisions (so both sides
+    share one topology); relative L2 over the allocated cells every 50 steps.
+    Not a timing: the line's value is the final FP16 density error."""
+    from dcgrid_gb300 import Simulation, capi, scenes
+    from oracle import pyoracle
+    import numpy as np
+    pyoracle.set_threads(os.cpu_count() or 1)
+    em = scenes.emission_field(EM_N, 1)
+    fields = ["density", "temperature", "vapor", "vel_x", "vel_y", "vel_z", "pressure"]
+    out = {}
+    t0 = time.perf_counter()
+    for name, prec in [("fp32", capi.PRECISION_FP32), ("fp16", capi.PRECISION_MIXED_FP16),
+                       ("bf16", capi.PRECISION_MIXED)]:
+        p = scenes.cloud256(precision=prec)
+        g = Simulation(p)
+        g.set_stream(ctx.stream.cuda_stream)
+        q = capi.params_from_dict(capi.params_to_dict(p))
+        q.precision = capi.PRECISION_FP32
+        o = pyoracle.OracleSim(q, precision="double")
+        for s in (g, o):
+            s.set_emission(em)
+            s.add_velocity_noise(0, 0.01)
+        rows = []
+        for step in range(1, PRECISION_STEPS + 1):
+            g.advect_velocity()
+            o.advect_velocity()
+            g.adapt()
+            mv, rf = g.get_last_adapt()
+            o.adapt_replay(mv, rf)
+            g.project()
+            o.project()
+            g.advect_scalars()
+            o.advect_scalars()
+            if step % PRECISION_EVERY == 0:
+                g.sync()
+                alloc = np.repeat(o.get_topology()["pos"][:, 3] >= 0, 64)
+                row = {"step": step, "active_cells": int(g.stats().active_cells)}
+                for f in fields:
+                    a = g.get_field(f)[alloc].astype(np.float64)
+                    b = o.get_field(f)[alloc]
+                    row[f] = float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+                rows.append(row)
+        g.close()
+        out[name] = rows
+    final = out["fp16"][-1]["density"]
+    return {"metric": "relative L2 density error vs FP64 oracle (FP16 storage)", "value": final,
+            "unit": "relative L2", "n_gpus": ctx.world, "steps": PRECISION_STEPS, "warmup": 0,
+            "higher_is_better": False, "dtype": "fp16/bf16 storage, fp32 compute; fp32",
+            "data": "synthetic (seeded terrain, source bubble, emission map, velocity noise)",
+            "config": {"workload": "adaptive cloud scene, effective 256^3, 3 levels, 40000 block budget, "
+                                   f"{ITERS} Jacobi sweeps/level, {PRECISION_STEPS} steps",
+                       "oracle": "FP64, the GPU's adaptation decisions replayed",
+                       "cells": "allocated cells of all levels"},
+            "errors": out, "wall_s": time.perf_counter() - t0}
+
+
 # ------------------------------------------------------------------ reference arm
 def run_reference(args):
     """--impl reference: the reference's arithmetic on the host cores. The
@@ -687,7 +755,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "cloud", "large"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "cloud", "large", "precision"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and FP64 error legs")
     ap.add_argument("--no-ref-gpu", action="store_true", help="skip the reference-kernel GPU comparator")
     ap.add_argument("--profile", action="store_true",
@@ -698,7 +766,8 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     ctx = Ctx()
-    line = {"batch": run_batch, "cloud": run_cloud, "large": run_large}[args.workload](args, ctx)
+    line = {"batch": run_batch, "cloud": run_cloud, "large": run_large,
+            "precision": run_precision}[args.workload](args, ctx)
     if ctx.rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
