@@ -22,7 +22,7 @@ Workloads (--workload):
     (no CPU baseline or end-to-end leg at this size).
   precision — not a timing: the cloud scene over 200 steps in FP32, FP16 and
     BF16 scalar storage, per-field relative L2 error against the FP64 oracle
-    every 50 steps.
+    from 10 to 200 steps.
 
 Synthetic inputs throughout (seeded sources, terrain, noise, emission maps);
 scenes are spun up untimed before warm-up so the refined topology has
@@ -633,7 +633,7 @@ def run_large(args, ctx):
 
 # ------------------------------------------------------------------ precision
 PRECISION_STEPS = 200
-PRECISION_EVERY = 50
+PRECISION_AT = (10, 20, 30, 40, 50, 100, 150, 200)
 
 
 def run_precision(args, ctx):
@@ -641,7 +641,8 @@ def run_precision(args, ctx):
     the 3-level cloud scene at effective 256^3 with a 40000-block budget over
     200 steps: FP32, FP16 scalar storage and BF16 scalar storage, each driving
     its own FP64 oracle with the GPU's adaptation decisions (so both sides
-    share one topology); relative L2 over the allocated cells every 50 steps.
+    share one topology); relative L2 over the allocated cells after 10, 20, 30,
+    40, 50, 100, 150 and 200 steps.
     Not a timing: the line's value is the final FP16 density error."""
     from dcgrid_gb300 import Simulation, capi, scenes
     from oracle import pyoracle
@@ -673,7 +674,7 @@ def run_precision(args, ctx):
             o.project()
             g.advect_scalars()
             o.advect_scalars()
-            if step % PRECISION_EVERY == 0:
+            if step in PRECISION_AT:
                 g.sync()
                 alloc = np.repeat(o.get_topology()["pos"][:, 3] >= 0, 64)
                 row = {"step": step, "active_cells": int(g.stats().active_cells)}

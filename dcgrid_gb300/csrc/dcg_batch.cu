@@ -123,10 +123,10 @@ struct dcg_batch {
       CellBatch P{};
       P.n = std::min(BMAX, n() - g * BMAX);
       for (int i = 0; i < P.n; i++) P.d[i] = m[g * BMAX + i]->D;
-      launch_cells_batch(stage, P, tune.tile[stage], stream, tune.persistent != 0);
+      launch_cells_batch(stage, P, stage == 5 ? 1 : tune.tile[stage], stream, tune.persistent != 0);
     }
   }
-  // field: 0 velocity, 1 scalars, 2 divergence
+  // field: 0 velocity, 1 scalars, 2 divergence, 3 velocity and scalars
   void restrict_fields(int field) {
     int maxl = 0;
     for (dcg_sim *s : m) maxl = std::max(maxl, s->D.g.levels);
@@ -139,16 +139,19 @@ struct dcg_batch {
           const dcg_sim *s = m[g * BMAX + i];
           P.d[i] = s->D;
           FieldList &fl = P.fl[i];
-          if (field == 0) {
+          if (field == 0 || field == 3) {
             fl.n = 3;
             for (int d = 0; d < 3; d++) fl.f[d] = s->D.v[d];
-          } else if (field == 1) {
-            fl.n = s->P.n_scalars;
-            for (int k = 0; k < fl.n; k++) {
-              fl.f[k] = s->D.g.mixed ? static_cast<void *>(s->D.qh[k]) : static_cast<void *>(s->D.q[k]);
-              fl.mode[k] = s->D.g.mixed;
+          }
+          if (field == 1 || field == 3) {
+            const int o = fl.n;
+            fl.n += s->P.n_scalars;
+            for (int k = 0; k < s->P.n_scalars; k++) {
+              fl.f[o + k] = s->D.g.mixed ? static_cast<void *>(s->D.qh[k]) : static_cast<void *>(s->D.q[k]);
+              fl.mode[o + k] = s->D.g.mixed;
             }
-          } else {
+          }
+          if (field == 2) {
             fl.n = 1;
             fl.f[0] = s->D.div;
           }
@@ -296,6 +299,22 @@ struct dcg_batch {
     }
   }
   // Simulation::updateSimulation (simulation.cpp:104-112) for every member
+  // the pressure application and the scalar advection run as one staged pass
+  // when both stages are tuned to their staged forms
+  bool fused() const { return tune.tile[1] == 1 && tune.tile[3] == 1; }
+  void apply_advect() {
+    if (fused()) {
+      cells(5);  // apply pressure + advect scalars (+ sources, emission)
+      flip_q();
+      restrict_fields(3);
+    } else {
+      cells(3);  // apply pressure
+      restrict_fields(0);
+      cells(1);  // advect scalars (+ sources, emission)
+      flip_q();
+      restrict_fields(1);
+    }
+  }
   void step_once() {
     cells(0);  // advect velocity (+ buoyancy)
     flip_v();
@@ -305,15 +324,12 @@ struct dcg_batch {
     restrict_fields(2);
     solve_tuned();
     if (dpass > 0) defect_correct();
-    cells(3);  // apply pressure
-    restrict_fields(0);
-    cells(1);  // advect scalars (+ sources, emission)
-    flip_q();
-    restrict_fields(1);
+    apply_advect();
   }
 
   // One step as step_once() without the graph, with CUDA events between the
-  // stages: ms[0] velocity advection (+ its restriction), [1] adaptation,
+  // stages and the pressure application and scalar advection as separate
+  // passes: ms[0] velocity advection (+ its restriction), [1] adaptation,
   // [2] divergence (+ restriction), [3] pressure cascade (+ defect
   // correction), [4] pressure application (+ restriction), [5] scalar
   // advection (+ restriction), [6] the whole step.

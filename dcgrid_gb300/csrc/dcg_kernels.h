@@ -60,7 +60,8 @@ void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int gr
 // through the constant cache); BMAX members fit the 32 KB parameter space.
 constexpr int BMAX = 16;
 // cell stages: 0 advect velocity, 1 advect scalars, 2 divergence, 3 apply
-// pressure, 4 statistics (into each member's red; zero it first)
+// pressure, 4 statistics (into each member's red; zero it first), 5 apply
+// pressure and advect scalars in one staged pass (the results of 3 then 1)
 struct CellBatch {
   int n, pad;
   long long end[BMAX];  // cumulative CTA count of members 0..s

@@ -420,7 +420,9 @@ struct dcg_sim {
     restrict_v();
   }
   void a_adapt() { launch_adapt(D, S, keys, vals, keys2, vals2, sms, stream); }
-  void a_project(bool local) {
+  // apply = false leaves out the pressure application (and its restriction):
+  // the step then runs it fused with the scalar advection (a_apply_advect)
+  void a_project(bool local, bool apply = true) {
     cells(2, 1);
     restrict_div();
     const int top = D.g.levels - 1;
@@ -456,6 +458,7 @@ struct dcg_sim {
         }
       }
     }
+    if (!apply) return;
     cells(3, 1);
     restrict_v();
   }
@@ -527,6 +530,22 @@ struct dcg_sim {
     qpar ^= 1;
     bind_parity();
     restrict_q();
+  }
+  // pressure application and scalar advection in one staged pass (cell
+  // stage 5), then the restriction of velocity and scalars in one pass: the
+  // results of cells(3) + restrict_v() + a_advect_scalars()
+  void a_apply_advect() {
+    cells(5, 1);
+    qpar ^= 1;
+    bind_parity();
+    FieldList fl{};
+    fl.n = 3 + P.n_scalars;
+    for (int d = 0; d < 3; d++) fl.f[d] = D.v[d];
+    for (int k = 0; k < P.n_scalars; k++) {
+      fl.f[3 + k] = D.g.mixed ? static_cast<void *>(D.qh[k]) : static_cast<void *>(D.q[k]);
+      fl.mode[3 + k] = D.g.mixed;
+    }
+    launch_restrict(D, fl, stream);
   }
 
   // ---------------------------------------------------------------- uniform
@@ -635,8 +654,13 @@ struct dcg_sim {
   void step_once() {
     stage_advect_velocity();
     stage_adapt();
-    stage_project(false);
-    stage_advect_scalars();
+    if (mode == DCG_MODE_ADAPTIVE) {
+      a_project(false, false);
+      a_apply_advect();
+    } else {
+      stage_project(false);
+      stage_advect_scalars();
+    }
   }
 
   int step(int n) {

@@ -507,9 +507,24 @@ __device__ __forceinline__ void defect_residual_cell(const Dev &D, long long b, 
     r2 += __shfl_xor_sync(0xffffffffu, r2, o);
     b2 += __shfl_xor_sync(0xffffffffu, b2, o);
   }
-  if ((threadIdx.x & 31) == 0 && (r2 != 0.0 || b2 != 0.0)) {
-    atomicAdd(norms, r2);
-    atomicAdd(norms + 1, b2);
+  // the CTA's eight warp sums are added in shared memory: one atomic per CTA
+  // and quantity (atomics on the two norm words from every warp serialise)
+  __shared__ double s_norm[2][8];
+  if ((threadIdx.x & 31) == 0) {
+    s_norm[0][threadIdx.x >> 5] = r2;
+    s_norm[1][threadIdx.x >> 5] = b2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, c = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+      a += s_norm[0][i];
+      c += s_norm[1][i];
+    }
+    if (a != 0.0 || c != 0.0) {
+      atomicAdd(norms, a);
+      atomicAdd(norms + 1, c);
+    }
   }
 }
 __global__ void __launch_bounds__(256) k_defect_residual(Dev D, double *norms) {
@@ -1244,20 +1259,35 @@ __global__ void __launch_bounds__(256) k_cells_staged(const __grid_constant__ Ce
   uint32_t hpk[3], hax[3];
   halo_slots<SX, SY>(lane, oA, hpk, hax);
   const unsigned full = 0xffffffffu;
-  int seg = 0;
-  for (long long t = (long long)blockIdx.x * W + w; t < total; t += (long long)gridDim.x * W) {
-    while (t >= s_end[seg]) seg++;  // t grows: the segment only moves forward
+  // the warp's next block (segment, index, position, face entries, subblock
+  // child) is fetched while the current one is computed, so a block waits
+  // on one round of loads (its values and face halo) instead of two
+  const long long stride = (long long)gridDim.x * W;
+  const int fdir = lane == 0 ? 4 : lane == 1 ? 22 : lane == 2 ? 10 : lane == 3 ? 16 : lane == 4 ? 12 : 14;
+  int segn = 0;
+  uint32_t bn = 0, en = OUT, chn = NONE;
+  int4 bpn = make_int4(0, 0, 0, -1);
+  auto fetch = [&](long long tt) {
+    while (tt >= s_end[segn]) segn++;  // tt grows: the segment only moves forward
+    const Dev &Dn = P.d[segn / MAXL];
+    bn = (uint32_t)(Dn.g.off[segn % MAXL] + (tt - (segn ? s_end[segn - 1] : 0)));
+    bpn = Dn.pos[bn];
+    en = lane < 6 ? Dn.nbr[27u * bn + fdir] : OUT;
+    chn = Dn.child[8u * bn + (lane >> 2)];
+  };
+  long long t = (long long)blockIdx.x * W + w;
+  if (t < total) fetch(t);
+  for (; t < total; t += stride) {
+    const int seg = segn;
+    const uint32_t b = bn, e = en;
+    const int4 bp = bpn;
+    const bool leaf = chn == NONE;
+    if (t + stride < total) fetch(t + stride);
     const Dev &D = P.d[seg / MAXL];
-    const int l = seg % MAXL;
-    const uint32_t b = (uint32_t)(D.g.off[l] + (t - (seg ? s_end[seg - 1] : 0)));
-    const int4 bp = D.pos[b];
     const size_t own = (size_t)b * BV;
-    uint32_t e = OUT;
-    if (lane < 6) e = D.nbr[27u * b + (lane == 0 ? 4 : lane == 1 ? 22 : lane == 2 ? 10 : lane == 3 ? 16 : lane == 4 ? 12 : 14)];
     size_t hc[3];
 #pragma unroll
     for (int q = 0; q < 3; q++) hc[q] = halo_cell(D, b, bp, __shfl_sync(full, e, (int)(hax[q] >> 12)), hpk[q], hax[q]);
-    const bool leaf = D.child[8u * b + (lane >> 2)] == NONE;
     const int scale = 1 << bp.w;
     const float alpha = 0.5f * D.ph.rdx / (float)scale;
     float *T0 = s_tile[w][0], *T1 = s_tile[w][NT > 1 ? 1 : 0];
@@ -1475,10 +1505,17 @@ template <int MODE, int NQ> __device__ __noinline__ void advect_scalars_cell_ool
 // storage format MODE and NQ scalars (other members have no blocks here).
 // Four blocks per CTA pass, 64 threads (two warps) per block, one cell per
 // thread; the two warps of a block share its tiles through a named barrier.
-template <int STAGE, int MODE, int NQ>
+// APPLY (STAGE 1 only): the pressure application of the same step first, in
+// the same pass: the block's pressure and its face halo go into one more
+// tile, each leaf cell computes apply_pressure_cell's velocity from the
+// pressure and fluidity tiles, stores it and back-traces with it. The scalar
+// advection reads no velocity but its own cell's, so the fused pass gives
+// the results of the two stages run one after the other.
+template <int STAGE, int MODE, int NQ, bool APPLY = false>
 __global__ void __launch_bounds__(256, DCG_ADV_MINB) k_advect_staged(const __grid_constant__ CellBatch P) {
   constexpr int NBK = 4, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 8;
-  constexpr int NF = STAGE == 0 ? 4 : 1 + NQ;  // tile 0: fluidity
+  constexpr int QT = APPLY ? 2 : 1;                  // first scalar tile (tile 1: pressure with APPLY)
+  constexpr int NF = STAGE == 0 ? 4 : QT + NQ;  // tile 0: fluidity
   __shared__ long long s_end[BMAX * MAXL];
   __shared__ __align__(16) float s_tile[NBK][NF][TILE];
   __shared__ uint32_t s_slot[2][3][64];  // apron slots a = c + 64 r of thread c (pk ~0u: none)
@@ -1545,8 +1582,9 @@ __global__ void __launch_bounds__(256, DCG_ADV_MINB) k_advect_staged(const __gri
         if (D.g.nq > 1) qb = q_ld(D, 1, cell);
       }
     } else {
+      if constexpr (APPLY) s_tile[k][1][oC] = D.p[cell];
 #pragma unroll
-      for (int kq = 0; kq < NQ; kq++) s_tile[k][1 + kq][oC] = q_ldm<MODE>(D, kq, cell);
+      for (int kq = 0; kq < NQ; kq++) s_tile[k][QT + kq][oC] = q_ldm<MODE>(D, kq, cell);
     }
 #pragma unroll
     for (int r = 0; r < 3; r++) {
@@ -1561,22 +1599,40 @@ __global__ void __launch_bounds__(256, DCG_ADV_MINB) k_advect_staged(const __gri
           s_tile[k][2][at] = D.v[1][ac];
           s_tile[k][3][at] = D.v[2][ac];
         } else {
+          if constexpr (APPLY) {  // pressure on the six faces only
+            const uint32_t d = (ga >> 12) & 31u;
+            if (d == 4u || d == 22u || d == 10u || d == 16u || d == 12u || d == 14u) s_tile[k][1][at] = D.p[ac];
+          }
 #pragma unroll
-          for (int kq = 0; kq < NQ; kq++) s_tile[k][1 + kq][at] = q_ldm<MODE>(D, kq, ac);
+          for (int kq = 0; kq < NQ; kq++) s_tile[k][QT + kq][at] = q_ldm<MODE>(D, kq, ac);
         }
       }
     }
     pair_sync();
     const bool leaf = __shfl_sync(full, ch, c >> 3) == NONE;
+    float va2 = va, vb2 = vb, vc2 = vc;  // the velocity the cell back-traces with
+    if constexpr (STAGE == 1 && APPLY) {
+      if (leaf) {  // apply_pressure_cell's arithmetic, neighbours from the tiles
+        const float *Pt = s_tile[k][1];
+        const float alpha = 0.5f * D.ph.rdx / (float)(1 << bp.w);
+        const float pc = Pt[oC];
+        va2 = va - alpha * (Wt[oC + SX] * (Pt[oC + SX] - pc) + Wt[oC - SX] * (pc - Pt[oC - SX]));
+        vb2 = vb - alpha * (Wt[oC + SY] * (Pt[oC + SY] - pc) + Wt[oC - SY] * (pc - Pt[oC - SY]));
+        vc2 = vc - alpha * (Wt[oC + 1] * (Pt[oC + 1] - pc) + Wt[oC - 1] * (pc - Pt[oC - 1]));
+        D.v[0][cell] = va2;
+        D.v[1][cell] = vb2;
+        D.v[2][cell] = vc2;
+      }
+    }
     float px = 0.f, py = 0.f, pz = 0.f;
     bool fast = false;
     int sub = 0;
     if (leaf) {
       const float scale = (float)(1 << bp.w);
       const float alpha = D.ph.dt * D.ph.rdx;
-      px = ((float)(bp.x + lx) + 0.5f) * scale - va * alpha;
-      py = ((float)(bp.y + ly) + 0.5f) * scale - vb * alpha;
-      pz = ((float)(bp.z + lz) + 0.5f) * scale - vc * alpha;
+      px = ((float)(bp.x + lx) + 0.5f) * scale - va2 * alpha;
+      py = ((float)(bp.y + ly) + 0.5f) * scale - vb2 * alpha;
+      pz = ((float)(bp.z + lz) + 0.5f) * scale - vc2 * alpha;
       fast = sample_in_own(D, bp, px, py, pz, sub);
     }
     // the sample's subblock must have no child (else sample_at descends)
@@ -1635,7 +1691,7 @@ __global__ void __launch_bounds__(256, DCG_ADV_MINB) k_advect_staged(const __gri
               const int mode = inside ? 0 : q_bc_mode(D.g, D.ph, x, y, z, s.scale);
 #pragma unroll
               for (int kq = 0; kq < NQ; kq++) {
-                const float qc = mode == 0 ? s_tile[k][1 + kq][s.base + tile_delta<SX, SY>(kk)]
+                const float qc = mode == 0 ? s_tile[k][QT + kq][s.base + tile_delta<SX, SY>(kk)]
                                            : (mode == 1 && kq == 0 ? D.ph.d_emit : 0.f);
                 o[kq] = (kk == 0) ? qc * s.wt[0] : o[kq] + qc * s.wt[kk];
               }
@@ -1656,30 +1712,32 @@ __global__ void __launch_bounds__(256, DCG_ADV_MINB) k_advect_staged(const __gri
     pair_sync();  // the tiles are refilled for the next block
   }
 }
-template <int STAGE, int MODE, int NQ> static unsigned advect_grid() {
+template <int STAGE, int MODE, int NQ, bool APPLY = false> static unsigned advect_grid() {
   static unsigned g = 0;
   if (!g) {
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_advect_staged<STAGE, MODE, NQ>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_advect_staged<STAGE, MODE, NQ, APPLY>, 256, 0);
     g = (unsigned)(sms * (occ > 0 ? occ : 1));
   }
   return g;
 }
-static void launch_advect_staged(int stage, const CellBatch &P, cudaStream_t st) {
-  if (stage == 0) {
-    k_advect_staged<0, 0, 1><<<advect_grid<0, 0, 1>(), 256, 0, st>>>(P);
-    return;
-  }
+// the scalar advection, one launch per storage format and scalar count present
+template <bool APPLY> static void launch_advect_scalars_staged(const CellBatch &P, cudaStream_t st) {
   bool has[3][2] = {};
   for (int i = 0; i < P.n; i++) has[P.d[i].g.mixed][P.d[i].g.nq == 3 ? 1 : 0] = true;
-  if (has[0][0]) k_advect_staged<1, 0, 1><<<advect_grid<1, 0, 1>(), 256, 0, st>>>(P);
-  if (has[0][1]) k_advect_staged<1, 0, 3><<<advect_grid<1, 0, 3>(), 256, 0, st>>>(P);
-  if (has[1][0]) k_advect_staged<1, 1, 1><<<advect_grid<1, 1, 1>(), 256, 0, st>>>(P);
-  if (has[1][1]) k_advect_staged<1, 1, 3><<<advect_grid<1, 1, 3>(), 256, 0, st>>>(P);
-  if (has[2][0]) k_advect_staged<1, 2, 1><<<advect_grid<1, 2, 1>(), 256, 0, st>>>(P);
-  if (has[2][1]) k_advect_staged<1, 2, 3><<<advect_grid<1, 2, 3>(), 256, 0, st>>>(P);
+  if (has[0][0]) k_advect_staged<1, 0, 1, APPLY><<<advect_grid<1, 0, 1, APPLY>(), 256, 0, st>>>(P);
+  if (has[0][1]) k_advect_staged<1, 0, 3, APPLY><<<advect_grid<1, 0, 3, APPLY>(), 256, 0, st>>>(P);
+  if (has[1][0]) k_advect_staged<1, 1, 1, APPLY><<<advect_grid<1, 1, 1, APPLY>(), 256, 0, st>>>(P);
+  if (has[1][1]) k_advect_staged<1, 1, 3, APPLY><<<advect_grid<1, 1, 3, APPLY>(), 256, 0, st>>>(P);
+  if (has[2][0]) k_advect_staged<1, 2, 1, APPLY><<<advect_grid<1, 2, 1, APPLY>(), 256, 0, st>>>(P);
+  if (has[2][1]) k_advect_staged<1, 2, 3, APPLY><<<advect_grid<1, 2, 3, APPLY>(), 256, 0, st>>>(P);
+}
+static void launch_advect_staged(int stage, const CellBatch &P, cudaStream_t st) {
+  if (stage == 0) k_advect_staged<0, 0, 1><<<advect_grid<0, 0, 1>(), 256, 0, st>>>(P);
+  else if (stage == 5) launch_advect_scalars_staged<true>(P, st);
+  else launch_advect_scalars_staged<false>(P, st);
 }
 
 static unsigned staged_grid(int stage) {
@@ -1765,8 +1823,8 @@ static void cells_batch_tb(int stage, const CellBatch &P, unsigned grid, cudaStr
   }
 }
 void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st, bool persistent) {
-  if (tile == 1) {  // staged, one warp per block
-    if (stage < 2) launch_advect_staged(stage, P, st);
+  if (tile == 1 || stage == 5) {  // staged, one warp per block (5: staged only)
+    if (stage < 2 || stage == 5) launch_advect_staged(stage, P, st);
     else if (stage == 2) k_cells_staged<2><<<staged_grid(2), 256, 0, st>>>(P);
     else if (stage == 3) k_cells_staged<3><<<staged_grid(3), 256, 0, st>>>(P);
     else k_cells_staged<4><<<staged_grid(4), 256, 0, st>>>(P);

@@ -655,9 +655,7 @@ void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *
 // the products w*v0, w*v1, w*v2 and the density of the block and its face
 // halo go through shared tiles, then each lane computes field_cell_score's
 // arithmetic for its two cells from the tiles and the four lanes of a
-// subblock reduce the maximum. Blocks of every level's budget range are
-// visited (unallocated ones get the blocked score). Results equal
-// scores_fields_body.
+// subblock reduce the maximum.
 __device__ __forceinline__ float2 q_ld2(const Dev &D, size_t own, int lane) {
   if (D.g.mixed) {
     const uint32_t u = reinterpret_cast<const uint32_t *>(D.qh[0] + own)[lane];
@@ -688,30 +686,54 @@ struct ScoreBatchP {
   long long end[BMAX];  // cumulative block counts (0 for members without the field criterion)
   Dev d[BMAX];
 };
+// The warps walk the allocated blocks only (each level's allocated blocks are
+// the prefix [off, off + load) of its budget range), segment by segment
+// (member, level) as k_cells_staged does; a level that level_blocked refuses
+// gets the blocked score without loading anything, and the unallocated tails
+// of the budget ranges (and the blocks past them) get it from coalesced
+// stores after the walk. Results equal scores_fields_body.
 __global__ void __launch_bounds__(256) k_scores_staged(const __grid_constant__ ScoreBatchP P) {
   constexpr int W = 8, SX = DCG_TILE_SX, SY = DCG_TILE_SY, TILE = 5 * SX + 5 * SY + 8;
   __shared__ __align__(16) float s_tile[W][4][TILE];
-  if (blockIdx.x == 0 && threadIdx.x < P.n) {
-    const long long cnt = P.end[threadIdx.x] - (threadIdx.x ? P.end[threadIdx.x - 1] : 0);
-    if (cnt > 0) P.d[threadIdx.x].ss[8 * P.d[threadIdx.x].g.B] = 0.f;
+  __shared__ long long s_end[BMAX * MAXL], s_tail[BMAX * MAXL];
+  __shared__ uint8_t s_blk[BMAX * MAXL];
+  const int nseg = P.n * MAXL;
+  for (int i = threadIdx.x; i < nseg; i += blockDim.x) {
+    const int mi = i / MAXL, l = i % MAXL;
+    const Dev &D = P.d[mi];
+    const bool has = l < D.g.levels && P.end[mi] - (mi ? P.end[mi - 1] : 0) > 0;
+    const long long ld = has ? __ldcg(D.load + l) : 0;
+    s_end[i] = ld;
+    // the last level's tail also covers the blocks past every budget range
+    const long long past = l == D.g.levels - 1 ? D.g.B - (D.g.off[l] + D.g.budget[l]) : 0;
+    s_tail[i] = has ? D.g.budget[l] - ld + past : 0;
+    s_blk[i] = (uint8_t)(has && level_blocked(D, l));
+    if (blockIdx.x == 0 && l == 0 && has) D.ss[8 * D.g.B] = 0.f;
   }
-  const long long total = P.end[P.n - 1];
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int i = 1; i < nseg; i++) {
+      s_end[i] += s_end[i - 1];
+      s_tail[i] += s_tail[i - 1];
+    }
+  __syncthreads();
+  const long long total = s_end[nseg - 1];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int oA;
   uint32_t hpk[3], hax[3];
   halo_slots<SX, SY>(lane, oA, hpk, hax);
   const unsigned full = 0xffffffffu;
-  int m = 0;
+  int seg = 0;
   for (long long t = (long long)blockIdx.x * W + w; t < total; t += (long long)gridDim.x * W) {
-    while (t >= P.end[m]) m++;
-    const Dev &D = P.d[m];
-    const uint32_t b = (uint32_t)(t - (m ? P.end[m - 1] : 0));
-    const int4 bp = D.pos[b];
+    while (t >= s_end[seg]) seg++;
+    const Dev &D = P.d[seg / MAXL];
+    const uint32_t b = (uint32_t)(D.g.off[seg % MAXL] + (t - (seg ? s_end[seg - 1] : 0)));
     const uint32_t sb = 8u * b + (uint32_t)(lane >> 2);
-    if (bp.w < 0 || level_blocked(D, bp.w)) {  // warp-uniform
+    if (s_blk[seg]) {  // warp-uniform
       if ((lane & 3) == 0) D.ss[sb] = -FLT_MAX;
       continue;
     }
+    const int4 bp = D.pos[b];
     const bool blocked = D.child[sb] != NONE;
     const size_t own = (size_t)b * BV;
     uint32_t e = OUT;
@@ -762,6 +784,18 @@ __global__ void __launch_bounds__(256) k_scores_staged(const __grid_constant__ S
     mm = fmaxf(mm, __shfl_xor_sync(full, mm, 1));
     mm = fmaxf(mm, __shfl_xor_sync(full, mm, 2));
     if ((lane & 3) == 0) D.ss[sb] = blocked ? -FLT_MAX : mm;
+  }
+  // the unallocated tails: 8 subblock scores per block, float4 stores
+  const long long ttot = s_tail[nseg - 1];
+  seg = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < 2 * ttot;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long tb = i >> 1;  // tail block
+    while (tb >= s_tail[seg]) seg++;
+    const Dev &D = P.d[seg / MAXL];
+    const int l = seg % MAXL;
+    const long long b = D.g.off[l] + (s_end[seg] - (seg ? s_end[seg - 1] : 0)) + (tb - (seg ? s_tail[seg - 1] : 0));
+    reinterpret_cast<float4 *>(D.ss + 8 * b)[i & 1] = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX);
   }
 }
 static unsigned scores_staged_grid() {
