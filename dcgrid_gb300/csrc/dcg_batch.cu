@@ -188,7 +188,8 @@ struct dcg_batch {
         CellBatch P{};
         P.n = std::min(BMAX, n() - g * BMAX);
         for (int i = 0; i < P.n; i++) P.d[i] = m[g * BMAX + i]->D;
-        launch_defect_batch(0, P, k, stream);
+        P.arg = k;
+        launch_cells_batch(6, P, 1, stream);  // FP64 residual of pass k
       }
       if (k == dpass) break;
       cudaMemsetAsync(e_arena, 0, (size_t)arena_cells * sizeof(float), stream);
@@ -199,7 +200,7 @@ struct dcg_batch {
         CellBatch P{};
         P.n = std::min(BMAX, n() - g * BMAX);
         for (int i = 0; i < P.n; i++) P.d[i] = m[g * BMAX + i]->D;
-        launch_defect_batch(1, P, k, stream);
+        launch_add_correction_batch(P, stream);
       }
     }
   }

@@ -93,6 +93,7 @@ struct Dev {
   float *w, *p, *pt, *div;
   float *ss, *bs;          // subblock / block scores (8B+1, B)
   uint32_t *moves;         // (block, dest) pairs
+  int4 *mold;              // position of each moved block before its move
   uint32_t *refines;       // (subblock, new block) pairs
   uint32_t *touched;       // moved + new blocks
   long long *ctr;          // C_COUNT counters

@@ -49,7 +49,6 @@ void launch_jacobi(const Dev &D, int level, const float *src, float *dst, cudaSt
 void launch_prolongate(const Dev &D, int level, cudaStream_t st);
 void launch_apply_pressure(const Dev &D, cudaStream_t st);
 // defect correction: FP64 residual into D.rr (+ norms), p += e
-void launch_defect_residual(const Dev &D, double *norms, cudaStream_t st);
 void launch_add_correction(const Dev &D, cudaStream_t st);
 // cooperative persistent solve of one level (prolongation + sweeps)
 int level_solve_grid(int sms);
@@ -61,9 +60,10 @@ void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int gr
 constexpr int BMAX = 16;
 // cell stages: 0 advect velocity, 1 advect scalars, 2 divergence, 3 apply
 // pressure, 4 statistics (into each member's red; zero it first), 5 apply
-// pressure and advect scalars in one staged pass (the results of 3 then 1)
+// pressure and advect scalars in one staged pass (the results of 3 then 1),
+// 6 the FP64 defect residual of correction pass `arg` (staged only)
 struct CellBatch {
-  int n, pad;
+  int n, arg;
   long long end[BMAX];  // cumulative CTA count of members 0..s
   Dev d[BMAX];
 };
@@ -98,8 +98,8 @@ struct StatRecord {
 };
 void launch_stats_zero(const CellBatch &P, cudaStream_t st);
 void launch_stats_gather(const CellBatch &P, StatRecord *dst, cudaStream_t st);
-// batched defect correction: op 0 = FP64 residual of pass `pass`, op 1 = p += e
-void launch_defect_batch(int op, CellBatch &P, int pass, cudaStream_t st);
+// batched defect correction's update p += e (its residual is cell stage 6)
+void launch_add_correction_batch(CellBatch &P, cudaStream_t st);
 // CTAs of the batched solve for a variant (cache depth 0, 3, 4, 8; 16, 18, 19: pipelined
 // staged sweeps with two tile buffers and cache depth 0, 2, 3; 32, 34, 35: three buffers;
 // 64, 66: two buffers, registers for 5 CTAs per SM)

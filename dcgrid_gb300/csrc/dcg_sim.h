@@ -284,6 +284,7 @@ struct dcg_sim {
     if ((rc = alloc(&D.ss, 8 * B + 1))) return rc;
     if ((rc = alloc(&D.bs, B))) return rc;
     if ((rc = alloc(&D.moves, 2 * 2 * B))) return rc;
+    if ((rc = alloc(&D.mold, 2 * B))) return rc;
     if ((rc = alloc(&D.refines, 2 * 2 * B))) return rc;
     if ((rc = alloc(&D.touched, 2 * B))) return rc;
     if ((rc = alloc(&D.ctr, C_COUNT))) return rc;
@@ -493,7 +494,11 @@ struct dcg_sim {
     const int K = P.defect_passes, top = D.g.levels - 1;
     cudaMemsetAsync(D.dnorm, 0, sizeof(double) * 2 * (K + 1), stream);
     for (int k = 0; k <= K; k++) {
-      launch_defect_residual(D, D.dnorm + 2 * k, stream);
+      CellBatch C{};  // the staged FP64 residual of pass k
+      C.n = 1;
+      C.arg = k;
+      C.d[0] = D;
+      launch_cells_batch(6, C, 1, stream);
       if (k == K) break;
       cudaMemsetAsync(D.e, 0, (size_t)D.g.B * BV * sizeof(float), stream);
       for (int l = top; l >= 0; l--) solve_staged(l, 1, sweeps, D.e, D.et, D.rr);

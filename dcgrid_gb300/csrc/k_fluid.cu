@@ -481,55 +481,8 @@ __device__ __forceinline__ void apply_pressure_cell(const Dev &D, long long b, i
 }
 
 // ---------------------------------------------------------------- defect correction
-// FP64 residual of every allocated cell's Jacobi equation (the fixed point of
-// k_jacobi: sum6 p - 6 p = alpha div, alpha = (2^L dx)^2 in float as there),
-// r = div - (sum6 p - 6 p) / alpha, stored in FP32, with FP64 sums of r^2 and
-// div^2 reduced per warp into norms[0..1].
-__device__ __forceinline__ void defect_residual_cell(const Dev &D, long long b, double *norms) {
-  double r2 = 0.0, b2 = 0.0;
-  if (b < D.g.B) {
-    const int4 bp = D.pos[b];
-    if (bp.w >= 0) {
-      const long long cell = b * BV + (threadIdx.x & 63);
-      const Nb6 n = jacobi_neighbours(D, cell);
-      const int s = 1 << bp.w;
-      const float alpha = (float)(s * s) * D.ph.dx * D.ph.dx;
-      const double lap = (double)D.p[n.i0] + (double)D.p[n.i1] + (double)D.p[n.i2] + (double)D.p[n.i3] +
-                         (double)D.p[n.i4] + (double)D.p[n.i5] - 6.0 * (double)D.p[cell];
-      const double dv = (double)D.div[cell];
-      const double r = dv - lap / (double)alpha;
-      D.rr[cell] = (float)r;
-      r2 = r * r;
-      b2 = dv * dv;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    r2 += __shfl_xor_sync(0xffffffffu, r2, o);
-    b2 += __shfl_xor_sync(0xffffffffu, b2, o);
-  }
-  // the CTA's eight warp sums are added in shared memory: one atomic per CTA
-  // and quantity (atomics on the two norm words from every warp serialise)
-  __shared__ double s_norm[2][8];
-  if ((threadIdx.x & 31) == 0) {
-    s_norm[0][threadIdx.x >> 5] = r2;
-    s_norm[1][threadIdx.x >> 5] = b2;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double a = 0.0, c = 0.0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
-      a += s_norm[0][i];
-      c += s_norm[1][i];
-    }
-    if (a != 0.0 || c != 0.0) {
-      atomicAdd(norms, a);
-      atomicAdd(norms + 1, c);
-    }
-  }
-}
-__global__ void __launch_bounds__(256) k_defect_residual(Dev D, double *norms) {
-  defect_residual_cell(D, (long long)blockIdx.x * 4 + (threadIdx.x >> 6), norms);
-}
+// The FP64 residual of every allocated cell's Jacobi equation is cell stage 6
+// of k_cells_staged.
 // p += e on every allocated cell
 __device__ __forceinline__ void add_correction_cell(const Dev &D, long long b) {
   if (b >= D.g.B || D.pos[b].w < 0) return;
@@ -576,9 +529,6 @@ void launch_jacobi(const Dev &D, int level, const float *src, float *dst, cudaSt
 }
 void launch_prolongate(const Dev &D, int level, cudaStream_t st) {
   k_prolongate<<<cta_blocks(D.g.budget[level]), 256, 0, st>>>(D, level);
-}
-void launch_defect_residual(const Dev &D, double *norms, cudaStream_t st) {
-  k_defect_residual<<<cta_blocks(D.g.B), 256, 0, st>>>(D, norms);
 }
 void launch_add_correction(const Dev &D, cudaStream_t st) { k_add_correction<<<cta_blocks(D.g.B), 256, 0, st>>>(D); }
 void launch_apply_pressure(const Dev &D, cudaStream_t st) {
@@ -674,6 +624,7 @@ __global__ void __launch_bounds__(64 * TB) k_cells_persist(const __grid_constant
     const int n = (int)__reduce_add_sync(0xffffffffu, (unsigned)a_cnt);
     stats_flush(P.d[a_mem], r, m, a_lvl, (double)n);
   };
+
   for (long long t = blockIdx.x; t < total; t += gridDim.x) {
     int lo = 0, hi = nseg - 1;
     while (lo < hi) {
@@ -733,27 +684,19 @@ void launch_stats_gather(const CellBatch &P, StatRecord *dst, cudaStream_t st) {
   k_stats_gather<<<P.n, 128, 0, st>>>(P, dst);
 }
 
-// Defect correction of a batch, one launch over all members (4 blocks per
-// CTA, P.end cumulative): OP 0 the FP64 residual of pass `pass` into each
-// member's rr and dnorm[2 pass], [2 pass + 1]; OP 1 p += e. The cell bodies are
-// the single simulation's.
-template <int OP>
-__global__ void __launch_bounds__(256) k_defect_batch(const __grid_constant__ CellBatch P, int pass) {
+// p += e on every allocated cell of every member of a batch (4 blocks per
+// CTA, P.end cumulative); the cell body is the single simulation's.
+__global__ void __launch_bounds__(256) k_add_correction_batch(const __grid_constant__ CellBatch P) {
   const int s = batch_member(P.end, P.n, blockIdx.x);
-  const Dev &D = P.d[s];
-  const long long b = ((long long)blockIdx.x - (s ? P.end[s - 1] : 0)) * 4 + (threadIdx.x >> 6);
-  if (OP == 0) defect_residual_cell(D, b, D.dnorm + 2 * pass);
-  else add_correction_cell(D, b);
+  add_correction_cell(P.d[s], ((long long)blockIdx.x - (s ? P.end[s - 1] : 0)) * 4 + (threadIdx.x >> 6));
 }
-void launch_defect_batch(int op, CellBatch &P, int pass, cudaStream_t st) {
+void launch_add_correction_batch(CellBatch &P, cudaStream_t st) {
   long long acc = 0;
   for (int m = 0; m < P.n; m++) {
     acc += (P.d[m].g.B + 3) / 4;
     P.end[m] = acc;
   }
-  if (acc == 0) return;
-  if (op == 0) k_defect_batch<0><<<(unsigned)acc, 256, 0, st>>>(P, pass);
-  else k_defect_batch<1><<<(unsigned)acc, 256, 0, st>>>(P, pass);
+  if (acc > 0) k_add_correction_batch<<<(unsigned)acc, 256, 0, st>>>(P);
 }
 
 __global__ void __launch_bounds__(256) k_restrict_batch(const __grid_constant__ RestrictBatch P) {
@@ -1242,6 +1185,18 @@ __global__ void __launch_bounds__(256) k_cells_staged(const __grid_constant__ Ce
     }
     const int n = (int)__reduce_add_sync(0xffffffffu, (unsigned)a_cnt);
     stats_flush(P.d[a_mem], r, m, a_lvl, (double)n);
+  };  // defect residual (STAGE 6): a_res sums r^2, a_mass div^2 of the warp's member
+  auto flush_defect = [&]() {
+    double r = a_res, m = a_mass;
+    for (int o = 16; o > 0; o >>= 1) {
+      r += __shfl_xor_sync(0xffffffffu, r, o);
+      m += __shfl_xor_sync(0xffffffffu, m, o);
+    }
+    if ((threadIdx.x & 31) == 0 && (r != 0.0 || m != 0.0)) {
+      double *nrm = P.d[a_mem].dnorm + 2 * P.arg;
+      atomicAdd(nrm, r);
+      atomicAdd(nrm + 1, m);
+    }
   };
   const int nseg = P.n * MAXL;
   for (int i = threadIdx.x; i < nseg; i += blockDim.x) {
@@ -1291,7 +1246,45 @@ __global__ void __launch_bounds__(256) k_cells_staged(const __grid_constant__ Ce
     const int scale = 1 << bp.w;
     const float alpha = 0.5f * D.ph.rdx / (float)scale;
     float *T0 = s_tile[w][0], *T1 = s_tile[w][NT > 1 ? 1 : 0];
-    if constexpr (STAGE == 4) {
+    if constexpr (STAGE == 6) {
+      // the residual of the Jacobi equation (the fixed point of the sweeps:
+      // sum6 p - 6 p = alpha div, alpha = (2^L dx)^2 in float as there) for
+      // the lane's two cells (every allocated cell): the FP64 sum of the six
+      // neighbours in jacobi_neighbours' order (L, R, D, U, B, F) minus 6 p,
+      // r = div - lap / alpha, stored in FP32; the FP64 sums of r^2 and
+      // div^2 go to the member's norms of correction pass P.arg
+      const float2 p2 = reinterpret_cast<const float2 *>(D.p + own)[lane];
+      float hp[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) hp[q] = D.p[hc[q]];
+      *reinterpret_cast<float2 *>(T0 + oA) = p2;
+#pragma unroll
+      for (int q = 0; q < 3; q++) T0[hpk[q] & 511u] = hp[q];
+      __syncwarp();
+      if (seg / MAXL != a_mem) {  // warp-uniform
+        if (a_mem >= 0) flush_defect();
+        a_mem = seg / MAXL;
+        a_res = a_mass = 0.0;
+      }
+      const float2 dv = reinterpret_cast<const float2 *>(D.div + own)[lane];
+      const float2 L = *reinterpret_cast<const float2 *>(T0 + oA - SX);
+      const float2 R = *reinterpret_cast<const float2 *>(T0 + oA + SX);
+      const float2 Dn = *reinterpret_cast<const float2 *>(T0 + oA - SY);
+      const float2 U = *reinterpret_cast<const float2 *>(T0 + oA + SY);
+      const float Bk = T0[oA - 1], Fw = T0[oA + 2];
+      const float al = (float)(scale * scale) * D.ph.dx * D.ph.dx;
+      const double lA = (double)L.x + (double)R.x + (double)Dn.x + (double)U.x + (double)Bk + (double)p2.y -
+                        6.0 * (double)p2.x;
+      const double lB = (double)L.y + (double)R.y + (double)Dn.y + (double)U.y + (double)p2.x + (double)Fw -
+                        6.0 * (double)p2.y;
+      const double rA = (double)dv.x - lA / (double)al, rB = (double)dv.y - lB / (double)al;
+      reinterpret_cast<float2 *>(D.rr + own)[lane] = make_float2((float)rA, (float)rB);
+      a_res += rA * rA;
+      a_res += rB * rB;
+      a_mass += (double)dv.x * (double)dv.x;
+      a_mass += (double)dv.y * (double)dv.y;
+      __syncwarp();
+    } else if constexpr (STAGE == 4) {
       // stats_vals for the lane's two cells: pressure tile, FP32 residual and mass
       const float2 p2 = reinterpret_cast<const float2 *>(D.p + own)[lane];
       float hp[3];
@@ -1421,6 +1414,7 @@ __global__ void __launch_bounds__(256) k_cells_staged(const __grid_constant__ Ce
     }
   }
   if (STAGE == 4 && a_mem >= 0) flush();
+  if (STAGE == 6 && a_mem >= 0) flush_defect();
 }
 // ------------------------------------------------------ staged advection
 // Advection one warp per block: the block's 64 cells and its 152 apron cells
@@ -1741,15 +1735,16 @@ static void launch_advect_staged(int stage, const CellBatch &P, cudaStream_t st)
 }
 
 static unsigned staged_grid(int stage) {
-  static unsigned g[3] = {0, 0, 0};
-  const int i = stage == 2 ? 0 : stage == 3 ? 1 : 2;
+  static unsigned g[4] = {0, 0, 0, 0};
+  const int i = stage == 2 ? 0 : stage == 3 ? 1 : stage == 4 ? 2 : 3;
   if (!g[i]) {
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (stage == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cells_staged<2>, 256, 0);
     else if (stage == 3) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cells_staged<3>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cells_staged<4>, 256, 0);
+    else if (stage == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cells_staged<4>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cells_staged<6>, 256, 0);
     g[i] = (unsigned)(sms * (occ > 0 ? occ : 1));
   }
   return g[i];
@@ -1823,11 +1818,12 @@ static void cells_batch_tb(int stage, const CellBatch &P, unsigned grid, cudaStr
   }
 }
 void launch_cells_batch(int stage, CellBatch &P, int tile, cudaStream_t st, bool persistent) {
-  if (tile == 1 || stage == 5) {  // staged, one warp per block (5: staged only)
+  if (tile == 1 || stage >= 5) {  // staged, one warp per block (5, 6: staged only)
     if (stage < 2 || stage == 5) launch_advect_staged(stage, P, st);
     else if (stage == 2) k_cells_staged<2><<<staged_grid(2), 256, 0, st>>>(P);
     else if (stage == 3) k_cells_staged<3><<<staged_grid(3), 256, 0, st>>>(P);
-    else k_cells_staged<4><<<staged_grid(4), 256, 0, st>>>(P);
+    else if (stage == 4) k_cells_staged<4><<<staged_grid(4), 256, 0, st>>>(P);
+    else k_cells_staged<6><<<staged_grid(6), 256, 0, st>>>(P);
     return;
   }
   if (tile != 2 && tile != 8) tile = 4;

@@ -87,6 +87,64 @@ __device__ __forceinline__ void build_nbr_body(const Dev &D, int only_if_touched
 }
 __global__ void __launch_bounds__(256) k_build_nbr(Dev D, int only_if_touched) { build_nbr_body(D, only_if_touched, blockIdx.x, gridDim.x); }
 
+// The neighbour table after an adaptation. With ref_compat, the rules of the
+// reference's apron refresh (k_dcgrid_refresh_apron_indices,
+// dcgrid_structure.cu:30-92) applied to each direction's entry: a moved or
+// new block looks all its neighbours up afresh; another block looks a
+// direction up afresh when its neighbour there moved, and when that
+// neighbour is coarser and was refined it takes the refined subblock's child
+// (one level deeper, as the reference does even where a finer block now
+// lies). The cells of one direction's apron region lie in one subblock of a
+// coarser neighbour (block positions are multiples of 4 cells), so the
+// reference's per-cell update is the same for the whole direction. Without
+// ref_compat every entry is looked up afresh.
+__device__ __forceinline__ void refresh_nbr_body(const Dev &D, unsigned bx, unsigned gx) {
+  if (!D.g.ref_compat) {
+    build_nbr_body(D, 1, bx, gx);
+    return;
+  }
+  if (D.ctr[C_TOUCHED] == 0) return;
+  const long long gid = (long long)bx * blockDim.x + threadIdx.x;
+  const long long b = gid / 27;
+  if (b >= D.g.B) return;
+  const int d = (int)(gid % 27);
+  const int4 bp = D.pos[b];
+  if (bp.w < 0 || d == 13) return;
+  uint32_t e = D.nbr[27 * b + d];
+  bool fresh = (D.flags[b] & MOVED) != 0;
+  if (!fresh && e != OUT) {
+    const uint32_t nb = e & NBR_MASK;
+    const int k = (int)(e >> 28);
+    const uint8_t fl = D.flags[nb];
+    if (fl & MOVED) {
+      fresh = true;
+    } else if ((fl & REFINED) && k > 0) {
+      // a cell of the direction's region, at the neighbour's level
+      const int dx = d / 9 - 1, dy = (d / 3) % 3 - 1, dz = d % 3 - 1;
+      const int x = dx < 0 ? bp.x - 1 : (dx > 0 ? bp.x + BW : bp.x);
+      const int y = dy < 0 ? bp.y - 1 : (dy > 0 ? bp.y + BW : bp.y);
+      const int z = dz < 0 ? bp.z - 1 : (dz > 0 ? bp.z + BW : bp.z);
+      const int4 np = D.pos[nb];
+      const int lx = (x >> k) - np.x, ly = (y >> k) - np.y, lz = (z >> k) - np.z;
+      const uint32_t c = D.child[8u * nb + (uint32_t)((((lx >> 1) & 1) << 2) | (((ly >> 1) & 1) << 1) | ((lz >> 1) & 1))];
+      if (c != NONE) e = ((uint32_t)(k - 1) << 28) | c;
+    }
+  }
+  if (fresh) {
+    const int L = bp.w, scale = 1 << L;
+    const int qx = bp.x + BW * (d / 9 - 1), qy = bp.y + BW * ((d / 3) % 3 - 1), qz = bp.z + BW * (d % 3 - 1);
+    if (qx < 0 || qy < 0 || qz < 0 || qx * scale >= D.g.gx || qy * scale >= D.g.gy || qz * scale >= D.g.gz) {
+      e = OUT;
+    } else {
+      int lev;
+      const uint32_t nb = locate(D, qx, qy, qz, L, lev);
+      e = ((uint32_t)(lev - L) << 28) | nb;
+    }
+  }
+  D.nbr[27 * b + d] = e;
+}
+__global__ void __launch_bounds__(256) k_refresh_nbr(Dev D) { refresh_nbr_body(D, blockIdx.x, gridDim.x); }
+
 // ------------------------------------------------------------------ scores
 __device__ inline bool level_blocked(const Dev &D, int level) {
   return (level == 0 && D.load[0] == D.g.full[0]) ||
@@ -286,6 +344,7 @@ __device__ __forceinline__ void apply_moves_body(const Dev &D, int L, uint32_t *
     const uint32_t pb = dest >> 3;
     const int4 pp = D.pos[pb];
     const int4 old = D.pos[b];
+    D.mold[m] = old;
     D.pos[b] = make_int4(2 * pp.x + BW * ((dest >> 2) & 1), 2 * pp.y + BW * ((dest >> 1) & 1),
                          2 * pp.z + BW * (dest & 1), old.w);
     D.flags[b] |= MOVED;
@@ -301,7 +360,12 @@ __global__ void __launch_bounds__(256) k_apply_moves(Dev D, int L, uint32_t *pre
 // values; moves change only the positions of moved blocks and the child
 // pointers of their previous and new parent subblocks. Recomputing those
 // subblocks (10 per move: the moved block's 8, the old and the new parent
-// subblock) gives exactly the scores of a full pass.
+// subblock) gives exactly the scores of a full pass. The neighbour table is
+// rebuilt only after the refinements, as the reference's apron indices are
+// refreshed only then (dcgrid_structure.cu:30-92): until then a moved block
+// reads the neighbours of its old place, so its cells in a coarser neighbour
+// come from its position before the move (mold), as the stored apron
+// indices give them.
 __device__ __forceinline__ uint32_t rescore_target(const Dev &D, const uint32_t *prevs, long long t) {
   const long long m = t / 10;
   const int k = (int)(t - 10 * m);
@@ -326,7 +390,9 @@ __device__ __forceinline__ void rescore_body(const Dev &D, const uint32_t *prevs
     const long long t = tw + (lane >> 3);
     const uint32_t sb = t < ntask ? rescore_target(D, prevs, t) : NONE;
     const long long b = sb == NONE ? 0 : (long long)(sb >> 3);
-    const int4 bp = sb == NONE ? make_int4(0, 0, 0, -1) : D.pos[b];
+    // a moved block's own subblocks (targets 0-7 of its move): its old position
+    const bool own = t < ntask && t - 10 * (t / 10) < 8;
+    const int4 bp = sb == NONE ? make_int4(0, 0, 0, -1) : (own ? D.mold[t / 10] : D.pos[b]);
     const bool blocked = sb == NONE || subblock_blocked(D, sb, bp);
     const float m = max8(blocked ? 0.f : field_cell_score(D, b, bp, (int)(8 * (sb & 7) + (lane & 7))));
     if ((lane & 7) == 0 && sb != NONE) D.ss[sb] = blocked ? -FLT_MAX : m;
@@ -645,8 +711,8 @@ void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *
   }
   k_apply_refines<<<gs, 256, 0, st>>>(D);
   k_finish_refines<<<1, 1, 0, st>>>(D);
-  // neighbour tables + value propagation for touched blocks
-  launch_build_nbr(D, true, st);
+  // neighbour tables (the refresh after an adaptation) + value propagation for touched blocks
+  k_refresh_nbr<<<grid_for(D.g.B * 27), 256, 0, st>>>(D);
   for (int L = D.g.levels - 2; L >= 0; L--) k_propagate<<<gs, 256, 0, st>>>(D, L);
 }
 
@@ -901,7 +967,7 @@ template <int OP, int T> __global__ void __launch_bounds__(T) k_adapt_batch(cons
   if constexpr (OP == A_FINISH) {
     if (threadIdx.x == 0) finish_refines_body(D, bx, gx);
   }
-  if constexpr (OP == A_NBR) build_nbr_body(D, 1, bx, gx);
+  if constexpr (OP == A_NBR) refresh_nbr_body(D, bx, gx);
   if constexpr (OP == A_PROPAGATE) propagate_body(D, L, bx, gx);
 }
 

@@ -1389,8 +1389,17 @@ template <typename R> struct DC : Base {
   }
   // k_dcgrid_refresh_apron_indices (dcgrid_structure.cu:30-92). Out-of-domain
   // entries of moved blocks are set with SPREAD(clamp(i,1,4)) as in the
-  // reference (local coordinate i mod 4) when ref_compat is on.
+  // reference (local coordinate i mod 4) when ref_compat is on. The
+  // reference's refresh goes at most one level deeper for an entry whose
+  // block was refined: when a block moves into a place and one of its
+  // subblocks is refined in the same adaptation, a neighbour keeps pointing at
+  // the moved (coarser) block until a later refresh. ref_compat keeps that;
+  // without it every entry is the finest block's (a fresh lookup).
   void refresh_apron() {
+    if (!P.ref_compat) {
+      rebuild_apron_fresh();
+      return;
+    }
 #pragma omp parallel for schedule(dynamic, 64)
     for (int64_t b = 0; b < B; b++) {
       if (lvl[b] == FREE) continue;

@@ -8,9 +8,10 @@
   and the FP32 path stays within 1e-4 relative L2 of the FP64 oracle per field
   (the FP64 oracle replays the GPU's adaptation decisions).
 * Cloud, effective 256^3, 3 levels, 40000-block budget, terrain, wind inflow,
-  three scalars, field-driven refinement, 100 sweeps: after a GPU spin-up the
-  oracle's float mirror takes over the GPU state, and for the next steps both
-  step independently and stay bit-identical.
+  three scalars, field-driven refinement, 100 sweeps: from creation the GPU
+  and the oracle's float mirror stay bit-identical after every one of 12
+  steps; after a GPU spin-up the float mirror takes over the GPU state, and
+  for the next steps both step independently and stay bit-identical.
 * Largest plume of the benchmark batch (256^3, FP16 storage): density error
   against the FP64 oracle at the benchmark's horizon (spin-up + timed steps).
 """
@@ -104,6 +105,34 @@ def test_cloud256_40k_blocks_spun_up_window_bitexact():
         moved += g.stats().moved_blocks + g.stats().refined_subblocks
     assert g.stats().active_cells > 500_000
     assert moved > 0  # the window includes topology changes
+
+
+@pytest.mark.parametrize("compat", [0, 1])
+def test_cloud256_40k_blocks_from_creation_bitexact_every_step(compat):
+    """The same cloud from creation: GPU and float mirror step independently
+    for 12 steps and stay bit-identical after every step. The early steps
+    move blocks next to coarser levels while refining heavily, so the
+    rescoring after the moves must see a moved block's neighbours as the
+    not yet refreshed neighbour indices give them (from its old place). With
+    ref_compat the neighbour refresh after step 9 keeps the reference's
+    entries that point one level too coarse (a block moved in and refined in
+    the same adaptation); without it every entry is the finest block's."""
+    from dcgrid_gb300 import Simulation
+    p = scenes.cloud256()
+    p.ref_compat = compat
+    g, o = Simulation(p), _oracle(p, "float")
+    em = scenes.emission_field(16, 1)
+    for s in (g, o):
+        s.set_emission(em)
+        s.add_velocity_noise(0, 0.01)
+    moved = 0
+    for k in range(12):
+        g.step(1)
+        o.step(1)
+        g.sync()
+        compare(g, o, p, f"step {k + 1}")
+        moved += g.stats().moved_blocks
+    assert moved > 0
 
 
 def test_largest_batch_member_fp16_density_error_at_bench_horizon():
