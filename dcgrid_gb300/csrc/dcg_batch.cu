@@ -118,25 +118,33 @@ struct dcg_batch {
   }
 
   // ------------------------------------------------------------ stage launches
-  void cells(int stage) {
-    for (int g = 0; g < groups(); g++) {
+  // the members a stage launch covers: all, or the listed ones
+  std::vector<int> all_members() const {
+    std::vector<int> v(n());
+    for (int i = 0; i < n(); i++) v[i] = i;
+    return v;
+  }
+  void cells(int stage) { cells(stage, all_members(), stream); }
+  void cells(int stage, const std::vector<int> &mem, cudaStream_t st) {
+    for (size_t g = 0; g < mem.size(); g += BMAX) {
       CellBatch P{};
-      P.n = std::min(BMAX, n() - g * BMAX);
-      for (int i = 0; i < P.n; i++) P.d[i] = m[g * BMAX + i]->D;
-      launch_cells_batch(stage, P, stage == 5 ? 1 : tune.tile[stage], stream, tune.persistent != 0);
+      P.n = (int)std::min<size_t>(BMAX, mem.size() - g);
+      for (int i = 0; i < P.n; i++) P.d[i] = m[mem[g + i]]->D;
+      launch_cells_batch(stage, P, stage == 5 ? 1 : tune.tile[stage], st, tune.persistent != 0);
     }
   }
   // field: 0 velocity, 1 scalars, 2 divergence, 3 velocity and scalars
-  void restrict_fields(int field) {
+  void restrict_fields(int field) { restrict_fields(field, all_members(), stream); }
+  void restrict_fields(int field, const std::vector<int> &mem, cudaStream_t st) {
     int maxl = 0;
-    for (dcg_sim *s : m) maxl = std::max(maxl, s->D.g.levels);
+    for (int i : mem) maxl = std::max(maxl, m[i]->D.g.levels);
     for (int level = 0; level < maxl - 1; level++)
-      for (int g = 0; g < groups(); g++) {
+      for (size_t g = 0; g < mem.size(); g += BMAX) {
         RestrictBatch P{};
-        P.n = std::min(BMAX, n() - g * BMAX);
+        P.n = (int)std::min<size_t>(BMAX, mem.size() - g);
         P.level = level;
         for (int i = 0; i < P.n; i++) {
-          const dcg_sim *s = m[g * BMAX + i];
+          const dcg_sim *s = m[mem[g + i]];
           P.d[i] = s->D;
           FieldList &fl = P.fl[i];
           if (field == 0 || field == 3) {
@@ -156,7 +164,7 @@ struct dcg_batch {
             fl.f[0] = s->D.div;
           }
         }
-        launch_restrict_batch(P, stream);
+        launch_restrict_batch(P, st);
       }
   }
   // the arenas of the planes the cascade runs on; with the correction planes,
@@ -316,6 +324,42 @@ struct dcg_batch {
       restrict_fields(1);
     }
   }
+  // With rounds aligned at the coarsest levels, the members with fewer levels
+  // finish their cascade a round early. Their pressure application, scalar
+  // advection and restrictions then run on the second stream (a parallel
+  // graph branch) while the last rounds relax the other members: the
+  // stages read and write only their own members' planes, and the late
+  // rounds, small and bound by their grid barriers, leave most of the GPU free.
+  bool overlapped() const {
+    return dpass == 0 && fused() && can_split() && (tune.solve_barrier & 2) && !(tune.solve_barrier & 4);
+  }
+  void apply_advect_members(const std::vector<int> &mem, cudaStream_t st) {
+    cells(5, mem, st);  // apply pressure + advect scalars (+ sources, emission)
+    for (int i : mem) {
+      m[i]->qpar ^= 1;
+      m[i]->bind_parity();
+    }
+    restrict_fields(3, mem, st);
+  }
+  void solve_apply_overlapped() {
+    const int ga = m[lgroup[0][0]]->D.g.levels < m[lgroup[1][0]]->D.g.levels ? 0 : 1;  // fewer levels
+    const int last = m[lgroup[ga][0]]->D.g.levels - 1;  // its last round
+    for (int round = 0; round <= maxtop; round++) {
+      if (round < 4 && tune.round_ctas_per_sm[round] != 0)
+        solve_round(round, batch_solve_grid(sms, tune.round_cache[round], tune.round_ctas_per_sm[round]),
+                    tune.round_cache[round], tune.round_barrier[round]);
+      else
+        solve_round(round, solve_grid, tune.solve_cache, tune.solve_barrier & 1);
+      if (round == last) {
+        cudaEventRecord(ev_fork, stream);
+        cudaStreamWaitEvent(aux, ev_fork, 0);
+        apply_advect_members(lgroup[ga], aux);
+        cudaEventRecord(ev_join, aux);
+      }
+    }
+    apply_advect_members(lgroup[1 - ga], stream);
+    cudaStreamWaitEvent(stream, ev_join, 0);
+  }
   void step_once() {
     cells(0);  // advect velocity (+ buoyancy)
     flip_v();
@@ -323,6 +367,10 @@ struct dcg_batch {
     adapt();
     cells(2);  // divergence
     restrict_fields(2);
+    if (overlapped()) {
+      solve_apply_overlapped();
+      return;
+    }
     solve_tuned();
     if (dpass > 0) defect_correct();
     apply_advect();
