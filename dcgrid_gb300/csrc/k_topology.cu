@@ -665,6 +665,14 @@ static void launch_scores(const Dev &D, cudaStream_t st) {
     launch_scores_staged(&D, 1, st);
 }
 
+// A level whose budget covers its whole block grid is allocated in full when
+// the simulation is created and keeps every block (blocks are never freed),
+// so its move limit (free places at the level) and the refinement limit of
+// the level above it (free blocks at the level) are 0: those passes change
+// nothing and are not launched. (Their only writes are the pass's own
+// scratch counters.)
+static bool level_full(const Geom &g, int L) { return g.budget[L] == g.full[L]; }
+
 // FluidSimulationDCGrid::adaptTopology (fluid_simulation_dcgrid.cu:320-346)
 // as a fixed sequence of launches.
 void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *vals, uint32_t *keys2,
@@ -676,6 +684,7 @@ void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *
   launch_scores(D, st);
   k_block_scores<<<grid_for(D.g.B), 256, 0, st>>>(D);
   for (int L = 0; L < D.g.levels - 1; L++) {
+    if (level_full(D.g, L)) continue;  // no free place at level L: no move (limit 0)
     const long long d0 = D.g.budget[L], d1 = 8 * D.g.budget[L + 1];
     k_move_setup<<<1, 1, 0, st>>>(D, L);
     k_keys_blocks<<<grid_for(d0), 256, 0, st>>>(D, L, keys, vals);
@@ -685,11 +694,13 @@ void launch_adapt(const Dev &D, const SortScratch &s, uint32_t *keys, uint32_t *
     k_match<<<gs, 256, 0, st>>>(D, vals, vals2);
     k_commit_moves<<<gs, 256, 0, st>>>(D, L, vals, vals2);
   }
-  for (int L = D.g.levels - 2; L >= 0; L--) k_apply_moves<<<gs, 256, 0, st>>>(D, L, keys);
+  for (int L = D.g.levels - 2; L >= 0; L--)
+    if (!level_full(D.g, L)) k_apply_moves<<<gs, 256, 0, st>>>(D, L, keys);
   // refineSubblocks
   k_rescore<<<gs, 256, 0, st>>>(D, keys);
   uint8_t *sel = reinterpret_cast<uint8_t *>(keys2);  // 8*B bytes, reused as selection flags
   for (int L = 1; L < D.g.levels; L++) {
+    if (level_full(D.g, L - 1)) continue;  // no free block at level L-1: no refinement (limit 0)
     const long long n8 = 8 * D.g.budget[L];
     const long long nt = (n8 + CMP_TILE - 1) / CMP_TILE;
     k_refine_setup<<<1, 1, 0, st>>>(D, L);
@@ -1031,7 +1042,7 @@ struct AdaptLauncher {
     go<A_BLOCK_SCORES>([&](int i) { return (long long)grid_for(B(i)); });
     for (int L = 0; L < maxl - 1; L++) {
       P.L = L;
-      auto has = [&](int i) { return L < levels(i) - 1; };
+      auto has = [&](int i) { return L < levels(i) - 1 && !level_full(m[i].D.g, L); };
       go<A_MOVE_SETUP, 32>([&](int i) { return has(i) ? 1 : 0; });
       for (int i = 0; i < n; i++) {
         P.p0[i] = m[i].keys;
@@ -1064,7 +1075,7 @@ struct AdaptLauncher {
     for (int i = 0; i < n; i++) P.p0[i] = m[i].keys;  // previous parents of the moved blocks
     for (int L = maxl - 2; L >= 0; L--) {
       P.L = L;
-      go<A_APPLY_MOVES>([&](int i) { return L < levels(i) - 1 ? gs : 0u; });
+      go<A_APPLY_MOVES>([&](int i) { return L < levels(i) - 1 && !level_full(m[i].D.g, L) ? gs : 0u; });
     }
     // refineSubblocks
     go<A_RESCORE>([&](int i) { return gs; });
@@ -1072,7 +1083,7 @@ struct AdaptLauncher {
       P.L = L;
       std::vector<bool> in(n), compat(n), score(n);
       for (int i = 0; i < n; i++) {
-        in[i] = L < levels(i);
+        in[i] = L < levels(i) && !level_full(m[i].D.g, L - 1);
         compat[i] = in[i] && m[i].D.g.ref_compat;
         score[i] = in[i] && !m[i].D.g.ref_compat;
       }
