@@ -272,6 +272,19 @@ __device__ __forceinline__ float div6(float x) {
   return r == r ? y : q;
 }
 
+// div6 of both components with packed FP32x2 operations (each component the
+// correctly rounded operation of div6's scalar form, so the results are div6's)
+__device__ __forceinline__ float2 div6x2(float2 x) {
+  const float2 z = make_float2(0x1.555556p-3f, 0x1.555556p-3f);
+  const float2 q = __fmul2_rn(x, z);
+  const float2 r = __ffma2_rn(q, make_float2(-6.f, -6.f), x);  // x - 6 q, exactly as fmaf(-q, 6, x)
+  const float2 y = __ffma2_rn(r, z, q);
+  float2 o;
+  o.x = (!(fabsf(x.x) >= 0x1p-120f) && x.x == x.x) ? x.x / 6.f : (r.x == r.x ? y.x : q.x);
+  o.y = (!(fabsf(x.y) >= 0x1p-120f) && x.y == x.y) ? x.y / 6.f : (r.y == r.y ? y.y : q.y);
+  return o;
+}
+
 __device__ inline int dir_of(int a) { return a == 0 ? 0 : (a == AW - 1 ? 2 : 1); }
 
 // Global cell index of apron cell (ax, ay, az) in [0,6)^3 of block b.

@@ -930,11 +930,18 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
         const float Bk = T[oA - 1], Fw = T[oA + 2];
         const float2 dv = *reinterpret_cast<const float2 *>(s_pd[w][buf] + 2 * lane);
         const float al = __uint_as_float(b_alpha[buf]);
-        const float adA = al * dv.x, adB = al * dv.y;
-        float2 res;
-        res.x = div6(L.x + R.x + Dn.x + Up.x + Bk + ab.y - adA);
-        res.y = div6(L.y + R.y + Dn.y + Up.y + ab.x + Fw - adB);
-        dstl[own >> 1] = res;
+        // the lane's two cells with packed FP32x2 operations, each component
+        // the correctly rounded operation of the scalar form in the same order:
+        // cell a: L + R + D + U + B + (cell b) - alpha div; cell b: L + R + D +
+        // U + (cell a) + F - alpha div
+        float2 sum = __fadd2_rn(L, R);
+        sum = __fadd2_rn(sum, Dn);
+        sum = __fadd2_rn(sum, Up);
+        sum = __fadd2_rn(sum, make_float2(Bk, ab.x));
+        sum = __fadd2_rn(sum, make_float2(ab.y, Fw));
+        const float2 ad = __fmul2_rn(make_float2(al, al), dv);
+        sum = __fadd2_rn(sum, make_float2(-ad.x, -ad.y));
+        dstl[own >> 1] = div6x2(sum);
       }
       __syncwarp();  // buffer `buf` may be refilled by the next issue
     }
@@ -1750,7 +1757,8 @@ static unsigned staged_grid(int stage) {
   return g[i];
 }
 
-// Self-check of div6: every binary32 bit pattern against the IEEE division
+// Self-check of div6 and its packed form div6x2: every binary32 bit pattern
+// against the IEEE division
 // (NaN results compare equal whatever their payload).
 __global__ void __launch_bounds__(256) k_check_div6(unsigned long long *bad) {
   unsigned long long n = 0;
@@ -1759,7 +1767,13 @@ __global__ void __launch_bounds__(256) k_check_div6(unsigned long long *bad) {
        u += stride) {
     const float x = __uint_as_float((uint32_t)u);
     const float a = x / 6.f, b = div6(x);
-    if (__float_as_uint(a) != __float_as_uint(b) && !(a != a && b != b)) {
+    // the packed form, with x in either component (the other a different input)
+    const float2 p = div6x2(make_float2(x, __uint_as_float((uint32_t)u ^ 0x80000001u)));
+    const float2 p2 = div6x2(make_float2(__uint_as_float((uint32_t)u + 0x01234567u), x));
+    const bool ok = (__float_as_uint(a) == __float_as_uint(b) || (a != a && b != b)) &&
+                    (__float_as_uint(a) == __float_as_uint(p.x) || (a != a && p.x != p.x)) &&
+                    (__float_as_uint(a) == __float_as_uint(p2.y) || (a != a && p2.y != p2.y));
+    if (!ok) {
       n++;
       atomicMin(bad + 1, u);
     }
