@@ -35,7 +35,7 @@ struct dcg_batch {
   double *dnorm_arena = nullptr;
   // planes the cascade runs on: 0 = p, p~, div; 1 = e, e~, r (the correction)
   int planes = 0;
-  uint32_t *binfo = nullptr;  // block descriptions of a cascade round, 13 words per block
+  uint32_t *binfo = nullptr;  // block descriptions of a cascade round, BI_WORDS words per block
   uint32_t *bar = nullptr, *errw = nullptr;
   // concurrent cascades (solve_barrier bit 2): members with two different level
   // counts solved by two cooperative launch chains on parallel graph branches,
@@ -707,7 +707,7 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
     return rc;
   }
   if ((rc = b->alloc(&b->p_arena, cells)) || (rc = b->alloc(&b->pt_arena, cells)) ||
-      (rc = b->alloc(&b->div_arena, cells)) || (rc = b->alloc(&b->binfo, 13 * (cells / BV))) ||
+      (rc = b->alloc(&b->div_arena, cells)) || (rc = b->alloc(&b->binfo, BI_WORDS * (cells / BV))) ||
       (rc = b->alloc(&b->bar, 64 + 32 * 18)) || (rc = b->alloc(&b->errw, 4))) {
     delete b;
     return rc;
@@ -720,7 +720,7 @@ int dcg_batch_create(int32_t n, const dcg_params *params, dcg_batch **out) {
     delete b;
     return rc;
   }
-  if ((rc = b->alloc(&b->bar2, 64 + 32 * 18)) || (rc = b->alloc(&b->binfo2, 13 * (cells / BV)))) {
+  if ((rc = b->alloc(&b->bar2, 64 + 32 * 18)) || (rc = b->alloc(&b->binfo2, BI_WORDS * (cells / BV)))) {
     delete b;
     return rc;
   }

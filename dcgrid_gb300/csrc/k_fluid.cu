@@ -706,14 +706,15 @@ __global__ void __launch_bounds__(256) k_restrict_batch(const __grid_constant__ 
   restrict_subblock(D, P.level, P.fl[s], ((long long)blockIdx.x - (s ? P.end[s - 1] : 0)) * 256 + threadIdx.x);
 }
 
-// Description of one block for the staged sweep, BI_WORDS words: [0] arena
-// index of its first cell, [1] alpha (bits), [2..4] level-local position,
-// [5..10] arena index of the first cell of the block that holds the halo of
-// face f (-x, +x, -y, +y, -z, +z; the block itself when the face is outside),
-// [11..12] one byte per face: levels by which that block is coarser, 16 for
-// outside, 17 for outside under the compat quirk of apron_cell. Lanes 0-5
-// resolve one face each, lane 6 the rest.
-constexpr int BI_WORDS = 13;
+// Description of one block for the staged sweep, BI_WORDS words: [BI_OWN]
+// arena index of its first cell, [BI_ALPHA] alpha (bits), [BI_CODES..+1] one
+// byte per face (-x, +x, -y, +y, -z, +z): levels by which the block that holds
+// the face's halo is coarser, 16 for outside, 17 for outside under the compat
+// quirk of apron_cell, [BI_FACE..+5] arena index of the first cell of that
+// block (the block itself when the face is outside), [BI_POS..+2] level-local
+// position. Even word offsets for the pairs, so that a lane reads (own,
+// alpha) and the two code words with one 8-byte load each. Lanes 0-5 resolve
+// one face each, lane 6 the rest.
 __device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long long *s_end, const int *s_lev,
                                                 long long gb, uint32_t *bi, int lane) {
   const int m = batch_member(s_end, P.n, gb << 6);
@@ -732,16 +733,17 @@ __device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long 
       base = a + (e & NBR_MASK) * BV;
       code = e >> 28;
     }
-    bi[5 + lane] = base;
-    reinterpret_cast<uint8_t *>(bi + 11)[lane] = (uint8_t)code;
+    bi[BI_FACE + lane] = base;
+    reinterpret_cast<uint8_t *>(bi + BI_CODES)[lane] = (uint8_t)code;
   } else if (lane == 6) {
     const int4 bp = D.pos[b];
-    bi[0] = a + b * BV;
+    bi[BI_OWN] = a + b * BV;
     const int sc = 1 << lev;
-    bi[1] = __float_as_uint((float)(sc * sc) * D.ph.dx * D.ph.dx);
-    bi[2] = (uint32_t)bp.x;
-    bi[3] = (uint32_t)bp.y;
-    bi[4] = (uint32_t)bp.z;
+    bi[BI_ALPHA] = __float_as_uint((float)(sc * sc) * D.ph.dx * D.ph.dx);
+    bi[BI_POS] = (uint32_t)bp.x;
+    bi[BI_POS + 1] = (uint32_t)bp.y;
+    bi[BI_POS + 2] = (uint32_t)bp.z;
+    bi[BI_WORDS - 1] = 0u;
   }
 }
 
@@ -758,7 +760,7 @@ __device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long 
 #define DCG_SOLVE_MINB 4
 #endif
 #ifndef DCG_PIPE_MINB
-#define DCG_PIPE_MINB 4
+#define DCG_PIPE_MINB 3
 #endif
 
 // ---- pipelined staged sweeps
@@ -796,7 +798,11 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
 // while a block is computed from its tile.
 // The copies read the previous sweep's results written by other SMs; the grid
 // barrier's fences order them. Block descriptions come from the launch's
-// shared cache when they fit, else from the global table, through shuffles.
+// shared cache when they fit, else from the global table: every lane loads
+// the words it needs (warp-wide broadcasts). Broadcast loads cost the
+// shared-memory pipe, which bounds the sweep, less than warp shuffles of the
+// same words do; measured on the 16-plume batch, so are the shuffles that
+// would replace the tile reads of the neighbours inside the block.
 template <int CACHE, int NB>
 __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long long *s_end, const int *s_lev,
                                                 uint32_t *s_cache, long long total, unsigned nctas, int sweeps,
@@ -861,28 +867,35 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
       if (lane == 0) kk = atomicAdd(cnt, 1u);
       const int k = (int)__shfl_sync(full, kk, 0);
       const bool act = k < kcount;  // warp-uniform; a warp's claims only grow
-      uint32_t biw = 0;
-      if (act && lane < BI_WORDS) {
+      // the block's description: each lane loads the words it needs (the
+      // same address across the warp, one broadcast each) from the launch's
+      // shared cache or the global table
+      const long long gbk = ((long long)(k >> 3) * nctas + blockIdx.x) * W + (k & 7);
+      const uint32_t *big = P.binfo + gbk * BI_WORDS, *bis = s_cache + k * BI_WORDS;
+      uint2 oa = make_uint2(0u, 0u), cw = make_uint2(0u, 0u);
+      uint32_t fb[3] = {0u, 0u, 0u};
+      if (act) {
         if (cached) {
-          biw = s_cache[k * BI_WORDS + lane];
+          oa = *reinterpret_cast<const uint2 *>(bis + BI_OWN);
+          cw = *reinterpret_cast<const uint2 *>(bis + BI_CODES);
+#pragma unroll
+          for (int q = 0; q < 3; q++) fb[q] = bis[BI_FACE + (hax[q] >> 12)];
         } else {
-          const long long gb = ((long long)(k >> 3) * nctas + blockIdx.x) * W + (k & 7);
-          biw = __ldcg(P.binfo + gb * BI_WORDS + lane);
+          oa = __ldcg(reinterpret_cast<const uint2 *>(big + BI_OWN));
+          cw = __ldcg(reinterpret_cast<const uint2 *>(big + BI_CODES));
+#pragma unroll
+          for (int q = 0; q < 3; q++) fb[q] = __ldcg(big + BI_FACE + (hax[q] >> 12));
         }
       }
-      const uint32_t own = __shfl_sync(full, biw, 0);
-      const uint32_t alpha = __shfl_sync(full, biw, 1);
-      const uint32_t c11 = __shfl_sync(full, biw, 11), c12 = __shfl_sync(full, biw, 12);
-      uint32_t fb[3];
-#pragma unroll
-      for (int q = 0; q < 3; q++) fb[q] = __shfl_sync(full, biw, 5 + (int)(hax[q] >> 12));
+      const uint32_t own = oa.x, alpha = oa.y, c11 = cw.x, c12 = cw.y;
       uint32_t addr[3];
       if (c11 == 0u && (c12 & 0xFFFFu) == 0u) {  // all six faces border same-level blocks
 #pragma unroll
         for (int q = 0; q < 3; q++) addr[q] = fb[q] + ((hpk[q] >> 9) & 63u);
       } else {
-        const int bx = (int)__shfl_sync(full, biw, 2), by = (int)__shfl_sync(full, biw, 3),
-                  bz = (int)__shfl_sync(full, biw, 4);
+        const uint32_t *bip = (cached ? bis : big) + BI_POS;
+        const int bx = (int)(cached ? bip[0] : __ldcg(bip)), by = (int)(cached ? bip[1] : __ldcg(bip + 1)),
+                  bz = (int)(cached ? bip[2] : __ldcg(bip + 2));
 #pragma unroll
         for (int q = 0; q < 3; q++) {
           const uint32_t pk = hpk[q], ga = hax[q];
@@ -1092,14 +1105,14 @@ __global__ void __launch_bounds__(256, NB ? MB : DCG_SOLVE_MINB)
           if (lane < BI_WORDS) s_scratch[w][u][lane] = P.binfo[gb * BI_WORDS + lane];
           __syncwarp();
         }
-        const uint32_t own = bi[0];
+        const uint32_t own = bi[BI_OWN];
         uint32_t addr[3];
-        if (bi[11] == 0u && (bi[12] & 0xFFFFu) == 0u) {
+        if (bi[BI_CODES] == 0u && (bi[BI_CODES + 1] & 0xFFFFu) == 0u) {
           // all six faces border same-level blocks (warp-uniform fast path)
 #pragma unroll
-          for (int q = 0; q < 3; q++) addr[q] = bi[5 + (hax[q] >> 12)] + ((hpk[q] >> 9) & 63);
+          for (int q = 0; q < 3; q++) addr[q] = bi[BI_FACE + (hax[q] >> 12)] + ((hpk[q] >> 9) & 63);
         } else {
-          const uint8_t *codes = reinterpret_cast<const uint8_t *>(bi + 11);
+          const uint8_t *codes = reinterpret_cast<const uint8_t *>(bi + BI_CODES);
 #pragma unroll
           for (int q = 0; q < 3; q++) {
             const uint32_t pk = hpk[q], ga = hax[q];
@@ -1107,15 +1120,15 @@ __global__ void __launch_bounds__(256, NB ? MB : DCG_SOLVE_MINB)
             const int code = codes[f];
             uint32_t li = code == 0 ? (pk >> 9) & 63 : code == 16 ? (pk >> 15) & 63 : (pk >> 21) & 63;
             if (code > 0 && code < 16) {  // coarser by `code` levels: injection
-              const int cx = (int)bi[2] + (int)(ga & 15) - 1, cy = (int)bi[3] + (int)((ga >> 4) & 15) - 1,
-                        cz = (int)bi[4] + (int)((ga >> 8) & 15) - 1;
+              const int cx = (int)bi[BI_POS] + (int)(ga & 15) - 1, cy = (int)bi[BI_POS + 1] + (int)((ga >> 4) & 15) - 1,
+                        cz = (int)bi[BI_POS + 2] + (int)((ga >> 8) & 15) - 1;
               li = (uint32_t)local_of((cx >> code) & 3, (cy >> code) & 3, (cz >> code) & 3);
             }
-            addr[q] = bi[5 + f] + li;
+            addr[q] = bi[BI_FACE + f] + li;
           }
         }
         ps.own[u] = own;
-        ps.alpha[u] = __uint_as_float(bi[1]);
+        ps.alpha[u] = __uint_as_float(bi[BI_ALPHA]);
         ps.own_v[u] = __ldcg(reinterpret_cast<const float2 *>(src + own) + lane);
         ps.halo[u][0] = __ldcg(src + addr[0]);
         ps.halo[u][1] = __ldcg(src + addr[1]);
