@@ -59,7 +59,7 @@ void launch_level_solve(const Dev &D, int level, int prolong, int sweeps, int gr
 // through the constant cache); BMAX members fit the 32 KB parameter space.
 constexpr int BMAX = 16;
 // words of one block's description in a staged cascade sweep (fill_block_info)
-constexpr int BI_OWN = 0, BI_ALPHA = 1, BI_CODES = 2, BI_FACE = 4, BI_POS = 10, BI_WORDS = 14;
+constexpr int BI_OWN = 0, BI_ALPHA = 1, BI_CODES = 2, BI_FACE = 4, BI_POS = 10, BI_WORDS = 16;
 // cell stages: 0 advect velocity, 1 advect scalars, 2 divergence, 3 apply
 // pressure, 4 statistics (into each member's red; zero it first), 5 apply
 // pressure and advect scalars in one staged pass (the results of 3 then 1),

@@ -712,9 +712,9 @@ __global__ void __launch_bounds__(256) k_restrict_batch(const __grid_constant__ 
 // the face's halo is coarser, 16 for outside, 17 for outside under the compat
 // quirk of apron_cell, [BI_FACE..+5] arena index of the first cell of that
 // block (the block itself when the face is outside), [BI_POS..+2] level-local
-// position. Even word offsets for the pairs, so that a lane reads (own,
-// alpha) and the two code words with one 8-byte load each. Lanes 0-5 resolve
-// one face each, lane 6 the rest.
+// position, the rest zero. 16 words, so that a lane reads words 0-3 and 4-7
+// with one 16-byte load each and faces 4-5 with one 8-byte load. Lanes 0-5
+// resolve one face each, lane 6 the rest.
 __device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long long *s_end, const int *s_lev,
                                                 long long gb, uint32_t *bi, int lane) {
   const int m = batch_member(s_end, P.n, gb << 6);
@@ -743,7 +743,7 @@ __device__ __forceinline__ void fill_block_info(const SolveBatch &P, const long 
     bi[BI_POS] = (uint32_t)bp.x;
     bi[BI_POS + 1] = (uint32_t)bp.y;
     bi[BI_POS + 2] = (uint32_t)bp.z;
-    bi[BI_WORDS - 1] = 0u;
+    for (int j = BI_POS + 3; j < BI_WORDS; j++) bi[j] = 0u;
   }
 }
 
@@ -882,27 +882,29 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
         npend = DCG_PIPE_CLAIM - 1;
       }
       const bool act = k < kcount;  // warp-uniform; a warp's claims only grow
-      // the block's description: each lane loads the words it needs (the
-      // same address across the warp, one broadcast each) from the launch's
-      // shared cache or the global table
+      // the block's description: words 0-9 in three warp-wide broadcast
+      // loads (16, 16 and 8 bytes) from the launch's shared cache or the
+      // global table; a lane's halo slot q lies on face 2q or 2q + 1
+      static_assert(BI_OWN == 0 && BI_ALPHA == 1 && BI_CODES == 2 && BI_FACE == 4 && BI_WORDS % 4 == 0,
+                    "description words read as (own, alpha, codes), faces 0-3, faces 4-5");
       const long long gbk = ((long long)(k >> 3) * nctas + blockIdx.x) * W + (k & 7);
       const uint32_t *big = P.binfo + gbk * BI_WORDS, *bis = s_cache + k * BI_WORDS;
-      uint2 oa = make_uint2(0u, 0u), cw = make_uint2(0u, 0u);
-      uint32_t fb[3] = {0u, 0u, 0u};
+      uint4 wa = make_uint4(0u, 0u, 0u, 0u), wb = make_uint4(0u, 0u, 0u, 0u);
+      uint2 wc = make_uint2(0u, 0u);
       if (act) {
         if (cached) {
-          oa = *reinterpret_cast<const uint2 *>(bis + BI_OWN);
-          cw = *reinterpret_cast<const uint2 *>(bis + BI_CODES);
-#pragma unroll
-          for (int q = 0; q < 3; q++) fb[q] = bis[BI_FACE + (hax[q] >> 12)];
+          wa = *reinterpret_cast<const uint4 *>(bis);
+          wb = *reinterpret_cast<const uint4 *>(bis + 4);
+          wc = *reinterpret_cast<const uint2 *>(bis + 8);
         } else {
-          oa = __ldcg(reinterpret_cast<const uint2 *>(big + BI_OWN));
-          cw = __ldcg(reinterpret_cast<const uint2 *>(big + BI_CODES));
-#pragma unroll
-          for (int q = 0; q < 3; q++) fb[q] = __ldcg(big + BI_FACE + (hax[q] >> 12));
+          wa = __ldcg(reinterpret_cast<const uint4 *>(big));
+          wb = __ldcg(reinterpret_cast<const uint4 *>(big + 4));
+          wc = __ldcg(reinterpret_cast<const uint2 *>(big + 8));
         }
       }
-      const uint32_t own = oa.x, alpha = oa.y, c11 = cw.x, c12 = cw.y;
+      const uint32_t own = wa.x, alpha = wa.y, c11 = wa.z, c12 = wa.w;
+      const uint32_t fb[3] = {((hax[0] >> 12) & 1u) ? wb.y : wb.x, ((hax[1] >> 12) & 1u) ? wb.w : wb.z,
+                              ((hax[2] >> 12) & 1u) ? wc.y : wc.x};
       uint32_t addr[3];
       if (c11 == 0u && (c12 & 0xFFFFu) == 0u) {  // all six faces border same-level blocks
 #pragma unroll
@@ -994,7 +996,7 @@ __global__ void __launch_bounds__(256, NB ? MB : DCG_SOLVE_MINB)
     k_level_solve_batch(const __grid_constant__ SolveBatch P, int round, int sweeps, int tree) {
   __shared__ long long s_end[BMAX];
   __shared__ int s_lev[BMAX];
-  extern __shared__ uint32_t s_cache[];
+  extern __shared__ __align__(16) uint32_t s_cache[];
   const int t = threadIdx.x;
   if (t == 0) {
     long long acc = 0;
