@@ -100,7 +100,7 @@ struct dcg_batch {
       return fail(DCG_E_INVALID, "solve_barrier must be 0..7 (bit 0 two-level barrier, bit 1 coarsest-aligned rounds, "
                                  "bit 2 concurrent cascades of the two level counts)");
     if (!solve_variant_valid(tune.solve_cache))
-      return fail(DCG_E_INVALID, "solve_cache must be 0, 3, 4, 8 or a pipelined variant 16, 18, 19, 32, 34, 35, 64, 66");
+      return fail(DCG_E_INVALID, "solve_cache must be 0, 3, 4, 8 or a pipelined variant 16, 18, 19, 32, 34, 35, 64, 66, 83");
     for (int k = 0; k < 4; k++)
       if (tune.tile[k] != 1 && tune.tile[k] != 2 && tune.tile[k] != 4 && tune.tile[k] != 8)
         return fail(DCG_E_INVALID, "tiles must be 1 (staged), 2, 4 or 8 blocks");
@@ -548,7 +548,7 @@ struct dcg_batch {
     }
     // level solve: cache depth x CTAs per SM x barrier kind
     float best_solve = 1e30f;
-    for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66}) {
+    for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66, 83}) {
       const int occ = batch_solve_grid(sms, cache, 0) / std::max(1, sms);
       for (int k = 1; k <= occ; k++)
         for (int tb = 0; tb < 8; tb++) {  // bit 0: two-level barrier; bit 1: coarsest-aligned rounds;
@@ -575,7 +575,7 @@ struct dcg_batch {
       });
       float bms = base;
       best.round_ctas_per_sm[r] = 0;
-      for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66}) {
+      for (int cache : {0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66, 83}) {
         const int occ = batch_solve_grid(sms, cache, 0) / std::max(1, sms);
         std::vector<int> ks = {-8, -4, -2};  // k < 0: one CTA per -k SMs (small rounds)
         for (int k = 1; k <= occ; k++) ks.push_back(k);

@@ -76,7 +76,10 @@ struct dcg_sim {
   int ls_grid_staged = 0;  // CTAs of the staged solve
   // level solve of single simulations: pipelined staged sweeps, two tile buffers,
   // block descriptions cached in 3 x 8 KB of shared memory when they fit
-  static constexpr int kSolveVariant = 19;
+#ifndef DCG_SA_VARIANT
+#define DCG_SA_VARIANT 83
+#endif
+  static constexpr int kSolveVariant = DCG_SA_VARIANT;
   // batch members: p and p~ are slices of the batch's arenas, and the batch
   // steps the member (its own step and stage entry points are refused)
   float *ext_p = nullptr, *ext_pt = nullptr, *ext_div = nullptr;

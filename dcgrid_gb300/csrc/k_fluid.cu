@@ -806,7 +806,7 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
 // shared-memory pipe, which bounds the sweep, less than warp shuffles of the
 // same words do; measured on the 16-plume batch, so are the shuffles that
 // would replace the tile reads of the neighbours inside the block.
-template <int CACHE, int NB>
+template <int CACHE, int NB, int CLAIM>
 __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long long *s_end, const int *s_lev,
                                                 uint32_t *s_cache, long long total, unsigned nctas, int sweeps,
                                                 int tree) {
@@ -865,21 +865,22 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
     float2 *dstl = reinterpret_cast<float2 *>(dst) + lane;
     if (t == 0) s_next[(it + 1) & 1] = 0u;  // the next sweep's counter; its last use ended before the barrier
     unsigned *cnt = &s_next[it & 1];
-    // a warp claims DCG_PIPE_CLAIM consecutive CTA-local blocks per counter
-    // update (fewer shared atomics and broadcasts per block; two measured
-    // best: 3, 4 and 8 balance the warps worse)
+    // a warp claims CLAIM consecutive CTA-local blocks per counter update
+    // (fewer shared atomics and broadcasts per block; on the batch's large
+    // rounds two measured best, 3, 4 and 8 balance the warps worse; one for
+    // levels of a few blocks per warp, which the pairs would unbalance)
     int kpend = 0, npend = 0;
     auto issue = [&](int buf) {
       int k;
-      if (DCG_PIPE_CLAIM > 1 && npend > 0) {
+      if (CLAIM > 1 && npend > 0) {
         k = kpend++;
         npend--;
       } else {
         unsigned kk = 0;
-        if (lane == 0) kk = atomicAdd(cnt, (unsigned)DCG_PIPE_CLAIM);
+        if (lane == 0) kk = atomicAdd(cnt, (unsigned)CLAIM);
         k = (int)__shfl_sync(full, kk, 0);
         kpend = k + 1;
-        npend = DCG_PIPE_CLAIM - 1;
+        npend = CLAIM - 1;
       }
       const bool act = k < kcount;  // warp-uniform; a warp's claims only grow
       // the block's description: words 0-9 in three warp-wide broadcast
@@ -991,7 +992,7 @@ __device__ __forceinline__ void solve_pipelined(const SolveBatch &P, const long 
 // store per cell. Larger levels are swept one block per warp through a 6^3
 // shared-memory tile holding the block and its face halo. Arithmetic is that
 // of k_jacobi (identical results).
-template <int CACHE, int NB = 0, int MB = DCG_PIPE_MINB>
+template <int CACHE, int NB = 0, int MB = DCG_PIPE_MINB, int CLAIM = DCG_PIPE_CLAIM>
 __global__ void __launch_bounds__(256, NB ? MB : DCG_SOLVE_MINB)
     k_level_solve_batch(const __grid_constant__ SolveBatch P, int round, int sweeps, int tree) {
   __shared__ long long s_end[BMAX];
@@ -1063,7 +1064,7 @@ __global__ void __launch_bounds__(256, NB ? MB : DCG_SOLVE_MINB)
       if (it + 1 < sweeps) barrier();
     }
   } else if constexpr (NB > 0) {
-    solve_pipelined<CACHE, NB>(P, s_end, s_lev, s_cache, total, nctas, sweeps, tree);
+    solve_pipelined<CACHE, NB, CLAIM>(P, s_end, s_lev, s_cache, total, nctas, sweeps, tree);
   } else {
     // staged sweeps, one warp per block: per round each of the CTA's 8 warps
     // takes one block; its 64 cells and 96 face-halo cells go into a 6^3 tile
@@ -1896,22 +1897,24 @@ void launch_restrict_batch(RestrictBatch &P, cudaStream_t st) {
   if (acc > 0) k_restrict_batch<<<(unsigned)acc, 256, 0, st>>>(P);
 }
 
-template <int C, int NB, int MB = DCG_PIPE_MINB>
+template <int C, int NB, int MB = DCG_PIPE_MINB, int CLAIM = DCG_PIPE_CLAIM>
 static int solve_batch_occupancy() {
   // static + dynamic shared memory above 48 KB needs the opt-in
   const int smem = C * 8 * 256 * 4;
-  if (smem > 0 && cudaFuncSetAttribute(k_level_solve_batch<C, NB, MB>,
+  if (smem > 0 && cudaFuncSetAttribute(k_level_solve_batch<C, NB, MB, CLAIM>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
     return 0;
   int a = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_level_solve_batch<C, NB, MB>, 256, smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_level_solve_batch<C, NB, MB, CLAIM>, 256, smem) != cudaSuccess)
     return 0;
   return a;
 }
 // solve variants: cache depth 0, 3, 4 or 8 (cells per thread of the small-level
 // path; 8 KB of dynamic shared memory each); 16 + c: pipelined staged sweeps
-// with two tile buffers per warp (registers for 4 CTAs per SM), 32 + c: three
-// buffers, 64 + c: two buffers with registers for 5 CTAs per SM
+// with two tile buffers per warp (registers for 3 CTAs per SM, two blocks per
+// claim), 32 + c: three buffers, 64 + c: two buffers with registers for 5
+// CTAs per SM, 80 + c: two buffers, registers for 4 CTAs per SM, one block per
+// claim
 static int solve_occupancy(int cache) {
   switch (cache) {
     case 8: return solve_batch_occupancy<8, 0>();
@@ -1926,12 +1929,13 @@ static int solve_occupancy(int cache) {
     case 32 + 3: return solve_batch_occupancy<3, 3>();
     case 64: return solve_batch_occupancy<0, 2, 5>();
     case 64 + 2: return solve_batch_occupancy<2, 2, 5>();
+    case 80 + 3: return solve_batch_occupancy<3, 2, 4, 1>();
     default: return 0;
   }
 }
 bool solve_variant_valid(int cache) {
   return cache == 0 || cache == 3 || cache == 4 || cache == 8 || cache == 16 || cache == 18 || cache == 19 ||
-         cache == 32 || cache == 34 || cache == 35 || cache == 64 || cache == 66;
+         cache == 32 || cache == 34 || cache == 35 || cache == 64 || cache == 66 || cache == 83;
 }
 int batch_solve_grid(int sms, int cache, int ctas_per_sm) {
   const int occ = solve_occupancy(cache);
@@ -1965,6 +1969,7 @@ void launch_level_solve_batch(const SolveBatch &P, int round, int sweeps, int gr
     case 35: cudaLaunchKernelEx(&cfg, k_level_solve_batch<3, 3>, P, round, sweeps, tree); break;
     case 64: cudaLaunchKernelEx(&cfg, k_level_solve_batch<0, 2, 5>, P, round, sweeps, tree); break;
     case 66: cudaLaunchKernelEx(&cfg, k_level_solve_batch<2, 2, 5>, P, round, sweeps, tree); break;
+    case 83: cudaLaunchKernelEx(&cfg, k_level_solve_batch<3, 2, 4, 1>, P, round, sweeps, tree); break;
     default: cudaLaunchKernelEx(&cfg, k_level_solve_batch<0, 0>, P, round, sweeps, tree); break;
   }
 }

@@ -349,8 +349,10 @@ typedef struct {
   int32_t solve_cache;       /* cells per thread whose stencil the level solve keeps in
                                 shared memory: 0, 3, 4 or 8 (8 KB of shared memory each);
                                 16 + c (c = 0, 2, 3): pipelined staged sweeps, asynchronous
-                                copies into two tile buffers per warp; 32 + c: three;
-                                64 + c (c = 0, 2): two, registers for 5 CTAs per SM      */
+                                copies into two tile buffers per warp, registers for 3 CTAs
+                                per SM, two blocks per claim; 32 + c: three buffers;
+                                64 + c (c = 0, 2): two, registers for 5 CTAs per SM;
+                                83: two, registers for 4 CTAs per SM, one block per claim */
   int32_t solve_ctas_per_sm; /* CTAs per SM of the cooperative solve (0 = occupancy limit) */
   int32_t solve_barrier;     /* bit 0: grid barrier between sweeps, 0 flat, 1 two-level;
                                 bit 1: cascade round r solves every member's level
