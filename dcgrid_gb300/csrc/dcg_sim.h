@@ -75,11 +75,13 @@ struct dcg_sim {
   int ls_epoch = 3;
   int ls_grid_staged = 0;  // CTAs of the staged solve
   // level solve of single simulations: pipelined staged sweeps, two tile buffers,
-  // block descriptions cached in 3 x 8 KB of shared memory when they fit
-#ifndef DCG_SA_VARIANT
-#define DCG_SA_VARIANT 83
-#endif
-  static constexpr int kSolveVariant = DCG_SA_VARIANT;
+  // block descriptions cached in 3 x 8 KB of shared memory when they fit.
+  // Variant 19 (3 CTAs per SM, two blocks per claim); variant 83 (4 CTAs per
+  // SM, one block per claim) measured faster on the 256^3 cloud (1.85 against
+  // 1.93 ms per step) but slower on the 16 plumes stepped as single
+  // simulations (27.3 against 26.5 ms) and on the reference-default scenes
+  // (2.01 / 4.00 against 1.99 / 3.89 ms per step).
+  static constexpr int kSolveVariant = 19;
   // batch members: p and p~ are slices of the batch's arenas, and the batch
   // steps the member (its own step and stage entry points are refused)
   float *ext_p = nullptr, *ext_pt = nullptr, *ext_div = nullptr;
