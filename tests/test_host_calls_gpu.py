@@ -77,4 +77,4 @@ def test_kernel_timing_and_launch_counts():
         assert ms > 0 and nbytes > 0, which
     b = Batch(scenarios.plume_batch(2, 1, sizes=(16, 32), iters=10))
     t = b.get_tuning()
-    assert all(x in (1, 2, 4, 8) for x in t.tile) and t.solve_cache in (0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66)
+    assert all(x in (1, 2, 4, 8) for x in t.tile) and t.solve_cache in (0, 3, 4, 8, 16, 18, 19, 32, 34, 35, 64, 66, 83)
