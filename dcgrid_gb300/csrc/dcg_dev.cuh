@@ -101,7 +101,7 @@ struct Dev {
   double *red;             // reductions (stats)
   uint32_t *bar;           // grid barrier {arrivals, generation}
   uint32_t *epoch;         // per block: sweeps completed in the running level solve
-  uint32_t *binfo;         // level solve: block descriptions of the running level (13 words per block)
+  uint32_t *binfo;         // level solve: block descriptions of the running level (BI_WORDS words per block)
   float *rr, *e, *et;      // defect correction: residual, correction and its ping-pong plane
   double *dnorm;           // defect correction: FP64 ||r||^2, ||div||^2 per pass
 };

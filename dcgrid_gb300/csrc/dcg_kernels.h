@@ -81,7 +81,7 @@ struct SolveBatch {
   int n, maxtop, prolong, pad;
   float *p, *pt;
   const float *div;  // divergence arena (same layout as p)
-  uint32_t *binfo;   // block descriptions of the round's level, 13 words per level block
+  uint32_t *binfo;   // block descriptions of the round's level, BI_WORDS words per level block
   uint32_t *bar, *err;
   unsigned long long arena[BMAX];  // first cell of member s in the arenas
   Dev d[BMAX];

@@ -297,7 +297,7 @@ struct dcg_sim {
     if ((rc = alloc(&D.red, 32))) return rc;
     if ((rc = alloc(&D.bar, 64 + 32 * 18))) return rc;
     if ((rc = alloc(&D.epoch, B))) return rc;
-    if ((rc = alloc(&D.binfo, 13 * B))) return rc;
+    if ((rc = alloc(&D.binfo, (long long)BI_WORDS * B))) return rc;
     if (P.defect_passes > 0) {
       if (ext_rr) {
         D.rr = ext_rr;
